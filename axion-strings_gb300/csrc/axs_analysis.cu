@@ -1,0 +1,752 @@
+// Per-output analysis on the device: plaquette string finder, power spectra
+// after cuFFT, background means, energies and the finiteness check.
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+
+#include "axs_internal.h"
+
+namespace axs {
+
+static int grid_cap(int64_t work, int threads, int per_sm) {
+    int64_t want = (work + threads - 1) / threads;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)num_sms() * per_sm));
+}
+
+// ============================================================== string finder
+//
+// cores2 / cores3 (src/common/string_finding.cpp:3-86) flag a cell when the sum
+// of min(|dn|, 1-|dn|) over three edges of a plaquette exceeds
+// accept = (double)(0.5f*(1-thr/100.0f)), with n = (theta+pi)/(2 pi) and
+// theta = atan2(phi1, phi2). The decision is taken in two stages:
+//  1. FP32: n from atan2f, edges and sums in float. The error of each float
+//     sum against the exact double sum is below 2e-6 (|n| <= 1: atan2f within
+//     a few ulp of pi, n within 3e-7, each edge within 7e-7), so a float sum
+//     farther than kMargin = 1e-5 from accept decides the cell.
+//  2. Otherwise the cell is recomputed with the reference's double
+//     expressions in the reference's order (no contraction, IEEE division),
+//     which makes the decision bit-exact to the reference on a given theta.
+static constexpr float kMargin = 1e-5f;
+
+template <typename T, bool FROM_THETA>
+struct Corner {
+    const typename Cplx<T>::type *psi;
+    const double *theta;
+    __device__ __forceinline__ float nf(int64_t m) const {
+        float th;
+        if (FROM_THETA) th = (float)theta[m];
+        else { auto v = psi[m]; th = atan2f((float)v.x, (float)v.y); }
+        return fmaf(th, 0.15915494309189535f, 0.5f);
+    }
+    __device__ __forceinline__ double nd(int64_t m) const {
+        double th;
+        if (FROM_THETA) th = theta[m];
+        else { auto v = psi[m]; th = atan2((double)v.x, (double)v.y); }
+        return __ddiv_rn(__dadd_rn(th, 3.14159265358979323846), 6.28318530717958647692);   // (theta + M_PI)/(2*M_PI)
+    }
+};
+
+__device__ __forceinline__ float circf(float a, float b) {
+    float d = fabsf(b - a);
+    return fminf(d, 1.0f - d);
+}
+// std::min(abs(d), 1 - abs(d)) of string_finding.cpp:22-24 in double
+__device__ __forceinline__ double circd(double a, double b) {
+    double d = fabs(__dsub_rn(b, a));
+    double e = __dsub_rn(1.0, d);
+    return (e < d) ? e : d;
+}
+__device__ __forceinline__ double sum3(double a, double b, double c) { return __dadd_rn(__dadd_rn(a, b), c); }
+
+template <typename T, int ND, bool FROM_THETA>
+__global__ void __launch_bounds__(256) k_cores(const typename Cplx<T>::type *__restrict__ psi,
+                                               const double *__restrict__ theta, uint8_t *__restrict__ mask, int N,
+                                               int64_t len, double accept, unsigned long long *count) {
+    Corner<T, FROM_THETA> cn{psi, theta};
+    const float acc_f = (float)accept;
+    unsigned long long local = 0;
+    const int64_t NN = (int64_t)N * N;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        int flag;
+        if (ND == 2) {
+            int64_t i = m % N, j = m / N;
+            int64_t ip = i + 1 == N ? 0 : i + 1, jp = j + 1 == N ? 0 : j + 1;
+            int64_t o1 = m, o2 = ip + N * j, o3 = ip + N * jp, o4 = i + N * jp;
+            float s = circf(cn.nf(o1), cn.nf(o2)) + circf(cn.nf(o2), cn.nf(o3)) + circf(cn.nf(o3), cn.nf(o4));
+            if (s > acc_f + kMargin) flag = 1;
+            else if (s < acc_f - kMargin) flag = 0;
+            else {
+                double n1 = cn.nd(o1), n2 = cn.nd(o2), n3 = cn.nd(o3), n4 = cn.nd(o4);
+                flag = sum3(circd(n1, n2), circd(n2, n3), circd(n3, n4)) > accept;
+            }
+        } else {
+            // reference (i,j,k) = (z,y,x) here: i slowest, k fastest
+            int64_t x = m % N, y = (m / N) % N, z = m / NN;
+            int64_t xp = x + 1 == N ? 0 : x + 1, yp = y + 1 == N ? 0 : y + 1, zp = z + 1 == N ? 0 : z + 1;
+            int64_t o000 = m;                       // (i,j,k)
+            int64_t o100 = zp * NN + y * N + x;     // (i+1,j,k)
+            int64_t o110 = zp * NN + yp * N + x;    // (i+1,j+1,k)
+            int64_t o010 = z * NN + yp * N + x;     // (i,j+1,k)
+            int64_t o011 = z * NN + yp * N + xp;    // (i,j+1,k+1)
+            int64_t o001 = z * NN + y * N + xp;     // (i,j,k+1)
+            float f000 = cn.nf(o000), f100 = cn.nf(o100), f110 = cn.nf(o110), f010 = cn.nf(o010), f011 = cn.nf(o011),
+                  f001 = cn.nf(o001);
+            float e_000_100 = circf(f000, f100);
+            float e_011_001 = circf(f011, f001);
+            float sa = e_000_100 + circf(f100, f110) + circf(f110, f010);
+            float sb = e_000_100 + circf(f100, f011) + e_011_001;    // plaquette b, string_finding.cpp:54-57
+            float sc = circf(f000, f010) + circf(f010, f011) + e_011_001;
+            float mx = fmaxf(sa, fmaxf(sb, sc));
+            if (mx > acc_f + kMargin) flag = 1;
+            else if (mx < acc_f - kMargin) flag = 0;
+            else {
+                double d000 = cn.nd(o000), d100 = cn.nd(o100), d110 = cn.nd(o110), d010 = cn.nd(o010),
+                       d011 = cn.nd(o011), d001 = cn.nd(o001);
+                double ta = sum3(circd(d000, d100), circd(d100, d110), circd(d110, d010));
+                double tb = sum3(circd(d000, d100), circd(d100, d011), circd(d011, d001));
+                double tc = sum3(circd(d000, d010), circd(d010, d011), circd(d011, d001));
+                flag = (ta > accept || tb > accept || tc > accept);
+            }
+        }
+        mask[m] = (uint8_t)flag;
+        local += flag;
+    }
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
+}
+
+// ---- ordered compaction of the mask: chunk counts, scan, ordered write
+static constexpr int kChunk = 4096;   // cells per block
+
+__global__ void k_chunk_counts(const uint8_t *__restrict__ mask, int64_t len, int64_t *__restrict__ counts) {
+    int64_t base = (int64_t)blockIdx.x * kChunk;
+    int c = 0;
+    for (int q = threadIdx.x; q < kChunk; q += blockDim.x) {
+        int64_t m = base + q;
+        if (m < len) c += mask[m];
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    __shared__ int ws[8];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t s = 0;
+        for (int w = 0; w < 8; ++w) s += ws[w];
+        counts[blockIdx.x] = s;
+    }
+}
+
+// Exclusive scan of n counts by one block of 1024 threads.
+__global__ void k_scan(int64_t *__restrict__ counts, int64_t n, int64_t *__restrict__ total) {
+    __shared__ int64_t part[1024];
+    int64_t per = (n + 1023) / 1024;
+    int64_t b = threadIdx.x * per, e = b + per < n ? b + per : n;
+    int64_t s = 0;
+    for (int64_t i = b; i < e; ++i) s += counts[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t run = 0;
+        for (int i = 0; i < 1024; ++i) { int64_t v = part[i]; part[i] = run; run += v; }
+        *total = run;
+    }
+    __syncthreads();
+    int64_t run = part[threadIdx.x];
+    for (int64_t i = b; i < e; ++i) { int64_t v = counts[i]; counts[i] = run; run += v; }
+}
+
+__global__ void k_chunk_write(const uint8_t *__restrict__ mask, int64_t len, const int64_t *__restrict__ offsets,
+                              int64_t *__restrict__ list) {
+    __shared__ int wsum[8];
+    int64_t base = (int64_t)blockIdx.x * kChunk;
+    int64_t out = offsets[blockIdx.x];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int q0 = 0; q0 < kChunk; q0 += blockDim.x) {
+        int64_t m = base + q0 + threadIdx.x;
+        int f = (m < len) ? mask[m] : 0;
+        unsigned bal = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) wsum[w] = __popc(bal);
+        __syncthreads();
+        int before = 0, tot = 0;
+        for (int i = 0; i < 8; ++i) { if (i < w) before += wsum[i]; tot += wsum[i]; }
+        if (f) list[out + before + __popc(bal & ((1u << lane) - 1))] = m;
+        out += tot;
+        __syncthreads();
+    }
+}
+
+// Neighbouring-plaquette pairs of s_run.cpp:101-109 over the ascending list.
+__global__ void k_pairs2(const int64_t *__restrict__ list, int64_t n, int N, unsigned long long *pairs) {
+    unsigned long long local = 0;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q + 1 < n; q += stride) {
+        int64_t a = list[q], b = list[q + 1];
+        int64_t dx = (b % N) - (a % N), dy = (b / N) - (a / N);
+        local += (dy == 0 && dx == 1) || (dy == 1 && dx == 0);
+    }
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(pairs, local);
+}
+
+__global__ void k_positions(const int64_t *__restrict__ list, int64_t n, int N, int ndims, int32_t *__restrict__ pos) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t NN = (int64_t)N * N;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
+        int64_t m = list[q];
+        if (ndims == 2) { pos[2 * q] = (int32_t)(m % N); pos[2 * q + 1] = (int32_t)(m / N); }
+        else { pos[3 * q] = (int32_t)(m / NN); pos[3 * q + 1] = (int32_t)((m / N) % N); pos[3 * q + 2] = (int32_t)(m % N); }
+    }
+}
+
+static void ensure_mask(Lattice *L) {
+    if (!L->dmask) L->dmask = (uint8_t *)dalloc((size_t)L->length);
+    if (!L->dcount) L->dcount = (int64_t *)dalloc(4 * sizeof(int64_t));
+}
+
+// Build the ascending list of flagged offsets from the device mask.
+static int64_t compact(Lattice *L) {
+    int64_t nch = (L->length + kChunk - 1) / kChunk;
+    int64_t *counts = (int64_t *)dalloc((size_t)nch * sizeof(int64_t));
+    int64_t total = 0;
+    try {
+        k_chunk_counts<<<(unsigned)nch, 256, 0, L->stream>>>(L->dmask, L->length, counts);
+        k_scan<<<1, 1024, 0, L->stream>>>(counts, nch, L->dcount + 2);
+        count_launches(2);
+        AXS_CUDA(cudaGetLastError());
+        AXS_CUDA(cudaMemcpyAsync(&total, L->dcount + 2, sizeof(int64_t), cudaMemcpyDeviceToHost, L->stream));
+        AXS_CUDA(cudaStreamSynchronize(L->stream));
+        if (total > L->list_cap) {
+            dfree(L->dlist);
+            L->dlist = nullptr;
+            L->list_cap = std::max<int64_t>(total, 1024);
+            L->dlist = (int32_t *)dalloc((size_t)L->list_cap * sizeof(int64_t));
+        }
+        k_chunk_write<<<(unsigned)nch, 256, 0, L->stream>>>(L->dmask, L->length, counts, (int64_t *)L->dlist);
+        count_launches(1);
+        AXS_CUDA(cudaGetLastError());
+        AXS_CUDA(cudaStreamSynchronize(L->stream));
+    } catch (...) {
+        dfree(counts);
+        throw;
+    }
+    dfree(counts);
+    L->list_valid = true;
+    return total;
+}
+
+template <typename T>
+static void launch_cores(Lattice *L, bool from_theta, double accept, unsigned long long *cnt) {
+    typedef typename Cplx<T>::type C;
+    const C *psi = (const C *)L->psi[L->cur];
+    int g = grid_cap(L->length, 256, 8);
+    int N = L->p.N;
+    if (L->p.NDIMS == 2) {
+        if (from_theta) k_cores<T, 2, true><<<g, 256, 0, L->stream>>>(psi, L->dtheta, L->dmask, N, L->length, accept, cnt);
+        else k_cores<T, 2, false><<<g, 256, 0, L->stream>>>(psi, nullptr, L->dmask, N, L->length, accept, cnt);
+    } else {
+        if (from_theta) k_cores<T, 3, true><<<g, 256, 0, L->stream>>>(psi, L->dtheta, L->dmask, N, L->length, accept, cnt);
+        else k_cores<T, 3, false><<<g, 256, 0, L->stream>>>(psi, nullptr, L->dmask, N, L->length, accept, cnt);
+    }
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+
+void find_strings(Lattice *L, const double *theta_host, uint8_t *mask_host, int64_t *nplaq, int64_t *ncores) {
+    ensure_mask(L);
+    bool from_theta = theta_host != nullptr;
+    if (from_theta) {
+        if (!L->dtheta) L->dtheta = (double *)dalloc((size_t)L->length * sizeof(double));
+        AXS_CUDA(cudaMemcpyAsync(L->dtheta, theta_host, (size_t)L->length * sizeof(double), cudaMemcpyHostToDevice,
+                                 L->stream));
+    }
+    int thr = L->p.thr;
+    double accept = (double)(0.5f * (1.0f - thr / 100.0f));   // string_finding.cpp:8,40
+    AXS_CUDA(cudaMemsetAsync(L->dcount, 0, 2 * sizeof(int64_t), L->stream));
+    unsigned long long *cnt = (unsigned long long *)L->dcount;
+    if (L->esz == 4) launch_cores<float>(L, from_theta, accept, cnt);
+    else launch_cores<double>(L, from_theta, accept, cnt);
+    int64_t n = 0;
+    AXS_CUDA(cudaMemcpyAsync(&n, L->dcount, sizeof(int64_t), cudaMemcpyDeviceToHost, L->stream));
+    if (mask_host) AXS_CUDA(cudaMemcpyAsync(mask_host, L->dmask, (size_t)L->length, cudaMemcpyDeviceToHost, L->stream));
+    AXS_CUDA(cudaStreamSynchronize(L->stream));
+    L->last_nplaq = n;
+    L->list_valid = false;
+    int64_t cores = n;
+    if (L->p.NDIMS == 2) {
+        int64_t total = compact(L);
+        AXS_CUDA(cudaMemsetAsync(L->dcount + 1, 0, sizeof(int64_t), L->stream));
+        k_pairs2<<<grid_cap(std::max<int64_t>(total, 1), 256, 4), 256, 0, L->stream>>>(
+            (const int64_t *)L->dlist, total, L->p.N, (unsigned long long *)(L->dcount + 1));
+        count_launches(1);
+        AXS_CUDA(cudaGetLastError());
+        int64_t pairs = 0;
+        AXS_CUDA(cudaMemcpyAsync(&pairs, L->dcount + 1, sizeof(int64_t), cudaMemcpyDeviceToHost, L->stream));
+        AXS_CUDA(cudaStreamSynchronize(L->stream));
+        cores = n - pairs;
+    }
+    if (nplaq) *nplaq = n;
+    if (ncores) *ncores = cores;
+}
+
+void string_positions(Lattice *L, int32_t *pos, int64_t cap, int64_t *n) {
+    if (L->last_nplaq < 0) fail(AXS_ERR_STATE, "axs_string_positions needs a preceding axs_find_strings");
+    int64_t total = L->list_valid ? L->last_nplaq : compact(L);
+    if (n) *n = total;
+    int64_t w = std::min<int64_t>(cap, total);
+    if (w <= 0 || !pos) return;
+    int nd = L->p.NDIMS;
+    int32_t *dpos = (int32_t *)dalloc((size_t)w * nd * sizeof(int32_t));
+    try {
+        k_positions<<<grid_cap(w, 256, 4), 256, 0, L->stream>>>((const int64_t *)L->dlist, w, L->p.N, nd, dpos);
+        count_launches(1);
+        AXS_CUDA(cudaGetLastError());
+        AXS_CUDA(cudaMemcpyAsync(pos, dpos, (size_t)w * nd * sizeof(int32_t), cudaMemcpyDeviceToHost, L->stream));
+        AXS_CUDA(cudaStreamSynchronize(L->stream));
+    } catch (...) {
+        dfree(dpos);
+        throw;
+    }
+    dfree(dpos);
+}
+
+// ============================================================== spectra
+//
+// Real field -> R2C cuFFT -> binning. The half spectrum stands for the full
+// one: a mode with 0 < kx < N/2 represents itself and its mirror (weight 2);
+// kx = 0 is its own mirror set (weight 1); kx = N/2 lies at |n| >= N/2, which
+// both spectra drop or place in the last bin like any other mode.
+//
+// Binning is deterministic: each warp owns a shared-memory histogram it alone
+// updates; lanes holding the same bin are summed by a fixed shuffle tree; the
+// block adds its warps' histograms in order and writes one partial row; a
+// final kernel adds the rows in block order.
+
+struct RefBins {     // pk_estimation.cpp:92-100: floor(|n|) - 1 for 0 < |n| < N/2
+    int half;
+    __device__ __forceinline__ int bin(int64_t n2) const {
+        double kmag = sqrt((double)n2);
+        if (kmag == 0.0 || kmag >= half) return -1;
+        return (int)floor(kmag) - 1;
+    }
+};
+struct LogBins {     // nbins log-spaced in |n| between 1 and sqrt(d) N/2
+    const double *edge2;   // edge2[b] = t_b^2, b = 1..nbins-1
+    int nbins;
+    __device__ __forceinline__ int bin(int64_t n2) const {
+        if (n2 == 0) return -1;
+        double v = (double)n2;
+        int lo = 0, hi = nbins - 1;    // largest b with edge2[b] <= v (edge2[0] = 0)
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (edge2[mid] <= v) lo = mid; else hi = mid - 1;
+        }
+        return lo;
+    }
+};
+
+template <typename T, typename B>
+__global__ void __launch_bounds__(128) k_bin(const typename Cplx<T>::type *__restrict__ F, int N, int ndims, B binner,
+                                             int nbins, double *__restrict__ partials, unsigned long long *__restrict__ counts) {
+    extern __shared__ double hist[];   // [4 warps][2][nbins]
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < 4 * 2 * nbins; i += blockDim.x) hist[i] = 0.0;
+    __syncthreads();
+    double *hp = hist + (size_t)w * 2 * nbins;
+    double *hk = hp + nbins;
+    const int nh = N / 2 + 1;
+    const int64_t rows = ndims == 2 ? (int64_t)N : (int64_t)N * N;
+    const int64_t total = rows * nh;
+    const int64_t wstride = (int64_t)gridDim.x * 4 * 32;
+    const int64_t start = ((int64_t)blockIdx.x * 4 + w) * 32;
+    for (int64_t base = start; base < total; base += wstride) {
+        int64_t q = base + lane;
+        int b = -1;
+        double v = 0.0, kk = 0.0, wt = 0.0;
+        if (q < total) {
+            int ix = (int)(q % nh);
+            int64_t r = q / nh;
+            int64_t fx = ix;
+            int64_t n2;
+            if (ndims == 2) {
+                int64_t iy = r, fy = iy < N / 2 ? iy : iy - N;
+                n2 = fx * fx + fy * fy;
+            } else {
+                int64_t iz = r / N, iy = r % N;
+                int64_t fz = iz < N / 2 ? iz : iz - N, fy = iy < N / 2 ? iy : iy - N;
+                n2 = fx * fx + fy * fy + fz * fz;
+            }
+            b = binner.bin(n2);
+            if (b >= 0) {
+                auto f = F[q];
+                wt = (ix == 0 || 2 * ix == N) ? 1.0 : 2.0;
+                double re = (double)f.x, im = (double)f.y;
+                v = wt * (re * re + im * im);
+                kk = wt * sqrt((double)n2);
+            }
+        }
+        unsigned active = __ballot_sync(0xffffffffu, b >= 0);
+        while (active) {
+            const int leader = __ffs(active) - 1;
+            const int bl = __shfl_sync(0xffffffffu, b, leader);
+            const unsigned same = __ballot_sync(0xffffffffu, b == bl) & active;
+            const bool mine = (same >> lane) & 1u;
+            double sv = mine ? v : 0.0, sk = mine ? kk : 0.0;
+            unsigned long long sc = mine ? (unsigned long long)wt : 0ull;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sv += __shfl_xor_sync(0xffffffffu, sv, o);
+                sk += __shfl_xor_sync(0xffffffffu, sk, o);
+                sc += __shfl_xor_sync(0xffffffffu, sc, o);
+            }
+            if (lane == 0) {
+                hp[bl] += sv;
+                hk[bl] += sk;
+                atomicAdd(&counts[bl], sc);
+            }
+            active &= ~same;
+        }
+    }
+    __syncthreads();
+    for (int bn = threadIdx.x; bn < nbins; bn += blockDim.x) {
+        double sp = 0.0, sk = 0.0;
+        for (int ww = 0; ww < 4; ++ww) { sp += hist[(size_t)ww * 2 * nbins + bn]; sk += hist[(size_t)ww * 2 * nbins + nbins + bn]; }
+        partials[((int64_t)blockIdx.x * 2 + 0) * nbins + bn] = sp;
+        partials[((int64_t)blockIdx.x * 2 + 1) * nbins + bn] = sk;
+    }
+}
+
+__global__ void k_bin_final(const double *__restrict__ partials, int nblocks, int nbins, double *__restrict__ out) {
+    int bn = blockIdx.x * blockDim.x + threadIdx.x;
+    if (bn >= nbins) return;
+    double sp = 0.0, sk = 0.0;
+    for (int b = 0; b < nblocks; ++b) {
+        sp += partials[((int64_t)b * 2 + 0) * nbins + bn];
+        sk += partials[((int64_t)b * 2 + 1) * nbins + bn];
+    }
+    out[bn] = sp;
+    out[nbins + bn] = sk;
+}
+
+// gather a real field into fft_in: src = complex array, component comp
+template <typename T>
+__global__ void k_gather_real(const T *__restrict__ src_cplx, int comp, T *__restrict__ dst, int64_t len) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) dst[m] = src_cplx[2 * m + comp];
+}
+
+// f = |phi| dtheta/dtau = (psi2 pi1 - psi1 pi2) / (tau |psi|)
+template <typename T>
+__global__ void k_gather_axion(const typename Cplx<T>::type *__restrict__ psi, const typename Cplx<T>::type *__restrict__ pi,
+                               T *__restrict__ dst, int64_t len, double tau) {
+    const T itau = (T)(1.0 / tau);
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        auto a = psi[m];
+        auto p = pi[m];
+        T r = sqrt(a.x * a.x + a.y * a.y);
+        dst[m] = r > (T)0 ? (a.y * p.x - a.x * p.y) * itau / r : (T)0;
+    }
+}
+
+static void ensure_fft(Lattice *L) {
+    if (L->have_plan) return;
+    int N = L->p.N;
+    int64_t half = (L->p.NDIMS == 2 ? (int64_t)N : (int64_t)N * N) * (N / 2 + 1);
+    L->fft_in = dalloc((size_t)L->length * L->esz);
+    L->fft_out = dalloc((size_t)half * 2 * L->esz);
+    cufftType ty = L->esz == 4 ? CUFFT_R2C : CUFFT_D2Z;
+    if (L->p.NDIMS == 2) AXS_CUFFT(cufftPlan2d(&L->plan_r2c, N, N, ty));
+    else AXS_CUFFT(cufftPlan3d(&L->plan_r2c, N, N, N, ty));
+    AXS_CUFFT(cufftSetStream(L->plan_r2c, L->stream));
+    L->have_plan = true;
+}
+
+static void exec_r2c(Lattice *L) {
+    if (L->esz == 4) AXS_CUFFT(cufftExecR2C(L->plan_r2c, (cufftReal *)L->fft_in, (cufftComplex *)L->fft_out));
+    else AXS_CUFFT(cufftExecD2Z(L->plan_r2c, (cufftDoubleReal *)L->fft_in, (cufftDoubleComplex *)L->fft_out));
+}
+
+// Bin the current fft_out; returns per-bin sums (pk, |n|) and weighted counts.
+template <typename B>
+static void bin_spectrum(Lattice *L, const B &binner, int nbins, std::vector<double> &psum, std::vector<double> &nsum,
+                         std::vector<unsigned long long> &cnt) {
+    int N = L->p.N;
+    int64_t half = (L->p.NDIMS == 2 ? (int64_t)N : (int64_t)N * N) * (N / 2 + 1);
+    int nblk = grid_cap(half, 128, 2);
+    double *part = (double *)dalloc((size_t)nblk * 2 * nbins * sizeof(double) + (size_t)2 * nbins * sizeof(double) +
+                                    (size_t)nbins * sizeof(unsigned long long));
+    double *out = part + (size_t)nblk * 2 * nbins;
+    unsigned long long *dc = (unsigned long long *)(out + 2 * nbins);
+    try {
+        AXS_CUDA(cudaMemsetAsync(dc, 0, (size_t)nbins * sizeof(unsigned long long), L->stream));
+        size_t sm = (size_t)4 * 2 * nbins * sizeof(double);
+        if (sm > 48 * 1024) {
+            if (L->esz == 4) AXS_CUDA(cudaFuncSetAttribute(k_bin<float, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            else AXS_CUDA(cudaFuncSetAttribute(k_bin<double, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        }
+        if (L->esz == 4)
+            k_bin<float, B><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part, dc);
+        else
+            k_bin<double, B><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part, dc);
+        AXS_CUDA(cudaGetLastError());
+        k_bin_final<<<(nbins + 127) / 128, 128, 0, L->stream>>>(part, nblk, nbins, out);
+        AXS_CUDA(cudaGetLastError());
+        count_launches(2);
+        std::vector<double> h(2 * nbins);
+        cnt.assign(nbins, 0);
+        AXS_CUDA(cudaMemcpyAsync(h.data(), out, 2 * nbins * sizeof(double), cudaMemcpyDeviceToHost, L->stream));
+        AXS_CUDA(cudaMemcpyAsync(cnt.data(), dc, nbins * sizeof(unsigned long long), cudaMemcpyDeviceToHost, L->stream));
+        AXS_CUDA(cudaStreamSynchronize(L->stream));
+        psum.assign(h.begin(), h.begin() + nbins);
+        nsum.assign(h.begin() + nbins, h.end());
+    } catch (...) {
+        dfree(part);
+        throw;
+    }
+    dfree(part);
+}
+
+void powerspec(Lattice *L, int field, double *pk, double *ks, int *count) {
+    ensure_fft(L);
+    const void *src;
+    int comp = field & 1;
+    if (field <= AXS_PHI2) src = L->psi[L->cur];
+    else { launch_sync_pi(L); src = L->scratch; }
+    int g = grid_cap(L->length, 256, 16);
+    if (L->esz == 4) k_gather_real<float><<<g, 256, 0, L->stream>>>((const float *)src, comp, (float *)L->fft_in, L->length);
+    else k_gather_real<double><<<g, 256, 0, L->stream>>>((const double *)src, comp, (double *)L->fft_in, L->length);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+    exec_r2c(L);
+    int N = L->p.N;
+    int nb = N / 2;
+    std::vector<double> ps, ns;
+    std::vector<unsigned long long> c;
+    bin_spectrum(L, RefBins{N / 2}, nb, ps, ns, c);
+    float Lf = N * L->p.space_step;                     // pk_estimation.cpp:41
+    for (int b = 0; b < nb; ++b) {                      // pk_estimation.cpp:117-121 / 195-199
+        double k = ns[b] / (double)(int)c[b];
+        double p = ps[b];
+        if (L->p.NDIMS == 2) p /= 2.0f * M_PI * k;
+        else p /= 4.0f * M_PI * (k * k);
+        k *= 2.0f * M_PI / Lf;
+        pk[b] = p;
+        ks[b] = k;
+        count[b] = (int)c[b];
+    }
+}
+
+void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *count) {
+    if (nbins < 1) fail(AXS_ERR_ARG, "nbins must be >= 1");
+    ensure_fft(L);
+    launch_sync_pi(L);
+    int g = grid_cap(L->length, 256, 16);
+    if (L->esz == 4)
+        k_gather_axion<float><<<g, 256, 0, L->stream>>>((const float2 *)L->psi[L->cur], (const float2 *)L->scratch,
+                                                        (float *)L->fft_in, L->length, L->tau);
+    else
+        k_gather_axion<double><<<g, 256, 0, L->stream>>>((const double2 *)L->psi[L->cur], (const double2 *)L->scratch,
+                                                         (double *)L->fft_in, L->length, L->tau);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+    exec_r2c(L);
+    int d = L->p.NDIMS, N = L->p.N;
+    double ratio = sqrt((double)d) * (double)N / 2.0;
+    std::vector<double> e2(nbins, 0.0);
+    for (int b = 1; b < nbins; ++b) { double t = exp(log(ratio) * (double)b / (double)nbins); e2[b] = t * t; }
+    double *de2 = (double *)dalloc(nbins * sizeof(double));
+    std::vector<double> ps, ns;
+    std::vector<unsigned long long> c;
+    try {
+        AXS_CUDA(cudaMemcpyAsync(de2, e2.data(), nbins * sizeof(double), cudaMemcpyHostToDevice, L->stream));
+        bin_spectrum(L, LogBins{de2, nbins}, nbins, ps, ns, c);
+    } catch (...) {
+        dfree(de2);
+        throw;
+    }
+    dfree(de2);
+    double Ld = (double)N * (double)L->p.space_step;
+    double norm = pow(Ld, d) / pow((double)L->length, 2.0);
+    for (int b = 0; b < nbins; ++b) {
+        count[b] = (int64_t)c[b];
+        if (c[b]) {
+            kmean[b] = 2.0 * M_PI * (ns[b] / (double)c[b]) / Ld;
+            pk[b] = norm * ps[b] / (double)c[b];
+        } else {
+            kmean[b] = 0.0;
+            pk[b] = 0.0;
+        }
+    }
+}
+
+// ============================================================== reductions
+
+// Kahan-compensated accumulator for the FP32 path; plain double for FP64.
+template <typename T> struct Acc;
+template <> struct Acc<float> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        float y = x - c;
+        float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+template <> struct Acc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_background(const typename Cplx<T>::type *__restrict__ psi,
+                                                    const typename Cplx<T>::type *__restrict__ pi, int64_t len,
+                                                    double *__restrict__ partials) {
+    Acc<T> a[6];
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        auto f = psi[m];
+        auto p = pi[m];
+        a[0].add(f.x);
+        a[1].add(f.y);
+        a[2].add(p.x);
+        a[3].add(p.y);
+        a[4].add(fabs(atan2(f.x, f.y)));
+        a[5].add(sqrt(f.x * f.x + f.y * f.y));
+    }
+    double v[6];
+    for (int k = 0; k < 6; ++k) v[k] = a[k].value();
+    block_reduce_store<6>(v, partials);
+}
+
+template <typename T, int ND>
+__global__ void __launch_bounds__(256) k_energies(const typename Cplx<T>::type *__restrict__ psi,
+                                                  const typename Cplx<T>::type *__restrict__ pi, int N, int64_t len,
+                                                  double tau, double dx, double lam_eff, double *__restrict__ partials) {
+    Acc<T> a[3];
+    const T it = (T)(1.0 / tau), idx = (T)(1.0 / dx), q = (T)(0.25 * lam_eff);
+    const int64_t NN = (int64_t)N * N;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        auto s = psi[m];
+        auto p = pi[m];
+        T f1 = s.x * it, f2 = s.y * it;
+        T d1 = (p.x - f1) * it, d2 = (p.y - f2) * it;
+        a[0].add((T)0.5 * (d1 * d1 + d2 * d2));
+        int64_t x = m % N, nb[3];
+        int nn;
+        if (ND == 2) {
+            int64_t y = m / N;
+            nb[0] = m - x + (x + 1 == N ? 0 : x + 1);
+            nb[1] = (y + 1 == N ? 0 : y + 1) * N + x;
+            nn = 2;
+        } else {
+            int64_t y = (m / N) % N, z = m / NN;
+            nb[0] = m - x + (x + 1 == N ? 0 : x + 1);
+            nb[1] = z * NN + (y + 1 == N ? 0 : y + 1) * N + x;
+            nb[2] = (z + 1 == N ? 0 : z + 1) * NN + y * N + x;
+            nn = 3;
+        }
+        T g = 0;
+        for (int k = 0; k < nn; ++k) {
+            auto o = psi[nb[k]];
+            T g1 = (o.x * it - f1) * idx, g2 = (o.y * it - f2) * idx;
+            g += g1 * g1 + g2 * g2;
+        }
+        a[1].add((T)0.5 * g);
+        T r = f1 * f1 + f2 * f2 - (T)1;
+        a[2].add(q * r * r);
+    }
+    double v[3];
+    for (int k = 0; k < 3; ++k) v[k] = a[k].value();
+    block_reduce_store<3>(v, partials);
+}
+
+template <typename T>
+__global__ void k_finite(const T *__restrict__ a, int64_t n, int *flag) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int bad = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) bad |= !isfinite(a[i]);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+static double *ensure_partials(Lattice *L, int nblocks, int K) {
+    size_t need = (size_t)nblocks * K;
+    if (!L->dpartials || L->partials_cap < need) {
+        dfree(L->dpartials);
+        L->dpartials = nullptr;
+        L->partials_cap = std::max<size_t>(need, 4096);
+        L->dpartials = (double *)dalloc(L->partials_cap * sizeof(double));
+    }
+    return L->dpartials;
+}
+
+void background(Lattice *L, double out[6]) {
+    launch_sync_pi(L);
+    int g = reduce_grid(L->length);
+    double *part = ensure_partials(L, g, 6);
+    if (L->esz == 4) k_background<float><<<g, 256, 0, L->stream>>>((const float2 *)L->psi[L->cur], (const float2 *)L->scratch, L->length, part);
+    else k_background<double><<<g, 256, 0, L->stream>>>((const double2 *)L->psi[L->cur], (const double2 *)L->scratch, L->length, part);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+    double s[6];
+    sum_partials(part, g, 6, s, L->stream);
+    for (int k = 0; k < 6; ++k) out[k] = s[k] / (double)L->length;   // s_run.cpp:149
+}
+
+void energies(Lattice *L, double out[3]) {
+    launch_sync_pi(L);
+    int g = reduce_grid(L->length);
+    double *part = ensure_partials(L, g, 3);
+    double lam = (double)L->p.lambda * (L->p.prs ? 1.0 : L->tau * L->tau);
+    double dx = L->p.space_step;
+    if (L->esz == 4) {
+        if (L->p.NDIMS == 2) k_energies<float, 2><<<g, 256, 0, L->stream>>>((const float2 *)L->psi[L->cur], (const float2 *)L->scratch, L->p.N, L->length, L->tau, dx, lam, part);
+        else k_energies<float, 3><<<g, 256, 0, L->stream>>>((const float2 *)L->psi[L->cur], (const float2 *)L->scratch, L->p.N, L->length, L->tau, dx, lam, part);
+    } else {
+        if (L->p.NDIMS == 2) k_energies<double, 2><<<g, 256, 0, L->stream>>>((const double2 *)L->psi[L->cur], (const double2 *)L->scratch, L->p.N, L->length, L->tau, dx, lam, part);
+        else k_energies<double, 3><<<g, 256, 0, L->stream>>>((const double2 *)L->psi[L->cur], (const double2 *)L->scratch, L->p.N, L->length, L->tau, dx, lam, part);
+    }
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+    double s[3];
+    sum_partials(part, g, 3, s, L->stream);
+    for (int k = 0; k < 3; ++k) out[k] = s[k] / (double)L->length;
+}
+
+int check_finite(Lattice *L) {
+    int *flag = (int *)(L->dcount ? L->dcount : (L->dcount = (int64_t *)dalloc(4 * sizeof(int64_t)))) + 6;
+    AXS_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), L->stream));
+    int64_t n = L->length * 2;
+    int g = grid_cap(n, 256, 8);
+    if (L->esz == 4) {
+        k_finite<float><<<g, 256, 0, L->stream>>>((const float *)L->psi[L->cur], n, flag);
+        k_finite<float><<<g, 256, 0, L->stream>>>((const float *)L->pih, n, flag);
+    } else {
+        k_finite<double><<<g, 256, 0, L->stream>>>((const double *)L->psi[L->cur], n, flag);
+        k_finite<double><<<g, 256, 0, L->stream>>>((const double *)L->pih, n, flag);
+    }
+    AXS_CUDA(cudaGetLastError());
+    count_launches(2);
+    int h = 0;
+    AXS_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, L->stream));
+    AXS_CUDA(cudaStreamSynchronize(L->stream));
+    return h == 0;
+}
+
+void analysis_release(Lattice *L) {
+    dfree(L->dmask); L->dmask = nullptr;
+    dfree(L->dcount); L->dcount = nullptr;
+    dfree(L->dlist); L->dlist = nullptr;
+    dfree(L->dtheta); L->dtheta = nullptr;
+    dfree(L->fft_in); L->fft_in = nullptr;
+    dfree(L->fft_out); L->fft_out = nullptr;
+    if (L->have_plan) cufftDestroy(L->plan_r2c);
+    L->have_plan = false;
+    dfree(L->dpartials); L->dpartials = nullptr;
+}
+
+}  // namespace axs

@@ -1,0 +1,294 @@
+// Internal declarations shared by the CUDA translation units of libaxs.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/axs.h"
+
+namespace axs {
+
+// ---------------------------------------------------------------- errors
+struct Error {
+    int code;
+    std::string msg;
+};
+[[noreturn]] void fail(int code, const char *fmt, ...);
+void set_last_error(int code, const std::string &msg);
+void clear_last_error();
+
+#define AXS_CUDA(call)                                                                          \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess) ::axs::fail(AXS_ERR_CUDA, "%s failed: %s (%s:%d)", #call,       \
+                                           cudaGetErrorString(e_), __FILE__, __LINE__);         \
+    } while (0)
+#define AXS_CUFFT(call)                                                                         \
+    do {                                                                                        \
+        cufftResult r_ = (call);                                                                \
+        if (r_ != CUFFT_SUCCESS) ::axs::fail(AXS_ERR_CUDA, "%s failed: cufft status %d", #call, \
+                                             (int)r_);                                          \
+    } while (0)
+
+// Count of kernels launched by the library (host-side claim for benches).
+void count_launches(int64_t n);
+
+// Device error-flag bits (Lattice::derr).
+enum : int { DEVERR_TIMEOUT = 1 };
+
+// ---------------------------------------------------------------- lattice
+struct StepConfig {
+    int kind = 0;        // 0 = generic per-site kernel, 1 = TMA z-march kernel
+    int variant = 0;     // z-march template variant index
+    int zchunk = 64;     // planes per work item
+    int tx = 0;          // x tile (sites)
+    int ctas_per_sm = 0; // persistent grid occupancy
+    std::string describe() const;
+};
+
+struct Lattice;
+
+// One lattice's slot in a z-march launch (device-resident table entry).
+struct ZLat {
+    CUtensorMap tm_row[2];   // box {tx, 1, 1} over psi[b]
+    CUtensorMap tm_main[2];  // box {tx, TY, 1}
+    CUtensorMap tm_xh[2];    // box {16-byte halo, TY, 1}
+    void *psi[2];
+    void *pih;
+    double *clock;           // [2] tau at the parity of psi
+    int N, tx, ntx, nty, nzc;
+    int a_index;             // which of psi[0]/psi[1] is "current" at launch parity 0
+    int64_t item_base;
+    double dt, inv_dx2, lambda, T0sq3;
+    int prs, pad_;
+};
+
+struct GraphKey {
+    int nsteps, parity;
+    bool operator<(const GraphKey &o) const { return nsteps != o.nsteps ? nsteps < o.nsteps : parity < o.parity; }
+};
+
+struct Lattice {
+    axs_params p{};
+    int64_t length = 0;   // N^NDIMS
+    int esz = 8;          // bytes per real component (4 or 8)
+    void *psi[2] = {nullptr, nullptr};
+    void *pih = nullptr;  // half-step momentum (or pi_0 when fresh)
+    void *scratch = nullptr;  // complex, length sites: synchronised pi
+    double *dclock = nullptr; // [2]
+    int *derr = nullptr;      // device error flags
+    int *dcounter = nullptr;  // [2] work counters of the persistent step kernel
+    int cur = 0;              // psi[cur] holds the current field; dclock[cur] its tau
+    int fresh = 1;            // next step is the pure drift of a freshly set state
+    double tau = 1.0;
+    int64_t steps = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = true;
+    bool in_ensemble = false;
+    StepConfig cfg;
+    bool tuned = false;
+    // z-march launch table for this lattice alone
+    ZLat *dzlat = nullptr;
+    int zlat_variant = -1, zlat_tx = -1, zlat_zchunk = -1, zlat_a_index = 0;
+    int64_t zitems = 0;
+    // analysis buffers (lazily allocated)
+    uint8_t *dmask = nullptr;
+    int64_t *dcount = nullptr;       // [4] scratch counters
+    int32_t *dlist = nullptr;        // ascending flagged offsets (compacted)
+    int64_t list_cap = 0;
+    int64_t last_nplaq = -1;
+    bool list_valid = false;
+    double *dtheta = nullptr;        // caller theta upload
+    void *fft_in = nullptr;          // real, length
+    void *fft_out = nullptr;         // complex, R2C half spectrum
+    cufftHandle plan_r2c = 0;
+    bool have_plan = false;
+    double *dpartials = nullptr;     // reduction partials
+    size_t partials_cap = 0;
+    void *dstage = nullptr;          // transfer staging (length reals)
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+};
+
+struct Ensemble {
+    std::vector<Lattice *> members;
+    cudaStream_t stream = nullptr;
+    StepConfig cfg;
+    bool tuned = false;
+    ZLat *dzlat = nullptr;
+    int64_t zitems = 0;
+    int *dcounter = nullptr;
+    int *derr = nullptr;
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+};
+
+// ---- step module (axs_step.cu)
+void step_setup(Lattice *L);
+void step_release(Lattice *L);
+bool zmarch_supported(const axs_params &p);
+void lattice_step_once(Lattice *L);                   // one step (eager or inside capture)
+void lattice_evolve(Lattice *L, int nsteps);          // graph-cached
+void lattice_autotune(Lattice *L);
+void ensemble_setup(Ensemble *E);
+void ensemble_evolve(Ensemble *E, int nsteps);
+void ensemble_autotune(Ensemble *E);
+void launch_sync_pi(Lattice *L);                      // scratch <- pi_n
+void launch_laplacian(Lattice *L, int comp, double *dout);
+void launch_unpack(Lattice *L, const void *src, int which, int comp, void *dst_real, int dst_is_double);
+void launch_pack(Lattice *L, const void *src_real, int src_is_double, int which, int comp);
+void check_device_errors(Lattice *L);
+void check_device_error_flag(int *derr, cudaStream_t s);
+
+// ---- init module (axs_init.cu)
+void init_gaussian(Lattice *L, uint64_t seed, int thermal, double kcut);
+
+// ---- analysis module (axs_analysis.cu)
+void find_strings(Lattice *L, const double *theta_host, uint8_t *mask_host, int64_t *nplaq, int64_t *ncores);
+void string_positions(Lattice *L, int32_t *pos, int64_t cap, int64_t *n);
+void powerspec(Lattice *L, int field, double *pk, double *ks, int *count);
+void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *count);
+void background(Lattice *L, double out[6]);
+void energies(Lattice *L, double out[3]);
+int check_finite(Lattice *L);
+void analysis_release(Lattice *L);
+
+// helpers
+inline int64_t lattice_length(const axs_params &p) {
+    int64_t N = p.N;
+    return p.NDIMS == 3 ? N * N * N : N * N;
+}
+int num_sms();
+int reduce_grid(int64_t len);   // fixed grid size of the deterministic reductions
+// Sum per-block partials (nblocks x K, device) in block order on the host.
+void sum_partials(const double *dpart, int nblocks, int K, double *out, cudaStream_t s);
+void *dalloc(size_t bytes);
+void dfree(void *p);
+
+}  // namespace axs
+
+// ------------------------------------------------------------------ device side
+#ifdef __CUDACC__
+namespace axs {
+
+// Stencil coefficients of build_coefficient_matrix (src/standard/s_integrate.cpp:9-14):
+// float expressions, as the reference stores them.
+__host__ __device__ inline float stencil_coef(int setting, int ndims, int l) {
+    switch (setting) {
+    case 0: { const float c[2] = {-2.0f * ndims, 1.0f}; return c[l]; }
+    case 1: { const float c[3] = {-5.0f / 2.0f * ndims, 4.0f / 3.0f, -1.0f / 12.0f}; return c[l]; }
+    case 2: { const float c[4] = {-49.0f / 18.0f * ndims, 3.0f / 2.0f, -3.0f / 20.0f, 1.0f / 90.0f}; return c[l]; }
+    default: { const float c[5] = {-205.0f / 72.0f * ndims, 8.0f / 5.0f, -1.0f / 5.0f, 8.0f / 315.0f, -1.0f / 560.0f}; return c[l]; }
+    }
+}
+
+template <typename T> struct Cplx;
+template <> struct Cplx<float> { typedef float2 type; };
+template <> struct Cplx<double> { typedef double2 type; };
+
+// Per-step scalars, derived from tau (double) once per CTA.
+template <typename T> struct StepCoefs {
+    T dt;        // drift
+    T kdt_idx2;  // kick * 1/dx^2
+    T kdt_coef;  // kick * (-lambda / tau^(2 prs))
+    T c0;        // T0^2/3 - tau^2
+};
+
+template <typename T>
+__device__ __forceinline__ StepCoefs<T> make_coefs(double tau, double dt, double kick, double inv_dx2,
+                                                    double lambda, double T0sq3, int prs) {
+    StepCoefs<T> c;
+    double coef = prs ? -lambda / (tau * tau) : -lambda;
+    c.dt = (T)dt;
+    c.kdt_idx2 = (T)(kick * inv_dx2);
+    c.kdt_coef = (T)(kick * coef);
+    c.c0 = (T)(T0sq3 - tau * tau);
+    return c;
+}
+
+// Radius-1 stencil sum, fixed association order shared by every kernel:
+// ((x- + x+) + (y- + y+)) + (z- + z+), then centre * (-2 d) fused.
+template <typename T>
+__device__ __forceinline__ T lap7(T c, T xm, T xp, T ym, T yp, T zm, T zp) {
+    T s = ((xm + xp) + (ym + yp)) + (zm + zp);
+    return fma((T)-6, c, s);
+}
+template <typename T>
+__device__ __forceinline__ T lap5(T c, T xm, T xp, T ym, T yp) {
+    T s = (xm + xp) + (ym + yp);
+    return fma((T)-4, c, s);
+}
+
+// The fused kick + drift of one site. (a, b) = psi, L = stencil sums (not
+// divided by dx^2), (p1, p2) = half-step momentum in/out, (an, bn) = new psi.
+template <typename T>
+__device__ __forceinline__ void site_update(T a, T b, T L1, T L2, T &p1, T &p2, T &an, T &bn,
+                                            const StepCoefs<T> &c) {
+    T r = fma(a, a, fma(b, b, c.c0));
+    T g = c.kdt_coef * r;
+    p1 = fma(c.kdt_idx2, L1, fma(g, a, p1));
+    p2 = fma(c.kdt_idx2, L2, fma(g, b, p2));
+    an = fma(c.dt, p1, a);
+    bn = fma(c.dt, p2, b);
+}
+
+// Philox-4x32-10 (Salmon et al., SC'11) and Box-Muller; the deviate for
+// array a at offset m. Must agree with the oracle's definition.
+__device__ __forceinline__ double normal_draw(uint64_t seed, int a, int64_t m) {
+    uint32_t c0 = (uint32_t)((uint64_t)m & 0xffffffffu), c1 = (uint32_t)((uint64_t)m >> 32);
+    uint32_t c2 = (uint32_t)(a >> 1), c3 = 0x41585331u;
+    uint32_t k0 = (uint32_t)(seed & 0xffffffffu), k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    uint64_t b1 = (((uint64_t)c0 << 21) ^ (uint64_t)(c1 >> 11)) & ((1ull << 53) - 1);
+    uint64_t b2 = (((uint64_t)c2 << 21) ^ (uint64_t)(c3 >> 11)) & ((1ull << 53) - 1);
+    const double two_m53 = 1.1102230246251565404e-16;
+    double u1 = (double)(b1 + 1) * two_m53;
+    double u2 = (double)b2 * two_m53;
+    double rr = sqrt(-2.0 * log(u1));
+    double ang = 6.283185307179586232 * u2;
+    return (a & 1) ? rr * sin(ang) : rr * cos(ang);
+}
+
+__device__ __forceinline__ int64_t wrapi(int64_t i, int64_t N) { return i < 0 ? i + N : (i >= N ? i - N : i); }
+
+// Deterministic block reduction of K doubles (fixed shuffle tree, warps summed
+// in order); thread 0 writes the block's K partial sums to out[blockIdx.x*K+k].
+// blockDim.x must be 256.
+template <int K>
+__device__ __forceinline__ void block_reduce_store(double (&v)[K], double *out) {
+    __shared__ double red[8][K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double x = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        v[k] = x;
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) red[w][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double s = 0.0;
+            for (int i = 0; i < 8; ++i) s += red[i][k];
+            out[(int64_t)blockIdx.x * K + k] = s;
+        }
+    }
+    __syncthreads();
+}
+
+}  // namespace axs
+#endif

@@ -1,0 +1,1155 @@
+// Leapfrog evolution of the complex field: the fused kick/drift step and its
+// helpers. Replaces vvsl_field_rescaled (src/standard/s_integrate.cpp:305-348)
+// and the COO Laplacian it applies (s_integrate.cpp:5-149, 322-324).
+//
+// Formulation. The reference keeps (psi, pi, ker) and per step runs
+//   psi += dt (pi + dt/2 ker);  tau += dt;  ker' = lap(psi) + V'(psi, tau);
+//   pi  += dt/2 (ker + ker');   ker = ker'
+// with ker = 0 before the first step (calloc, s_run.cpp:44-47). Writing
+// pih = pi + dt/2 ker (the momentum at the half step) the same recursion is
+//   step 0:       psi_1 = psi_0 + dt pi_0,              pih_0 = pi_0
+//   step n >= 1:  pih_n = pih_{n-1} + dt K(psi_n, tau_n),  psi_{n+1} = psi_n + dt pih_n
+// so one pass reads psi (with stencil halo) and pih and writes both: 4 reals
+// read + 4 written per site, no stored kernel arrays. The synchronised
+// momentum the reference holds between steps is pi_n = pih_{n-1} + dt/2 K_n,
+// produced on demand by k_sync_pi.
+//
+// Device layout: psi and pih are complex-interleaved arrays (re = field 1,
+// im = field 2) in the reference's site order; psi is double-buffered.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include <functional>
+
+#include "axs_internal.h"
+
+namespace axs {
+
+// ============================================================== small kernels
+
+template <typename T>
+__global__ void k_drift0(const typename Cplx<T>::type *__restrict__ psi, typename Cplx<T>::type *__restrict__ out,
+                         const typename Cplx<T>::type *__restrict__ pih, const double *clock_in, double *clock_out,
+                         int64_t len, double dt) {
+    T d = (T)dt;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        auto a = psi[m];
+        auto p = pih[m];
+        a.x = fma(d, p.x, a.x);
+        a.y = fma(d, p.y, a.y);
+        out[m] = a;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *clock_out = *clock_in + dt;
+}
+
+// Stencil sums of both components at site m for radius R (R = 1 uses the
+// shared lap5/lap7 association order). Unscaled by 1/dx^2.
+template <typename T, int ND, int R>
+__device__ __forceinline__ void stencil_at(const typename Cplx<T>::type *__restrict__ psi, int64_t m, int N,
+                                           int setting, T &L1, T &L2, typename Cplx<T>::type &centre) {
+    typedef typename Cplx<T>::type C;
+    int64_t NN = (int64_t)N * N;
+    int64_t x, y, z = 0;
+    if (ND == 2) { x = m % N; y = m / N; }
+    else { x = m % N; y = (m / N) % N; z = m / NN; }
+    int64_t rowbase = m - x;                       // start of the x-row
+    int64_t planebase = (ND == 2) ? 0 : z * NN;    // start of the z-plane
+    C c = psi[m];
+    centre = c;
+    if (R == 1) {
+        C xm = psi[rowbase + wrapi(x - 1, N)], xp = psi[rowbase + wrapi(x + 1, N)];
+        C ym = psi[planebase + wrapi(y - 1, N) * N + x], yp = psi[planebase + wrapi(y + 1, N) * N + x];
+        if (ND == 2) {
+            L1 = lap5<T>(c.x, xm.x, xp.x, ym.x, yp.x);
+            L2 = lap5<T>(c.y, xm.y, xp.y, ym.y, yp.y);
+        } else {
+            int64_t yx = y * N + x;
+            C zm = psi[wrapi(z - 1, N) * NN + yx], zp = psi[wrapi(z + 1, N) * NN + yx];
+            L1 = lap7<T>(c.x, xm.x, xp.x, ym.x, yp.x, zm.x, zp.x);
+            L2 = lap7<T>(c.y, xm.y, xp.y, ym.y, yp.y, zm.y, zp.y);
+        }
+        return;
+    }
+    T a1 = (T)stencil_coef(setting, ND, 0) * c.x;
+    T a2 = (T)stencil_coef(setting, ND, 0) * c.y;
+#pragma unroll
+    for (int l = 1; l <= R; ++l) {
+        C xm = psi[rowbase + wrapi(x - l, N)], xp = psi[rowbase + wrapi(x + l, N)];
+        C ym = psi[planebase + wrapi(y - l, N) * N + x], yp = psi[planebase + wrapi(y + l, N) * N + x];
+        T s1 = (xm.x + xp.x) + (ym.x + yp.x), s2 = (xm.y + xp.y) + (ym.y + yp.y);
+        if (ND == 3) {
+            int64_t yx = y * N + x;
+            C zm = psi[wrapi(z - l, N) * NN + yx], zp = psi[wrapi(z + l, N) * NN + yx];
+            s1 = s1 + (zm.x + zp.x);
+            s2 = s2 + (zm.y + zp.y);
+        }
+        T cl = (T)stencil_coef(setting, ND, l);
+        a1 = fma(cl, s1, a1);
+        a2 = fma(cl, s2, a2);
+    }
+    L1 = a1;
+    L2 = a2;
+}
+
+// One step, one thread per site (grid-stride). Used for 2D, stencil radii
+// 2..4 and lattice shapes the z-march kernel does not tile.
+template <typename T, int ND, int R>
+__global__ void __launch_bounds__(256) k_step_generic(const typename Cplx<T>::type *__restrict__ psi,
+                                                      typename Cplx<T>::type *__restrict__ out,
+                                                      typename Cplx<T>::type *__restrict__ pih,
+                                                      const double *clock_in, double *clock_out, int N, int64_t len,
+                                                      double dt, double inv_dx2, double lambda, double T0sq3, int prs,
+                                                      int setting) {
+    double tau = *clock_in;
+    StepCoefs<T> c = make_coefs<T>(tau, dt, dt, inv_dx2, lambda, T0sq3, prs);
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        T L1, L2;
+        typename Cplx<T>::type ctr;
+        stencil_at<T, ND, R>(psi, m, N, setting, L1, L2, ctr);
+        auto p = pih[m];
+        typename Cplx<T>::type o;
+        site_update<T>(ctr.x, ctr.y, L1, L2, p.x, p.y, o.x, o.y, c);
+        pih[m] = p;
+        out[m] = o;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *clock_out = tau + dt;
+}
+
+// Synchronised momentum pi_n = pih_{n-1} + dt/2 K(psi_n, tau_n) into `dst`.
+template <typename T, int ND, int R>
+__global__ void k_sync_pi(const typename Cplx<T>::type *__restrict__ psi, const typename Cplx<T>::type *__restrict__ pih,
+                          typename Cplx<T>::type *__restrict__ dst, const double *clock, int N, int64_t len, double dt,
+                          double inv_dx2, double lambda, double T0sq3, int prs, int setting) {
+    StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs);
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        T L1, L2;
+        typename Cplx<T>::type ctr;
+        stencil_at<T, ND, R>(psi, m, N, setting, L1, L2, ctr);
+        auto p = pih[m];
+        T r = fma(ctr.x, ctr.x, fma(ctr.y, ctr.y, c.c0));
+        T g = c.kdt_coef * r;
+        p.x = fma(c.kdt_idx2, L1, fma(g, ctr.x, p.x));
+        p.y = fma(c.kdt_idx2, L2, fma(g, ctr.y, p.y));
+        dst[m] = p;
+    }
+}
+
+// (1/dx^2) * stencil of one component, in double.
+template <typename T, int ND, int R>
+__global__ void k_laplacian(const typename Cplx<T>::type *__restrict__ psi, double *__restrict__ out, int comp, int N,
+                            int64_t len, double inv_dx2, int setting) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        T L1, L2;
+        typename Cplx<T>::type ctr;
+        stencil_at<T, ND, R>(psi, m, N, setting, L1, L2, ctr);
+        out[m] = inv_dx2 * (double)(comp ? L2 : L1);
+    }
+}
+
+// Real host-order array <-> one component of a complex device array.
+template <typename T, typename S>
+__global__ void k_pack(const S *__restrict__ src, T *__restrict__ dst_cplx, int comp, int64_t len) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride)
+        dst_cplx[2 * m + comp] = (T)src[m];
+}
+template <typename T, typename S>
+__global__ void k_unpack(const T *__restrict__ src_cplx, S *__restrict__ dst, int comp, int64_t len) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride)
+        dst[m] = (S)src_cplx[2 * m + comp];
+}
+
+// ============================================================== z-march kernel
+//
+// 3D, radius 1. A work item is (lattice, x-y tile of tx * TY sites, z-chunk).
+// A CTA marches its tile through the z-chunk keeping the psi planes z-1, z,
+// z+1 in a ring of S shared-memory slots. Each plane (tile plus one-row y halo
+// and 16-byte x halo, periodic) arrives by 3-5 TMA tensor loads completing on
+// the slot's mbarrier; thread 0 refills a slot as soon as the CTA has finished
+// with the plane in it, so S-3 planes are in flight ahead of the consumer.
+// pih streams through registers one plane ahead. CTAs are persistent and take
+// items from a global counter in z-chunk-major order, so tiles that share
+// halo rows run at the same time and meet their halos in L2.
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: gives up after ~2^31 SM cycles (about a second).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > (1ll << 31)) return false;
+    }
+    return true;
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { typedef float4 type; };
+template <> struct Vec16<double> { typedef double2 type; };
+
+template <typename T, int TY, int TXMAX, int S>
+struct ZCfg {
+    static constexpr int CS = 2 * (int)sizeof(T);             // bytes per complex site
+    static constexpr int VS = 16 / CS;                        // sites per 16-byte vector
+    static constexpr int EU = CS / 8;                         // tensor-map elements per site
+    static constexpr int NT = 256;
+    static constexpr int MAXV = (TXMAX * TY / VS + NT - 1) / NT;
+    static constexpr int C_BYTES = (TY + 2) * TXMAX * CS;
+    static constexpr int H_BYTES = TY * 16;                   // one x-halo strip
+    static constexpr int H_PAD = (H_BYTES + 127) / 128 * 128; // strips start 128-byte aligned
+    static constexpr int SLOT = ((C_BYTES + 2 * H_PAD) + 127) / 128 * 128;
+    static constexpr int SMEM = S * SLOT + 128;               // + mbarriers and item broadcast
+};
+
+template <typename T, int TY, int TXMAX, int S>
+__global__ void __launch_bounds__(256) k_zmarch(const ZLat *__restrict__ lats, int nlat, int64_t total_items,
+                                                int *counters, int parity, int *derr) {
+    typedef ZCfg<T, TY, TXMAX, S> K;
+    typedef typename Cplx<T>::type C;
+    typedef typename Vec16<T>::type V;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * K::SLOT);
+    volatile int64_t *item_bc = reinterpret_cast<volatile int64_t *>(smem + S * K::SLOT + 64);
+    const int tid = threadIdx.x;
+
+    (void)parity;
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    // counters[0]: next work item; counters[1]: CTAs finished. The last CTA
+    // to finish zeroes both, so every launch starts from a clean counter.
+    int64_t qbase = 0;   // loads issued by this CTA before the current item
+    for (;;) {
+        if (tid == 0) *item_bc = (int64_t)atomicAdd(&counters[0], 1);
+        __syncthreads();
+        const int64_t item = *item_bc;
+        if (item >= total_items) break;
+        // ---- decode the item
+        int li = 0;
+        while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+        const ZLat &Lt = lats[li];
+        const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
+        const int64_t local = item - Lt.item_base;
+        const int ncols = ntx * nty;
+        const int zq = (int)(local / ncols), col = (int)(local % ncols);
+        const int x0 = (col % ntx) * tx, y0 = (col / ntx) * TY;
+        const int za = (int)((int64_t)zq * N / nzc), zb = (int)((int64_t)(zq + 1) * N / nzc);
+        const int T_steps = zb - za;
+        const int nload = T_steps + 2;
+        const int bin = Lt.a_index ^ parity;   // input psi buffer / clock slot
+        C *psi_out = reinterpret_cast<C *>(Lt.psi[bin ^ 1]);
+        C *pih = reinterpret_cast<C *>(Lt.pih);
+        const double tau = Lt.clock[bin];
+        const StepCoefs<T> cf = make_coefs<T>(tau, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs);
+        if (local == 0 && tid == 0) Lt.clock[bin ^ 1] = tau + Lt.dt;   // tau += dt, s_integrate.cpp:317
+        const bool xhalo = tx < N;
+        const uint32_t slot_bytes_tx = (uint32_t)((TY + 2) * tx * K::CS + (xhalo ? 2 * K::H_BYTES : 0));
+
+        auto issue = [&](int64_t q) {   // load q of the CTA stream = plane za-1+(q-qbase)
+            const int i = (int)(q - qbase);
+            int z = za - 1 + i;
+            z = z < 0 ? z + N : (z >= N ? z - N : z);
+            const int s = (int)(q % S);
+            unsigned char *slot = smem + s * K::SLOT;
+            const uint32_t bar = smem_u32(&bars[s]);
+            mbar_expect_tx(bar, slot_bytes_tx);
+            const int ym = y0 == 0 ? N - 1 : y0 - 1;
+            const int yp = (y0 + TY == N) ? 0 : y0 + TY;
+            tma_load_3d(smem_u32(slot), &Lt.tm_row[bin], x0 * K::EU, ym, z, bar);
+            tma_load_3d(smem_u32(slot + tx * K::CS), &Lt.tm_main[bin], x0 * K::EU, y0, z, bar);
+            tma_load_3d(smem_u32(slot + (TY + 1) * tx * K::CS), &Lt.tm_row[bin], x0 * K::EU, yp, z, bar);
+            if (xhalo) {
+                const int xl = (x0 - K::VS + N) % N, xr = (x0 + tx) % N;
+                tma_load_3d(smem_u32(slot + K::C_BYTES), &Lt.tm_xh[bin], xl * K::EU, y0, z, bar);
+                tma_load_3d(smem_u32(slot + K::C_BYTES + K::H_PAD), &Lt.tm_xh[bin], xr * K::EU, y0, z, bar);
+            }
+        };
+
+        int64_t issued = qbase;
+        if (tid == 0) {
+            const int64_t lim = qbase + min(nload, S);
+            for (; issued < lim; ++issued) issue(issued);
+        }
+        const int nvx = tx / K::VS;
+        const int nvec = nvx * TY;
+        // prefetch pih for the first plane
+        V pcur[K::MAXV];
+#pragma unroll
+        for (int k = 0; k < K::MAXV; ++k) {
+            const int v = tid + k * K::NT;
+            if (v < nvec) {
+                const int yy = v / nvx, xx = (v % nvx) * K::VS;
+                const int64_t off = ((int64_t)za * N + (y0 + yy)) * N + (x0 + xx);
+                pcur[k] = *reinterpret_cast<const V *>(&pih[off]);
+            }
+        }
+        bool ok = true, aborted = false;
+        for (int t = 0; t < T_steps; ++t) {
+            const int z = za + t;
+            // planes z-1, z, z+1 = loads qbase+t, +t+1, +t+2
+            if (t == 0) {
+                ok = ok && mbar_wait_bounded(smem_u32(&bars[(qbase) % S]), (uint32_t)(((qbase) / S) & 1));
+                ok = ok && mbar_wait_bounded(smem_u32(&bars[(qbase + 1) % S]), (uint32_t)(((qbase + 1) / S) & 1));
+            }
+            const int64_t qn = qbase + t + 2;
+            ok = ok && mbar_wait_bounded(smem_u32(&bars[qn % S]), (uint32_t)((qn / S) & 1));
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) atomicOr(derr, DEVERR_TIMEOUT);
+                aborted = true;
+                break;
+            }
+            const C *Cm = reinterpret_cast<const C *>(smem + ((qbase + t) % S) * K::SLOT);
+            const C *Cz = reinterpret_cast<const C *>(smem + ((qbase + t + 1) % S) * K::SLOT);
+            const C *Cp = reinterpret_cast<const C *>(smem + ((qbase + t + 2) % S) * K::SLOT);
+            const C *Lh = reinterpret_cast<const C *>(smem + ((qbase + t + 1) % S) * K::SLOT + K::C_BYTES);
+            const C *Rh = reinterpret_cast<const C *>(smem + ((qbase + t + 1) % S) * K::SLOT + K::C_BYTES + K::H_PAD);
+            V pnext[K::MAXV];
+#pragma unroll
+            for (int k = 0; k < K::MAXV; ++k) {
+                const int v = tid + k * K::NT;
+                if (v < nvec && t + 1 < T_steps) {
+                    const int yy = v / nvx, xx = (v % nvx) * K::VS;
+                    const int64_t off = ((int64_t)(z + 1) * N + (y0 + yy)) * N + (x0 + xx);
+                    pnext[k] = *reinterpret_cast<const V *>(&pih[off]);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < K::MAXV; ++k) {
+                const int v = tid + k * K::NT;
+                if (v >= nvec) continue;
+                const int yy = v / nvx, xx = (v % nvx) * K::VS;
+                const int r = (1 + yy) * tx + xx;
+                C ctr[K::VS], up[K::VS], dn[K::VS], zm[K::VS], zp[K::VS];
+                *reinterpret_cast<V *>(ctr) = *reinterpret_cast<const V *>(&Cz[r]);
+                *reinterpret_cast<V *>(up) = *reinterpret_cast<const V *>(&Cz[r - tx]);
+                *reinterpret_cast<V *>(dn) = *reinterpret_cast<const V *>(&Cz[r + tx]);
+                *reinterpret_cast<V *>(zm) = *reinterpret_cast<const V *>(&Cm[r]);
+                *reinterpret_cast<V *>(zp) = *reinterpret_cast<const V *>(&Cp[r]);
+                C left, right;
+                if (xx > 0) left = Cz[r - 1];
+                else left = xhalo ? Lh[yy * K::VS + K::VS - 1] : Cz[(1 + yy) * tx + tx - 1];
+                if (xx + K::VS < tx) right = Cz[r + K::VS];
+                else right = xhalo ? Rh[yy * K::VS] : Cz[(1 + yy) * tx];
+                T pv[2 * K::VS];
+                *reinterpret_cast<V *>(pv) = pcur[k];
+                C outv[K::VS];
+#pragma unroll
+                for (int j = 0; j < K::VS; ++j) {
+                    const C xm = (j == 0) ? left : ctr[j - 1];
+                    const C xp = (j == K::VS - 1) ? right : ctr[j + 1];
+                    const T L1 = lap7<T>(ctr[j].x, xm.x, xp.x, up[j].x, dn[j].x, zm[j].x, zp[j].x);
+                    const T L2 = lap7<T>(ctr[j].y, xm.y, xp.y, up[j].y, dn[j].y, zm[j].y, zp[j].y);
+                    site_update<T>(ctr[j].x, ctr[j].y, L1, L2, pv[2 * j], pv[2 * j + 1], outv[j].x, outv[j].y, cf);
+                }
+                const int64_t off = ((int64_t)z * N + (y0 + yy)) * N + (x0 + xx);
+                *reinterpret_cast<V *>(&pih[off]) = *reinterpret_cast<V *>(pv);
+                *reinterpret_cast<V *>(&psi_out[off]) = *reinterpret_cast<V *>(outv);
+            }
+#pragma unroll
+            for (int k = 0; k < K::MAXV; ++k) pcur[k] = pnext[k];
+            __syncthreads();   // every thread is done with plane z-1's slot
+            if (tid == 0) {
+                const int64_t dead = (t == T_steps - 1) ? qbase + nload : qbase + t + 1;
+                const int64_t lim = min(qbase + nload, dead + S);
+                for (; issued < lim; ++issued) issue(issued);
+            }
+        }
+        if (aborted) {
+            // Wait (bounded) for this CTA's copies still in flight, then stop.
+            if (tid == 0) {
+                for (int64_t q = qbase; q < issued; ++q) mbar_wait_bounded(smem_u32(&bars[q % S]), (uint32_t)((q / S) & 1));
+            }
+            __syncthreads();
+            break;
+        }
+        qbase += nload;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&counters[1], 1) == (int)gridDim.x - 1) {
+            counters[0] = 0;
+            counters[1] = 0;
+            __threadfence();
+        }
+    }
+}
+
+// ============================================================== host side
+
+static int g_num_sms = 0;
+int num_sms() {
+    if (!g_num_sms) {
+        int dev = 0;
+        AXS_CUDA(cudaGetDevice(&dev));
+        AXS_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+    }
+    return g_num_sms;
+}
+
+static int grid_for(int64_t len, int threads = 256) {
+    int64_t want = (len + threads - 1) / threads;
+    int64_t cap = (int64_t)num_sms() * 16;
+    return (int)std::max<int64_t>(1, std::min(want, cap));
+}
+
+std::string StepConfig::describe() const {
+    char b[160];
+    if (kind == 0) snprintf(b, sizeof b, "generic per-site kernel");
+    else snprintf(b, sizeof b, "TMA z-march variant %d, tx=%d, zchunk=%d, %d CTA/SM", variant, tx, zchunk, ctas_per_sm);
+    return b;
+}
+
+// ---- z-march variants -------------------------------------------------------
+struct ZVariant {
+    int ty, txmax, slots;
+};
+static const ZVariant kZVariants[] = {
+    {8, 128, 4}, {8, 128, 5}, {16, 128, 4}, {4, 256, 4}, {8, 256, 4},
+};
+static const int kNumZVariants = sizeof(kZVariants) / sizeof(kZVariants[0]);
+
+// Sets the kernel's shared-memory attribute and caches its occupancy. Called
+// when a launch table is built, never inside a graph capture.
+template <typename T, int TY, int TXMAX, int S>
+static int prepare_zmarch_t() {
+    typedef ZCfg<T, TY, TXMAX, S> K;
+    static int occ = -1;
+    if (occ < 0) {
+        AXS_CUDA(cudaFuncSetAttribute(k_zmarch<T, TY, TXMAX, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
+        int o = 0;
+        AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_zmarch<T, TY, TXMAX, S>, K::NT, K::SMEM));
+        if (o < 1) fail(AXS_ERR_CUDA, "z-march kernel does not fit on an SM");
+        occ = o;
+    }
+    return occ;
+}
+
+template <typename T, int TY, int TXMAX, int S>
+static void launch_zmarch_t(const ZLat *d, int nlat, int64_t items, int *counters, int parity, int *derr,
+                            cudaStream_t st, int ctas_per_sm) {
+    typedef ZCfg<T, TY, TXMAX, S> K;
+    int occ = prepare_zmarch_t<T, TY, TXMAX, S>();
+    int per = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ) : occ;
+    int64_t grid = std::min<int64_t>((int64_t)per * num_sms(), items);
+    k_zmarch<T, TY, TXMAX, S><<<(int)grid, K::NT, K::SMEM, st>>>(d, nlat, items, counters, parity, derr);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+
+static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t items, int *counters, int parity,
+                          int *derr, cudaStream_t st, int ctas_per_sm) {
+#define AXS_ZV(I, TY, TX, S)                                                                                    \
+    case I:                                                                                                     \
+        if (esz == 4) launch_zmarch_t<float, TY, TX, S>(d, nlat, items, counters, parity, derr, st, ctas_per_sm); \
+        else launch_zmarch_t<double, TY, TX, S>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);         \
+        break;
+    switch (variant) {
+        AXS_ZV(0, 8, 128, 4)
+        AXS_ZV(1, 8, 128, 5)
+        AXS_ZV(2, 16, 128, 4)
+        AXS_ZV(3, 4, 256, 4)
+        AXS_ZV(4, 8, 256, 4)
+    default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
+    }
+#undef AXS_ZV
+}
+
+static void prepare_zmarch(int esz, int variant) {
+#define AXS_ZP(I, TY, TX, S)                                      \
+    case I:                                                       \
+        if (esz == 4) prepare_zmarch_t<float, TY, TX, S>();       \
+        else prepare_zmarch_t<double, TY, TX, S>();               \
+        break;
+    switch (variant) {
+        AXS_ZP(0, 8, 128, 4)
+        AXS_ZP(1, 8, 128, 5)
+        AXS_ZP(2, 16, 128, 4)
+        AXS_ZP(3, 4, 256, 4)
+        AXS_ZP(4, 8, 256, 4)
+    default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
+    }
+#undef AXS_ZP
+}
+
+// The tx a variant would use for an N (largest admissible divisor), or 0.
+static int variant_tx(const ZVariant &v, int N, int esz) {
+    int cs = 2 * esz;
+    int vs = 16 / cs;
+    int txmax = v.txmax;
+    if (esz == 8) txmax = std::min(txmax, 128);   // box inner dim: 2*tx doubles <= 256
+    if (N % v.ty != 0 || N < 4) return 0;
+    for (int tx = std::min(txmax, N); tx >= vs; --tx) {
+        if (N % tx) continue;
+        if (tx % vs) continue;
+        if ((tx * cs) % 128) continue;   // shared-memory destinations stay 128-byte aligned
+        return tx;
+    }
+    return 0;
+}
+
+bool zmarch_supported(const axs_params &p) {
+    if (p.NDIMS != 3 || p.stencil_setting != 0) return false;
+    int esz = p.precision == AXS_F32 ? 4 : 8;
+    for (int v = 0; v < kNumZVariants; ++v)
+        if (variant_tx(kZVariants[v], p.N, esz)) return true;
+    return false;
+}
+
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                     const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static PFN_encodeTiled get_encode() {
+    static PFN_encodeTiled fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void *f = nullptr;
+        AXS_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !f) fail(AXS_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+        fn = (PFN_encodeTiled)f;
+    }
+    return fn;
+}
+
+static void encode_map(CUtensorMap *m, void *base, int N, int esz, int box_x_sites, int box_y) {
+    // complex float sites as 8-byte elements; complex double as two 8-byte doubles
+    int eu = esz == 4 ? 1 : 2;
+    cuuint64_t dims[3] = {(cuuint64_t)N * eu, (cuuint64_t)N, (cuuint64_t)N};
+    cuuint64_t strides[2] = {(cuuint64_t)N * 2 * esz, (cuuint64_t)N * N * 2 * esz};
+    cuuint32_t box[3] = {(cuuint32_t)(box_x_sites * eu), (cuuint32_t)box_y, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = get_encode()(m, esz == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, base,
+                              dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) fail(AXS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+}
+
+// Fill the z-march table entry of lattice L for a variant; returns items.
+static int64_t fill_zlat(ZLat &z, Lattice *L, int variant, int zchunk, int64_t item_base) {
+    const ZVariant &v = kZVariants[variant];
+    int N = L->p.N;
+    int tx = variant_tx(v, N, L->esz);
+    if (!tx) fail(AXS_ERR_ARG, "z-march variant %d cannot tile N=%d", variant, N);
+    prepare_zmarch(L->esz, variant);
+    memset(&z, 0, sizeof z);
+    int vs = 16 / (2 * L->esz);
+    for (int b = 0; b < 2; ++b) {
+        encode_map(&z.tm_row[b], L->psi[b], N, L->esz, tx, 1);
+        encode_map(&z.tm_main[b], L->psi[b], N, L->esz, tx, v.ty);
+        encode_map(&z.tm_xh[b], L->psi[b], N, L->esz, vs, v.ty);
+        z.psi[b] = L->psi[b];
+    }
+    z.pih = L->pih;
+    z.clock = L->dclock;
+    z.N = N;
+    z.tx = tx;
+    z.ntx = N / tx;
+    z.nty = N / v.ty;
+    z.nzc = std::max(1, N / std::max(1, zchunk));
+    z.a_index = L->cur;
+    z.item_base = item_base;
+    z.dt = (double)L->p.time_step;
+    double dx = (double)L->p.space_step;
+    z.inv_dx2 = 1.0 / (dx * dx);
+    z.lambda = (double)L->p.lambda;
+    double T0 = (double)L->p.T_initial;
+    z.T0sq3 = (T0 * T0) / 3.0;
+    z.prs = L->p.prs;
+    return (int64_t)z.ntx * z.nty * z.nzc;
+}
+
+static void ensure_single_table(Lattice *L) {
+    ZLat z;
+    int64_t items = fill_zlat(z, L, L->cfg.variant, L->cfg.zchunk, 0);
+    if (!L->dzlat) L->dzlat = (ZLat *)dalloc(sizeof(ZLat));
+    AXS_CUDA(cudaMemcpyAsync(L->dzlat, &z, sizeof(ZLat), cudaMemcpyHostToDevice, L->stream));
+    AXS_CUDA(cudaStreamSynchronize(L->stream));
+    L->zlat_variant = L->cfg.variant;
+    L->zlat_zchunk = L->cfg.zchunk;
+    L->zlat_a_index = L->cur;
+    L->zitems = items;
+    L->cfg.tx = z.tx;
+}
+
+void step_setup(Lattice *L) {
+    L->cfg = StepConfig();
+    L->cfg.kind = 0;
+    if (zmarch_supported(L->p)) {
+        // default before tuning: first variant that tiles N
+        for (int v = 0; v < kNumZVariants; ++v)
+            if (variant_tx(kZVariants[v], L->p.N, L->esz)) { L->cfg.kind = 1; L->cfg.variant = v; break; }
+        L->cfg.zchunk = 64;
+    }
+    L->dcounter = (int *)dalloc(2 * sizeof(int));
+    AXS_CUDA(cudaMemsetAsync(L->dcounter, 0, 2 * sizeof(int), L->stream));
+}
+
+void step_release(Lattice *L) {
+    for (auto &g : L->graphs) cudaGraphExecDestroy(g.second);
+    L->graphs.clear();
+    dfree(L->dzlat);
+    L->dzlat = nullptr;
+    dfree(L->dcounter);
+    L->dcounter = nullptr;
+}
+
+template <typename T, int ND, int R>
+static void launch_generic_t(Lattice *L, const double *cin, double *cout) {
+    typedef typename Cplx<T>::type C;
+    const axs_params &p = L->p;
+    double dx = p.space_step;
+    double T0 = p.T_initial;
+    k_step_generic<T, ND, R><<<grid_for(L->length), 256, 0, L->stream>>>(
+        (const C *)L->psi[L->cur], (C *)L->psi[L->cur ^ 1], (C *)L->pih, cin, cout, p.N, L->length,
+        (double)p.time_step, 1.0 / (dx * dx), (double)p.lambda, (T0 * T0) / 3.0, p.prs, p.stencil_setting);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+
+template <typename T>
+static void launch_generic_dispatch(Lattice *L, const double *cin, double *cout) {
+    int R = L->p.stencil_setting + 1;
+    if (L->p.NDIMS == 2) {
+        switch (R) {
+        case 1: launch_generic_t<T, 2, 1>(L, cin, cout); break;
+        case 2: launch_generic_t<T, 2, 2>(L, cin, cout); break;
+        case 3: launch_generic_t<T, 2, 3>(L, cin, cout); break;
+        default: launch_generic_t<T, 2, 4>(L, cin, cout); break;
+        }
+    } else {
+        switch (R) {
+        case 1: launch_generic_t<T, 3, 1>(L, cin, cout); break;
+        case 2: launch_generic_t<T, 3, 2>(L, cin, cout); break;
+        case 3: launch_generic_t<T, 3, 3>(L, cin, cout); break;
+        default: launch_generic_t<T, 3, 4>(L, cin, cout); break;
+        }
+    }
+}
+
+// One step of a lattice (the handle's bookkeeping advances here; the kernels
+// may be running later inside a graph).
+void lattice_step_once(Lattice *L) {
+    const double *cin = L->dclock + L->cur;
+    double *cout = L->dclock + (L->cur ^ 1);
+    if (L->fresh) {
+        if (L->esz == 4)
+            k_drift0<float><<<grid_for(L->length), 256, 0, L->stream>>>((const float2 *)L->psi[L->cur],
+                                                                         (float2 *)L->psi[L->cur ^ 1],
+                                                                         (const float2 *)L->pih, cin, cout, L->length,
+                                                                         (double)L->p.time_step);
+        else
+            k_drift0<double><<<grid_for(L->length), 256, 0, L->stream>>>((const double2 *)L->psi[L->cur],
+                                                                          (double2 *)L->psi[L->cur ^ 1],
+                                                                          (const double2 *)L->pih, cin, cout,
+                                                                          L->length, (double)L->p.time_step);
+        AXS_CUDA(cudaGetLastError());
+        count_launches(1);
+        L->fresh = 0;
+    } else if (L->cfg.kind == 1) {
+        if (!L->dzlat || L->zlat_variant != L->cfg.variant || L->zlat_zchunk != L->cfg.zchunk) ensure_single_table(L);
+        // the table is built with a_index = cur at build time; parity is relative to it
+        int parity = L->cur ^ L->zlat_a_index;
+        launch_zmarch(L->esz, L->cfg.variant, L->dzlat, 1, L->zitems, L->dcounter, parity, L->derr, L->stream,
+                      L->cfg.ctas_per_sm);
+    } else {
+        if (L->esz == 4) launch_generic_dispatch<float>(L, cin, cout);
+        else launch_generic_dispatch<double>(L, cin, cout);
+    }
+    L->cur ^= 1;
+    L->tau = L->tau + (double)L->p.time_step;
+    L->steps += 1;
+}
+
+}  // namespace axs
+
+namespace axs {
+
+// ---------------------------------------------------------------- graphs
+static thread_local bool t_capturing = false;
+static int64_t g_launches = 0;
+void count_launches(int64_t n) {
+    if (!t_capturing) __atomic_fetch_add(&g_launches, n, __ATOMIC_RELAXED);
+}
+int64_t total_launches() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+
+static bool env_flag(const char *name, bool dflt) {
+    const char *v = getenv(name);
+    if (!v || !*v) return dflt;
+    return !(v[0] == '0' || v[0] == 'n' || v[0] == 'N' || v[0] == 'f' || v[0] == 'F');
+}
+
+static void prepare_tables(Lattice *L) {
+    if (L->cfg.kind == 1 && (!L->dzlat || L->zlat_variant != L->cfg.variant || L->zlat_zchunk != L->cfg.zchunk))
+        ensure_single_table(L);
+}
+
+template <typename StepFn>
+static cudaGraphExec_t capture(cudaStream_t st, StepFn fn) {
+    cudaGraph_t g = nullptr;
+    AXS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    t_capturing = true;
+    try {
+        fn();
+    } catch (...) {
+        t_capturing = false;
+        cudaStreamEndCapture(st, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    t_capturing = false;
+    AXS_CUDA(cudaStreamEndCapture(st, &g));
+    cudaGraphExec_t ex = nullptr;
+    AXS_CUDA(cudaGraphInstantiate(&ex, g, 0));
+    cudaGraphDestroy(g);
+    return ex;
+}
+
+void lattice_evolve(Lattice *L, int nsteps) {
+    if (nsteps <= 0) return;
+    if (!L->tuned) {
+        if (env_flag("AXS_AUTOTUNE", true)) lattice_autotune(L);
+        L->tuned = true;
+    }
+    if (L->fresh) {
+        lattice_step_once(L);
+        if (--nsteps == 0) return;
+    }
+    prepare_tables(L);
+    if (nsteps < 2 || !env_flag("AXS_GRAPHS", true)) {
+        for (int s = 0; s < nsteps; ++s) lattice_step_once(L);
+        return;
+    }
+    GraphKey key{nsteps, L->cur};
+    auto it = L->graphs.find(key);
+    if (it == L->graphs.end()) {
+        int cur0 = L->cur;
+        double tau0 = L->tau;
+        int64_t steps0 = L->steps;
+        cudaGraphExec_t ex = capture(L->stream, [&] {
+            for (int s = 0; s < nsteps; ++s) lattice_step_once(L);
+        });
+        L->cur = cur0;
+        L->tau = tau0;
+        L->steps = steps0;
+        it = L->graphs.insert(std::make_pair(key, ex)).first;
+    }
+    AXS_CUDA(cudaGraphLaunch(it->second, L->stream));
+    count_launches(nsteps);
+    for (int s = 0; s < nsteps; ++s) L->tau = L->tau + (double)L->p.time_step;
+    L->cur ^= (nsteps & 1);
+    L->steps += nsteps;
+}
+
+static void clear_graphs(std::map<GraphKey, cudaGraphExec_t> &g) {
+    for (auto &e : g) cudaGraphExecDestroy(e.second);
+    g.clear();
+}
+
+// ---------------------------------------------------------------- autotune
+struct TuneKey {
+    int n, ndims, esz, stencil;
+    bool operator<(const TuneKey &o) const {
+        if (n != o.n) return n < o.n;
+        if (ndims != o.ndims) return ndims < o.ndims;
+        if (esz != o.esz) return esz < o.esz;
+        return stencil < o.stencil;
+    }
+};
+static std::map<TuneKey, StepConfig> g_tune_cache;
+
+static double time_launches(cudaStream_t st, int reps, const std::function<void()> &fn) {
+    cudaEvent_t a, b;
+    AXS_CUDA(cudaEventCreate(&a));
+    AXS_CUDA(cudaEventCreate(&b));
+    fn();
+    fn();
+    AXS_CUDA(cudaEventRecord(a, st));
+    for (int r = 0; r < reps; ++r) fn();
+    AXS_CUDA(cudaEventRecord(b, st));
+    AXS_CUDA(cudaEventSynchronize(b));
+    float ms = 0;
+    AXS_CUDA(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms / reps;
+}
+
+// Candidate steps run with dt = 0: psi_out = psi + 0*pih and pih + 0*K are
+// bit-identical copies, so the state (and tau) is unchanged.
+void lattice_autotune(Lattice *L) {
+    L->tuned = true;
+    // AXS_FORCE_CONFIG="kind,variant,zchunk" pins a configuration (tests use it
+    // to show that every configuration gives bit-identical results).
+    const char *force = getenv("AXS_FORCE_CONFIG");
+    if (force && *force) {
+        StepConfig c;
+        int k = 0, v = 0, zc = 64;
+        if (sscanf(force, "%d,%d,%d", &k, &v, &zc) >= 1) {
+            c.kind = (k == 1 && zmarch_supported(L->p) && v >= 0 && v < kNumZVariants &&
+                      variant_tx(kZVariants[v], L->p.N, L->esz)) ? 1 : 0;
+            c.variant = c.kind ? v : 0;
+            c.zchunk = zc > 0 ? zc : 64;
+            L->cfg = c;
+            L->zlat_variant = -1;
+            clear_graphs(L->graphs);
+            return;
+        }
+    }
+    TuneKey key{L->p.N, L->p.NDIMS, L->esz, L->p.stencil_setting};
+    auto hit = g_tune_cache.find(key);
+    if (hit != g_tune_cache.end()) {
+        if (hit->second.kind != L->cfg.kind || hit->second.variant != L->cfg.variant || hit->second.zchunk != L->cfg.zchunk)
+            clear_graphs(L->graphs);
+        L->cfg = hit->second;
+        return;
+    }
+    if (!zmarch_supported(L->p)) {
+        L->cfg.kind = 0;
+        g_tune_cache[key] = L->cfg;
+        return;
+    }
+    float dt_save = L->p.time_step;
+    L->p.time_step = 0.0f;
+    int reps = L->length >= (1 << 27) ? 4 : 10;
+    StepConfig best = L->cfg;
+    double best_ms = 1e30;
+    int cur_save = L->cur;
+    std::vector<std::pair<StepConfig, double>> log;
+    // generic kernel
+    {
+        StepConfig c;
+        c.kind = 0;
+        double ms = time_launches(L->stream, reps, [&] {
+            const double *cin = L->dclock + L->cur;
+            double *cout = L->dclock + (L->cur ^ 1);
+            if (L->esz == 4) launch_generic_dispatch<float>(L, cin, cout);
+            else launch_generic_dispatch<double>(L, cin, cout);
+            L->cur ^= 1;
+        });
+        log.push_back({c, ms});
+        if (ms < best_ms) { best_ms = ms; best = c; }
+    }
+    const int zchunks[] = {32, 64, 128};
+    for (int v = 0; v < kNumZVariants; ++v) {
+        if (!variant_tx(kZVariants[v], L->p.N, L->esz)) continue;
+        for (int zc : zchunks) {
+            if (zc > L->p.N) continue;
+            StepConfig c;
+            c.kind = 1;
+            c.variant = v;
+            c.zchunk = zc;
+            L->cfg = c;
+            ensure_single_table(L);   // built with dt = 0
+            double ms = time_launches(L->stream, reps, [&] {
+                int parity = L->cur ^ L->zlat_a_index;
+                launch_zmarch(L->esz, v, L->dzlat, 1, L->zitems, L->dcounter, parity, L->derr, L->stream, 0);
+                L->cur ^= 1;
+            });
+            c.tx = L->cfg.tx;
+            log.push_back({c, ms});
+            if (ms < best_ms) { best_ms = ms; best = c; }
+        }
+    }
+    L->p.time_step = dt_save;
+    // dt = 0 steps copied psi back and forth; values are identical, but keep the
+    // buffer the caller had as current.
+    if (L->cur != cur_save) {
+        AXS_CUDA(cudaMemcpyAsync(L->psi[cur_save], L->psi[L->cur], (size_t)L->length * 2 * L->esz,
+                                 cudaMemcpyDeviceToDevice, L->stream));
+        AXS_CUDA(cudaMemcpyAsync(L->dclock + cur_save, L->dclock + L->cur, sizeof(double), cudaMemcpyDeviceToDevice,
+                                 L->stream));
+        L->cur = cur_save;
+    }
+    check_device_errors(L);
+    L->cfg = best;
+    L->zlat_variant = -1;   // rebuild the table with the real dt before the next step
+    clear_graphs(L->graphs);
+    g_tune_cache[key] = best;
+    if (env_flag("AXS_TUNE_LOG", false)) {
+        for (auto &e : log) fprintf(stderr, "[axs autotune N=%d] %-60s %.4f ms\n", L->p.N, e.first.describe().c_str(), e.second);
+        fprintf(stderr, "[axs autotune N=%d] chose %s\n", L->p.N, best.describe().c_str());
+    }
+}
+
+// ---------------------------------------------------------------- ensemble
+static bool ensemble_variant_ok(Ensemble *E, int v) {
+    for (Lattice *m : E->members)
+        if (m->p.NDIMS != 3 || m->p.stencil_setting != 0 || !variant_tx(kZVariants[v], m->p.N, m->esz)) return false;
+    return true;
+}
+
+static void ensemble_table(Ensemble *E, float dt_override, bool use_override) {
+    std::vector<int> order(E->members.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return E->members[a]->length > E->members[b]->length; });
+    std::vector<ZLat> tab(order.size());
+    int64_t base = 0;
+    for (size_t k = 0; k < order.size(); ++k) {
+        Lattice *m = E->members[order[k]];
+        float dt = m->p.time_step;
+        if (use_override) m->p.time_step = dt_override;
+        base += fill_zlat(tab[k], m, E->cfg.variant, E->cfg.zchunk, base);
+        m->p.time_step = dt;
+        m->zlat_a_index = m->cur;
+    }
+    if (!E->dzlat) E->dzlat = (ZLat *)dalloc(sizeof(ZLat) * std::max<size_t>(1, tab.size()));
+    AXS_CUDA(cudaMemcpyAsync(E->dzlat, tab.data(), sizeof(ZLat) * tab.size(), cudaMemcpyHostToDevice, E->stream));
+    AXS_CUDA(cudaStreamSynchronize(E->stream));
+    E->zitems = base;
+}
+
+void ensemble_setup(Ensemble *E) {
+    E->cfg = StepConfig();
+    E->cfg.kind = 0;
+    for (int v = 0; v < kNumZVariants; ++v)
+        if (ensemble_variant_ok(E, v)) { E->cfg.kind = 1; E->cfg.variant = v; E->cfg.zchunk = 64; break; }
+    E->dcounter = (int *)dalloc(2 * sizeof(int));
+    E->derr = (int *)dalloc(sizeof(int));
+    AXS_CUDA(cudaMemsetAsync(E->dcounter, 0, 2 * sizeof(int), E->stream));
+    AXS_CUDA(cudaMemsetAsync(E->derr, 0, sizeof(int), E->stream));
+    if (E->cfg.kind == 1) ensemble_table(E, 0.f, false);
+}
+
+static bool ensemble_table_valid(Ensemble *E) {
+    if (!E->dzlat) return false;
+    // every member must still sit at the same parity relative to its table entry
+    int d = E->members[0]->cur ^ E->members[0]->zlat_a_index;
+    for (Lattice *m : E->members)
+        if ((m->cur ^ m->zlat_a_index) != d) return false;
+    return true;
+}
+
+static void ensemble_step_once(Ensemble *E) {
+    if (E->cfg.kind == 1) {
+        int parity = E->members[0]->cur ^ E->members[0]->zlat_a_index;
+        launch_zmarch(E->members[0]->esz, E->cfg.variant, E->dzlat, (int)E->members.size(), E->zitems, E->dcounter,
+                      parity, E->derr, E->stream, E->cfg.ctas_per_sm);
+        for (Lattice *m : E->members) {
+            m->cur ^= 1;
+            m->tau = m->tau + (double)m->p.time_step;
+            m->steps += 1;
+        }
+    } else {
+        for (Lattice *m : E->members) lattice_step_once(m);
+    }
+}
+
+void ensemble_autotune(Ensemble *E) {
+    E->tuned = true;
+    if (E->cfg.kind != 1) return;
+    std::vector<int> cur_save;
+    for (Lattice *m : E->members) cur_save.push_back(m->cur);
+    int reps = 6;
+    StepConfig best = E->cfg;
+    double best_ms = 1e30;
+    const int zchunks[] = {32, 64, 128};
+    for (int v = 0; v < kNumZVariants; ++v) {
+        if (!ensemble_variant_ok(E, v)) continue;
+        for (int zc : zchunks) {
+            StepConfig c;
+            c.kind = 1;
+            c.variant = v;
+            c.zchunk = zc;
+            E->cfg = c;
+            ensemble_table(E, 0.f, true);
+            double ms = time_launches(E->stream, reps, [&] {
+                int parity = E->members[0]->cur ^ E->members[0]->zlat_a_index;
+                launch_zmarch(E->members[0]->esz, v, E->dzlat, (int)E->members.size(), E->zitems, E->dcounter, parity,
+                              E->derr, E->stream, 0);
+                for (Lattice *m : E->members) m->cur ^= 1;
+            });
+            if (ms < best_ms) { best_ms = ms; best = c; }
+            if (env_flag("AXS_TUNE_LOG", false))
+                fprintf(stderr, "[axs autotune ensemble] %-60s %.4f ms\n", c.describe().c_str(), ms);
+        }
+    }
+    for (size_t i = 0; i < E->members.size(); ++i) {
+        Lattice *m = E->members[i];
+        if (m->cur != cur_save[i]) {
+            AXS_CUDA(cudaMemcpyAsync(m->psi[cur_save[i]], m->psi[m->cur], (size_t)m->length * 2 * m->esz,
+                                     cudaMemcpyDeviceToDevice, E->stream));
+            AXS_CUDA(cudaMemcpyAsync(m->dclock + cur_save[i], m->dclock + m->cur, sizeof(double),
+                                     cudaMemcpyDeviceToDevice, E->stream));
+            m->cur = cur_save[i];
+        }
+    }
+    check_device_error_flag(E->derr, E->stream);
+    E->cfg = best;
+    ensemble_table(E, 0.f, false);
+    clear_graphs(E->graphs);
+}
+
+void ensemble_evolve(Ensemble *E, int nsteps) {
+    if (nsteps <= 0) return;
+    for (Lattice *m : E->members)
+        if (m->fresh != E->members[0]->fresh || m->steps != E->members[0]->steps)
+            fail(AXS_ERR_STATE, "ensemble members are not at the same step");
+    if (!E->tuned) {
+        if (env_flag("AXS_AUTOTUNE", true)) ensemble_autotune(E);
+        E->tuned = true;
+    }
+    if (E->members[0]->fresh) {
+        for (Lattice *m : E->members) lattice_step_once(m);   // pure drift per member
+        if (--nsteps == 0) return;
+    }
+    if (E->cfg.kind == 1 && !ensemble_table_valid(E)) {
+        ensemble_table(E, 0.f, false);
+        clear_graphs(E->graphs);
+    }
+    if (E->cfg.kind != 1)
+        for (Lattice *m : E->members) prepare_tables(m);
+    if (nsteps < 2 || !env_flag("AXS_GRAPHS", true)) {
+        for (int s = 0; s < nsteps; ++s) ensemble_step_once(E);
+        return;
+    }
+    GraphKey key{nsteps, E->members[0]->cur ^ E->members[0]->zlat_a_index};
+    auto it = E->graphs.find(key);
+    if (it == E->graphs.end()) {
+        std::vector<int> cur0;
+        std::vector<double> tau0;
+        std::vector<int64_t> st0;
+        for (Lattice *m : E->members) { cur0.push_back(m->cur); tau0.push_back(m->tau); st0.push_back(m->steps); }
+        cudaGraphExec_t ex = capture(E->stream, [&] {
+            for (int s = 0; s < nsteps; ++s) ensemble_step_once(E);
+        });
+        for (size_t i = 0; i < E->members.size(); ++i) {
+            E->members[i]->cur = cur0[i];
+            E->members[i]->tau = tau0[i];
+            E->members[i]->steps = st0[i];
+        }
+        it = E->graphs.insert(std::make_pair(key, ex)).first;
+    }
+    AXS_CUDA(cudaGraphLaunch(it->second, E->stream));
+    count_launches(E->cfg.kind == 1 ? nsteps : (int64_t)nsteps * (int64_t)E->members.size());
+    for (Lattice *m : E->members) {
+        for (int s = 0; s < nsteps; ++s) m->tau = m->tau + (double)m->p.time_step;
+        m->cur ^= (nsteps & 1);
+        m->steps += nsteps;
+    }
+}
+
+// ---------------------------------------------------------------- helpers
+template <typename T, int ND, int R>
+static void sync_pi_t(Lattice *L) {
+    typedef typename Cplx<T>::type C;
+    double dx = L->p.space_step, T0 = L->p.T_initial;
+    k_sync_pi<T, ND, R><<<grid_for(L->length), 256, 0, L->stream>>>(
+        (const C *)L->psi[L->cur], (const C *)L->pih, (C *)L->scratch, L->dclock + L->cur, L->p.N, L->length,
+        (double)L->p.time_step, 1.0 / (dx * dx), (double)L->p.lambda, (T0 * T0) / 3.0, L->p.prs, L->p.stencil_setting);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+template <typename T>
+static void sync_pi_dispatch(Lattice *L) {
+    int R = L->p.stencil_setting + 1;
+    if (L->p.NDIMS == 2) {
+        if (R == 1) sync_pi_t<T, 2, 1>(L); else if (R == 2) sync_pi_t<T, 2, 2>(L); else if (R == 3) sync_pi_t<T, 2, 3>(L); else sync_pi_t<T, 2, 4>(L);
+    } else {
+        if (R == 1) sync_pi_t<T, 3, 1>(L); else if (R == 2) sync_pi_t<T, 3, 2>(L); else if (R == 3) sync_pi_t<T, 3, 3>(L); else sync_pi_t<T, 3, 4>(L);
+    }
+}
+void launch_sync_pi(Lattice *L) {
+    if (L->fresh) {   // pih holds pi_0 and the reference's ker_curr is zero
+        AXS_CUDA(cudaMemcpyAsync(L->scratch, L->pih, (size_t)L->length * 2 * L->esz, cudaMemcpyDeviceToDevice, L->stream));
+        return;
+    }
+    if (L->esz == 4) sync_pi_dispatch<float>(L);
+    else sync_pi_dispatch<double>(L);
+}
+
+template <typename T, int ND, int R>
+static void lap_t(Lattice *L, int comp, double *dout) {
+    typedef typename Cplx<T>::type C;
+    double dx = L->p.space_step;
+    k_laplacian<T, ND, R><<<grid_for(L->length), 256, 0, L->stream>>>((const C *)L->psi[L->cur], dout, comp, L->p.N,
+                                                                       L->length, 1.0 / (dx * dx), L->p.stencil_setting);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+template <typename T>
+static void lap_dispatch(Lattice *L, int comp, double *dout) {
+    int R = L->p.stencil_setting + 1;
+    if (L->p.NDIMS == 2) {
+        if (R == 1) lap_t<T, 2, 1>(L, comp, dout); else if (R == 2) lap_t<T, 2, 2>(L, comp, dout); else if (R == 3) lap_t<T, 2, 3>(L, comp, dout); else lap_t<T, 2, 4>(L, comp, dout);
+    } else {
+        if (R == 1) lap_t<T, 3, 1>(L, comp, dout); else if (R == 2) lap_t<T, 3, 2>(L, comp, dout); else if (R == 3) lap_t<T, 3, 3>(L, comp, dout); else lap_t<T, 3, 4>(L, comp, dout);
+    }
+}
+void launch_laplacian(Lattice *L, int comp, double *dout) {
+    if (L->esz == 4) lap_dispatch<float>(L, comp, dout);
+    else lap_dispatch<double>(L, comp, dout);
+}
+
+// which: 0 = current psi, 1 = pih
+void launch_pack(Lattice *L, const void *src_real, int src_is_double, int which, int comp) {
+    void *dst = which == 0 ? L->psi[L->cur] : L->pih;
+    int g = grid_for(L->length);
+    if (L->esz == 4) {
+        if (src_is_double) k_pack<float, double><<<g, 256, 0, L->stream>>>((const double *)src_real, (float *)dst, comp, L->length);
+        else k_pack<float, float><<<g, 256, 0, L->stream>>>((const float *)src_real, (float *)dst, comp, L->length);
+    } else {
+        if (src_is_double) k_pack<double, double><<<g, 256, 0, L->stream>>>((const double *)src_real, (double *)dst, comp, L->length);
+        else k_pack<double, float><<<g, 256, 0, L->stream>>>((const float *)src_real, (double *)dst, comp, L->length);
+    }
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+
+void launch_unpack(Lattice *L, const void *src, int which, int comp, void *dst_real, int dst_is_double) {
+    (void)which;
+    int g = grid_for(L->length);
+    if (L->esz == 4) {
+        if (dst_is_double) k_unpack<float, double><<<g, 256, 0, L->stream>>>((const float *)src, (double *)dst_real, comp, L->length);
+        else k_unpack<float, float><<<g, 256, 0, L->stream>>>((const float *)src, (float *)dst_real, comp, L->length);
+    } else {
+        if (dst_is_double) k_unpack<double, double><<<g, 256, 0, L->stream>>>((const double *)src, (double *)dst_real, comp, L->length);
+        else k_unpack<double, float><<<g, 256, 0, L->stream>>>((const double *)src, (float *)dst_real, comp, L->length);
+    }
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+
+void check_device_error_flag(int *derr, cudaStream_t s) {
+    int h = 0;
+    AXS_CUDA(cudaMemcpyAsync(&h, derr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    AXS_CUDA(cudaStreamSynchronize(s));
+    if (h & DEVERR_TIMEOUT) {
+        AXS_CUDA(cudaMemsetAsync(derr, 0, sizeof(int), s));
+        fail(AXS_ERR_TIMEOUT, "a step kernel gave up waiting for a TMA load; the step was not completed");
+    }
+}
+void check_device_errors(Lattice *L) { check_device_error_flag(L->derr, L->stream); }
+
+}  // namespace axs

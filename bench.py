@@ -1,0 +1,371 @@
+"""Benchmark of the standard-lattice evolution path on GB300.
+
+Metric: lattice site-updates per second of the fused leapfrog step (one step
+of one site: psi1, psi2, pi1, pi2 read and written once), with the fraction
+of the measured HBM copy bandwidth it represents.
+
+Headline workload: 3D N=1024^3, FP32 fields (FP64 time bookkeeping),
+7-point stencil, lambda=1, dx=0.5, dt=0.1, the unrescaled-coupling equation
+(prs=0, T0=0), flat k_cut=1 Gaussian start (seed 1). The state (2 x 8.6 GB
+psi buffers + 8.6 GB pi) is far larger than L2 (129 MB), so every step
+streams from HBM; no L2 flush is needed between steps.
+
+Also reported (extra keys): the plain FP64 step on the same lattice and
+start, the 96-member uneven batched ensemble, and the reference CPU path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+For N > 1 (torchrun), each rank runs an independent replica on its own GPU
+(the single-lattice path does not shard) and rank 0 prints
+the aggregate.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "axion-strings_gb300")
+
+N_MAIN = 1024
+BYTES_PER_SITE = {32: 32, 64: 64}     # psi1, psi2, pi1, pi2: one read + one write each
+ENSEMBLE_SIZES = (64, 96, 128, 160, 192)
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "of measured"
+    except Exception:
+        return 6800.0, "of fallback"
+
+
+# --------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------- dist
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+# --------------------------------------------------------------------- CPU baseline
+def cpu_port_rate(n=256, target_s=10.0, max_steps=200, min_steps=2):
+    """The oracle port of vvsl_field_rescaled (reference loop structure, FP32
+    data_t, OpenMP on all host cores) on an n^3 sample; site-updates/s."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    orc = oracle_lib.load()
+    p = oracle_lib.make_params(NDIMS=3, N=n, lam=1.0, T0=0.0, dx=0.5, dt=0.1, prs=0)
+    rng = np.random.default_rng(1)
+    f = [rng.standard_normal((n, n, n)).astype(np.float32) * 0.5 for _ in range(2)] + \
+        [np.zeros((n, n, n), dtype=np.float32) for _ in range(2)]
+    k = [np.zeros((n, n, n), dtype=np.float32) for _ in range(4)]
+    t = ctypes.c_float(1.0)
+    ptr = [a.ctypes.data for a in f + k]
+    step = lambda: orc.lib.orc_vvsl_step_f32(ctypes.byref(p), *ptr, ctypes.byref(t))
+    step()
+    t0 = time.perf_counter()
+    step()
+    one = time.perf_counter() - t0
+    steps = int(max(min_steps, min(max_steps, target_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = time.perf_counter() - t0
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return n ** 3 * steps / dt, steps, dt, threads
+
+
+# --------------------------------------------------------------------- GPU legs
+def load_axs():
+    sys.path.insert(0, PKG)
+    if not os.path.exists(os.path.join(PKG, "libaxs.so")):
+        sys.path.insert(0, ROOT)
+        import __graft_entry__
+        __graft_entry__.build()
+    import axs
+    return axs
+
+
+def main_params(axs, precision, n=N_MAIN):
+    return axs.default_params(NDIMS=3, N=n, lambda_=1.0, T_initial=0.0, space_step=0.5, time_step=0.1,
+                              precision=precision, prs=0, thr=1)
+
+
+def run_lattice(axs, dist, precision, steps, warmup, with_e2e, sampler=None):
+    p = main_params(axs, precision)
+    L = axs.Lattice(p)
+    L.init_flat(1, 1.0)
+    L.evolve(warmup)                       # includes autotuning (dt = 0 trials) and graph capture
+    L.evolve_timed(steps)                  # captures the graph for `steps`
+    dist.barrier()
+    if sampler:
+        sampler.start()
+    launches0 = axs.kernel_launches()
+    ms = L.evolve_timed(steps)             # CUDA events on the lattice's stream, synchronised
+    launches = axs.kernel_launches() - launches0
+    clocks = sampler.stop() if sampler else None
+    dist.barrier()
+    ms_max = dist.max(ms)
+    rec = {"ms": ms_max, "launches": launches, "desc": L.describe(), "clocks": clocks,
+           "sites": p.N ** 3, "finite": L.check_finite()}
+    if with_e2e:
+        rec["e2e"] = e2e_leg(axs, L, dist, steps)
+    L.close()
+    return rec
+
+
+def e2e_leg(axs, L, dist, steps):
+    """The user's call sequence with host buffers: upload the state from
+    pinned host memory, evolve `steps` steps through axs_evolve, read the
+    step's result (the string count) and the final fields back to host."""
+    shape = L.shape
+    bufs = [axs.PinnedBuffer(shape, np.float32) for _ in range(4)]
+    f = L.download(dtype=np.float32)
+    for b, a in zip(bufs, f):
+        b.array[...] = a
+    del f
+    dist.barrier()
+    t0 = time.perf_counter()
+    L.upload(*[b.array for b in bufs], dtype=np.float32)
+    L.evolve(steps)
+    n, c, _ = L.find_strings()
+    out = axs._lib.axs_download_f32(L._h, bufs[0].array.ctypes.data, bufs[1].array.ctypes.data, None, None)
+    axs._check(out)
+    wall = time.perf_counter() - t0
+    dist.barrier()
+    wall = dist.max(wall)
+    for b in bufs:
+        b.free()
+    sites = L.length
+    h2d = 4 * 4 * sites
+    d2h = 2 * 4 * sites + 16
+    return {"wall_s": wall, "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
+            "string_count": int(n), "site_updates_per_s": sites * steps / wall}
+
+
+def run_ensemble(axs, dist, steps, warmup, master_seed=2026):
+    rng = np.random.default_rng(master_seed)
+    n_total = 96
+    mine = [i for i in range(n_total) if i % dist.world == dist.rank]   # realisations shard across ranks
+    sizes = rng.choice(ENSEMBLE_SIZES, size=n_total)
+    lams = np.exp(rng.uniform(np.log(0.5), np.log(4.0), size=n_total))
+    seeds = rng.integers(1, 2 ** 31, size=n_total)
+    plist = [axs.default_params(NDIMS=3, N=int(sizes[i]), lambda_=float(lams[i]), T_initial=0.0, space_step=0.5,
+                                time_step=0.1, precision=32, prs=1, thr=1) for i in mine]
+    E = axs.Ensemble(plist)
+    for m, i in zip(E.members, mine):
+        m.init_flat(int(seeds[i]), 1.0)
+    E.evolve(warmup)
+    E.evolve_timed(steps)
+    dist.barrier()
+    l0 = axs.kernel_launches()
+    ms = E.evolve_timed(steps)
+    launches = axs.kernel_launches() - l0
+    dist.barrier()
+    sites = sum(int(p.N) ** 3 for p in plist)
+    sites_all = dist.sum(sites)
+    ms_max = dist.max(ms)
+    E.close()
+    return {"members": n_total, "sites": int(sites_all), "ms": ms_max, "launches": launches,
+            "sizes": [int(s) for s in sizes], "master_seed": master_seed}
+
+
+# --------------------------------------------------------------------- arms
+def reference_arm(args, dist):
+    """The reference's CPU path: the oracle port of vvsl_field_rescaled
+    (reference loop structure) on the host cores; oracle/_ref is x86-only."""
+    if dist.rank != 0:
+        return
+    n = 256
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    rate, steps_done, secs, threads = cpu_port_rate(n=n, target_s=max(5.0, 0.5 * (args.steps + args.warmup)),
+                                                    max_steps=args.steps + args.warmup)
+    line = {"metric": "site-updates/s", "value": rate, "unit": "site-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n ** 3 / rate,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": "3D 1024^3 FP32 leapfrog step (prs=0, lambda=1, dx=0.5, dt=0.1)",
+                       "sample": "%d^3 lattice, %d steps" % (n, steps_done)},
+            "cpu_baseline": {"value": rate, "unit": "site-updates/s", "cores": threads, "kind": "port",
+                             "sample": "%d^3 FP32, %d steps of the reference-structured step (oracle port; "
+                                       "the reference's own build needs MKL/FFTW and x86)" % (n, steps_done)},
+            "e2e": {"value": rate, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def gpu_arm(args, dist):
+    axs = load_axs()
+    axs.set_device(dist.local)
+    hbm, peak_note = peaks()
+    sampler = ClockSampler(dist.local)
+    main = run_lattice(axs, dist, 32, args.steps, args.warmup, with_e2e=True, sampler=sampler)
+    sites_all = dist.sum(main["sites"])
+    value = sites_all * args.steps / (main["ms"] * 1e-3)
+    per_launch_ms = main["ms"] / args.steps
+    achieved = BYTES_PER_SITE[32] * main["sites"] / (per_launch_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        try:
+            traffic = json.load(open(tfile)).get("zmarch_fp32_1024_per_launch_bytes")
+        except Exception:
+            traffic = None
+    fp64 = ens = None
+    if not args.quick:
+        f64 = run_lattice(axs, dist, 64, max(3, args.steps // 2), args.warmup, with_e2e=False)
+        r64 = dist.sum(f64["sites"]) * max(3, args.steps // 2) / (f64["ms"] * 1e-3)
+        fp64 = {"value": r64, "unit": "site-updates/s", "ms_per_step": f64["ms"] / max(3, args.steps // 2),
+                "hbm_frac": r64 / dist.world * 64 / 1e9 / hbm, "kernel": f64["desc"],
+                "fp32_over_fp64": value / r64}
+        e = run_ensemble(axs, dist, args.steps, args.warmup)
+        re = e["sites"] * args.steps / (e["ms"] * 1e-3)
+        ens = {"value": re, "unit": "site-updates/s", "members": e["members"], "sites": e["sites"],
+               "ms_per_step": e["ms"] / args.steps, "hbm_frac": re / dist.world * 32 / 1e9 / hbm,
+               "master_seed": e["master_seed"], "launches_per_step": e["launches"] / args.steps}
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu:
+        rate, steps_done, secs, threads = cpu_port_rate(n=256, target_s=10.0)
+        cpu = {"value": rate, "unit": "site-updates/s", "cores": threads, "kind": "port",
+               "sample": "256^3 FP32, %d steps (%.1f s) of the reference-structured step (oracle port)"
+                         % (steps_done, secs)}
+    e2e = main["e2e"]
+    e2e_value = sites_all * args.steps / e2e["wall_s"]      # wall_s is already the max over ranks
+    if dist.rank != 0:
+        return
+    line = {
+        "metric": "site-updates/s", "value": value, "unit": "site-updates/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": main["ms"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "3D 1024^3 FP32 leapfrog step, 7-point stencil, prs=0, lambda=1, dx=0.5, dt=0.1, "
+                               "flat k_cut=1 start", "N": N_MAIN, "precision": "fp32 fields, fp64 tau",
+                   "parallelism": "replicas" if dist.world > 1 else "single",
+                   "l2": "state 25.8 GB >> 129 MB L2; no flush needed", "kernel": main["desc"]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "peak_source": peak_note,
+                     "algorithmic_bytes_per_site_update": BYTES_PER_SITE[32]},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "site-updates/s", "h2d_bytes_per_step": e2e["h2d_bytes_per_step"],
+                "d2h_bytes_per_step": e2e["d2h_bytes_per_step"], "wall_s": e2e["wall_s"]},
+        "gpu_launches": main["launches"],
+        "clocks": main["clocks"],
+        "fp64": fp64,
+        "ensemble": ens,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="axs", choices=["axs", "reference"])
+    ap.add_argument("--quick", action="store_true", help="headline only (no FP64 / ensemble legs)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            reference_arm(args, dist)
+        else:
+            gpu_arm(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,38 @@
+"""Background means (s_run.cpp:135-150), energies and the finite check."""
+import numpy as np
+import pytest
+
+from gpu_util import orc, params, rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision,tol", [(64, 1e-12), (32, 2e-6)])
+@pytest.mark.parametrize("nd,N", [(2, 64), (3, 32)])
+def test_background_and_energies(axs, oracle, precision, tol, nd, N):
+    p = params(axs, nd, N, precision, T_initial=0.0)
+    op = orc(p)
+    with axs.Lattice(p) as L:
+        L.init_flat(6, 1.0)
+        L.evolve(15)
+        g = L.download()
+        tau, _ = L.time
+        bg = L.background()
+        en = L.energies()
+    bo = oracle.background(op, *g)
+    eo = oracle.energies(op, *g, tau)
+    for q in range(6):
+        assert abs(bg[q] - bo[q]) <= tol * max(1.0, abs(bo[q])), (q, bg[q], bo[q])
+    for q in range(3):
+        assert abs(en[q] - eo[q]) <= tol * max(1e-3, abs(eo[q])) * 10, (q, en[q], eo[q])
+
+
+def test_finite_check_flags_seeded_nan(axs):
+    p = params(axs, 3, 32, 64)
+    with axs.Lattice(p) as L:
+        L.init_flat(1, 1.0)
+        assert L.check_finite()
+        f = list(L.download())
+        f[2][3, 4, 5] = np.nan
+        L.upload(*f)
+        assert not L.check_finite()

@@ -1,0 +1,60 @@
+"""Spectra: output_powerspec (src/common/pk_estimation.cpp:37-214) and the
+axion kinetic-energy spectrum, against the oracle. FP64 bins within 1e-11
+relative; FP32 fields within 1e-5."""
+import numpy as np
+import pytest
+
+from gpu_util import orc, params, rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("nd,N", [(2, 64), (2, 96), (3, 32), (3, 48)])
+@pytest.mark.parametrize("field", [1, 0, 3])
+def test_powerspec_matches_oracle(axs, oracle, nd, N, field):
+    p = params(axs, nd, N, 64)
+    op = orc(p)
+    f = oracle.init_thermal(op, 8)
+    with axs.Lattice(p) as L:
+        L.upload(*f)
+        L.evolve(5)
+        g = L.download()
+        pk, ks, cnt = L.powerspec(field)
+    pko, kso, cnto = oracle.powerspec(op, g[field])
+    assert np.array_equal(cnt, cnto)
+    ok = cnto > 0
+    assert rel(pk[ok], pko[ok]) <= 1e-11
+    assert rel(ks[ok], kso[ok]) <= 1e-11
+    assert np.all(np.isnan(pk[~ok])) and np.all(np.isnan(ks[~ok]))
+
+
+def test_powerspec_fp32(axs, oracle):
+    p = params(axs, 3, 32, 32)
+    op = orc(p)
+    f = oracle.init_thermal(op, 8)
+    with axs.Lattice(p) as L:
+        L.upload(*f)
+        pk, ks, cnt = L.powerspec(1)
+        g = L.download()
+    pko, kso, cnto = oracle.powerspec(op, g[1])
+    ok = cnto > 0
+    assert np.array_equal(cnt, cnto)
+    assert rel(pk[ok], pko[ok]) <= 1e-5
+
+
+@pytest.mark.parametrize("nd,N,nbins", [(3, 32, 16), (3, 48, 128), (2, 64, 32)])
+def test_axion_spectrum_matches_oracle(axs, oracle, nd, N, nbins):
+    p = params(axs, nd, N, 64, T_initial=0.0)
+    op = orc(p)
+    f = oracle.init_flat(op, 2, 2.0)
+    with axs.Lattice(p) as L:
+        L.upload(*f)
+        L.evolve(20)
+        g = L.download()
+        tau, _ = L.time
+        k, pk, cnt = L.axion_spectrum(nbins)
+    ko, pko, cnto = oracle.axion_spectrum(op, *g, tau, nbins)
+    assert np.array_equal(cnt, cnto)
+    ok = cnto > 0
+    assert rel(pk[ok], pko[ok]) <= 1e-10
+    assert rel(k[ok], ko[ok]) <= 1e-12
