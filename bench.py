@@ -178,13 +178,13 @@ def load_axs():
     return axs
 
 
-def main_params(axs, precision, n=N_MAIN):
+def main_params(axs, precision, n):
     return axs.default_params(NDIMS=3, N=n, lambda_=1.0, T_initial=0.0, space_step=0.5, time_step=0.1,
                               precision=precision, prs=0, thr=1)
 
 
-def run_lattice(axs, dist, precision, steps, warmup, with_e2e, sampler=None):
-    p = main_params(axs, precision)
+def run_lattice(axs, dist, precision, steps, warmup, with_e2e, sampler=None, n=N_MAIN):
+    p = main_params(axs, precision, n)
     L = axs.Lattice(p)
     L.init_flat(1, 1.0)
     L.evolve(warmup)                       # includes autotuning (dt = 0 trials) and graph capture
@@ -290,7 +290,7 @@ def gpu_arm(args, dist):
     axs.set_device(dist.local)
     hbm, peak_note = peaks()
     sampler = ClockSampler(dist.local)
-    main = run_lattice(axs, dist, 32, args.steps, args.warmup, with_e2e=True, sampler=sampler)
+    main = run_lattice(axs, dist, 32, args.steps, args.warmup, with_e2e=not args.no_e2e, sampler=sampler, n=args.n)
     sites_all = dist.sum(main["sites"])
     value = sites_all * args.steps / (main["ms"] * 1e-3)
     per_launch_ms = main["ms"] / args.steps
@@ -304,7 +304,7 @@ def gpu_arm(args, dist):
             traffic = None
     fp64 = ens = None
     if not args.quick:
-        f64 = run_lattice(axs, dist, 64, max(3, args.steps // 2), args.warmup, with_e2e=False)
+        f64 = run_lattice(axs, dist, 64, max(3, args.steps // 2), args.warmup, with_e2e=False, n=args.n)
         r64 = dist.sum(f64["sites"]) * max(3, args.steps // 2) / (f64["ms"] * 1e-3)
         fp64 = {"value": r64, "unit": "site-updates/s", "ms_per_step": f64["ms"] / max(3, args.steps // 2),
                 "hbm_frac": r64 / dist.world * 64 / 1e9 / hbm, "kernel": f64["desc"],
@@ -320,24 +320,27 @@ def gpu_arm(args, dist):
         cpu = {"value": rate, "unit": "site-updates/s", "cores": threads, "kind": "port",
                "sample": "256^3 FP32, %d steps (%.1f s) of the reference-structured step (oracle port)"
                          % (steps_done, secs)}
-    e2e = main["e2e"]
-    e2e_value = sites_all * args.steps / e2e["wall_s"]      # wall_s is already the max over ranks
+    e2e = main.get("e2e")
+    e2e_line = None
+    if e2e:
+        e2e_line = {"value": sites_all * args.steps / e2e["wall_s"],      # wall_s is already the max over ranks
+                    "unit": "site-updates/s", "h2d_bytes_per_step": e2e["h2d_bytes_per_step"],
+                    "d2h_bytes_per_step": e2e["d2h_bytes_per_step"], "wall_s": e2e["wall_s"]}
     if dist.rank != 0:
         return
     line = {
         "metric": "site-updates/s", "value": value, "unit": "site-updates/s", "n_gpus": dist.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": main["ms"] / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "3D 1024^3 FP32 leapfrog step, 7-point stencil, prs=0, lambda=1, dx=0.5, dt=0.1, "
-                               "flat k_cut=1 start", "N": N_MAIN, "precision": "fp32 fields, fp64 tau",
+        "config": {"workload": "3D %d^3 FP32 leapfrog step, 7-point stencil, prs=0, lambda=1, dx=0.5, dt=0.1, "
+                               "flat k_cut=1 start" % args.n, "N": args.n, "precision": "fp32 fields, fp64 tau",
                    "parallelism": "replicas" if dist.world > 1 else "single",
                    "l2": "state 25.8 GB >> 129 MB L2; no flush needed", "kernel": main["desc"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_source": peak_note,
                      "algorithmic_bytes_per_site_update": BYTES_PER_SITE[32]},
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e_value, "unit": "site-updates/s", "h2d_bytes_per_step": e2e["h2d_bytes_per_step"],
-                "d2h_bytes_per_step": e2e["d2h_bytes_per_step"], "wall_s": e2e["wall_s"]},
+        "e2e": e2e_line,
         "gpu_launches": main["launches"],
         "clocks": main["clocks"],
         "fp64": fp64,
@@ -354,6 +357,8 @@ def main():
     ap.add_argument("--impl", default="axs", choices=["axs", "reference"])
     ap.add_argument("--quick", action="store_true", help="headline only (no FP64 / ensemble legs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
+    ap.add_argument("--n", type=int, default=N_MAIN, help="lattice side (profiling cases use smaller N)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
