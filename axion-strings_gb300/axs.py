@@ -100,6 +100,7 @@ _sig("axs_ensemble_evolve_timed", [_vp, ctypes.c_int, _dp])
 _sig("axs_autotune", [_vp])
 _sig("axs_describe", [_vp, ctypes.c_char_p, ctypes.c_size_t])
 _sig("axs_kernel_launches", [], ctypes.c_int64)
+_sig("axs_powerspec_noalloc", [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, _vp, _vp, _vp, _vp])
 _sig("axs_set_device", [ctypes.c_int])
 _sig("axs_host_alloc", [ctypes.c_size_t, ctypes.POINTER(_vp)])
 _sig("axs_host_free", [_vp])
@@ -142,6 +143,13 @@ def kernel_launches():
 
 def set_device(device):
     _check(_lib.axs_set_device(int(device)))
+
+
+def powerspec_noalloc(spectrum_ptr, ndims, n, precision, space_step, pk_ptr, ks_ptr, count_ptr, stream=0):
+    """axs_powerspec_noalloc on caller-owned device buffers (raw device
+    addresses); asynchronous on `stream` (a cudaStream_t value, 0 = default)."""
+    _check(_lib.axs_powerspec_noalloc(_vp(spectrum_ptr), int(ndims), int(n), int(precision), float(space_step),
+                                      _vp(pk_ptr), _vp(ks_ptr), _vp(count_ptr), _vp(stream or None)))
 
 
 def _ptr(a):

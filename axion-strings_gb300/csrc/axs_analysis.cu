@@ -4,6 +4,7 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#include <mutex>
 
 #include "axs_internal.h"
 
@@ -750,3 +751,125 @@ void analysis_release(Lattice *L) {
 }
 
 }  // namespace axs
+
+// ============================================================== allocation-free binner
+//
+// axs_powerspec_noalloc serves callers that own all device memory themselves
+// and cannot let a library call cudaMalloc/cudaFree while they run: hosts that
+// budget the whole device up front, frameworks whose caching allocator must
+// be the only one handing out device memory, and applications that cannot
+// afford the device-wide synchronisation a cudaFree implies. They run their
+// own R2C FFT into their own buffer and ask only for the binning.
+//
+// Its scratch is one file-scope __device__ array (below), held by every GPU
+// that loads this library until the process exits. All calls share it and it
+// keeps the last call's contents: the per-bin counts are cleared at the start
+// of every call and everything else is overwritten, so calls that follow one
+// another on a stream are independent, but calls whose kernels overlap on the
+// GPU (different streams, no ordering) race on the array and give wrong
+// results.
+
+namespace axs {
+
+static constexpr int kNoAllocMaxBins = 1024;   // N/2 bins, so N <= 2048
+static constexpr int kNoAllocBlocks = 128;     // binning grid (partials rows)
+static constexpr int kNoAllocScratchDoubles = kNoAllocBlocks * 2 * kNoAllocMaxBins   // block partials
+                                              + kNoAllocMaxBins;                      // counts (as u64)
+// 2 MiB + 8 KiB per device.
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+__global__ void k_noalloc_clear(unsigned long long *counts, int nbins) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nbins) counts[b] = 0ull;
+}
+
+// Sum the block partials in block order and normalise as output_powerspec
+// does (pk_estimation.cpp:117-121 / 195-199).
+__global__ void k_noalloc_final(const double *__restrict__ partials, int nblocks, int nbins,
+                                const unsigned long long *__restrict__ counts, int ndims, float Lf,
+                                double *__restrict__ pk, double *__restrict__ ks, int *__restrict__ count) {
+    int bn = blockIdx.x * blockDim.x + threadIdx.x;
+    if (bn >= nbins) return;
+    double sp = 0.0, sk = 0.0;
+    for (int b = 0; b < nblocks; ++b) {
+        sp += partials[((int64_t)b * 2 + 0) * nbins + bn];
+        sk += partials[((int64_t)b * 2 + 1) * nbins + bn];
+    }
+    int c = (int)counts[bn];
+    double k = sk / (double)c;
+    double p = sp;
+    if (ndims == 2) p /= 2.0f * M_PI * k;
+    else p /= 4.0f * M_PI * (k * k);
+    k *= 2.0f * M_PI / Lf;
+    pk[bn] = p;
+    ks[bn] = k;
+    count[bn] = c;
+}
+
+// Device address of the scratch array on each device, looked up once per
+// device by the first call made with that device current.
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[128] = {nullptr};
+
+static double *noalloc_scratch() {
+    int dev = 0;
+    AXS_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) fail(AXS_ERR_ARG, "device index %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            fail(AXS_ERR_CUDA, "cudaGetSymbolAddress of the binner scratch failed: %s", cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    return (double *)g_noalloc_ptr[dev];
+}
+
+template <typename T>
+static void noalloc_bin(const void *spectrum, int ndims, int N, float Lf, double *pk, double *ks, int *count,
+                        cudaStream_t st) {
+    int nbins = N / 2;
+    double *scratch = noalloc_scratch();
+    double *partials = scratch;
+    unsigned long long *counts = (unsigned long long *)(scratch + (size_t)kNoAllocBlocks * 2 * kNoAllocMaxBins);
+    size_t sm = (size_t)4 * 2 * nbins * sizeof(double);
+    // Raise the kernel's dynamic shared-memory limit only above the 48 KiB
+    // default (never lower it: the allocating binner launches the same kernel).
+    if (sm > 48 * 1024)
+        AXS_CUDA(cudaFuncSetAttribute(k_bin<T, RefBins>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_noalloc_clear<<<(nbins + 127) / 128, 128, 0, st>>>(counts, nbins);
+    k_bin<T, RefBins><<<kNoAllocBlocks, 128, sm, st>>>((const typename Cplx<T>::type *)spectrum, N, ndims,
+                                                       RefBins{N / 2}, nbins, partials, counts);
+    k_noalloc_final<<<(nbins + 127) / 128, 128, 0, st>>>(partials, kNoAllocBlocks, nbins, counts, ndims, Lf, pk, ks,
+                                                         count);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(3);
+}
+
+}  // namespace axs
+
+extern "C" int axs_powerspec_noalloc(const void *spectrum, int NDIMS, int N, int precision, float space_step,
+                                     double *pk, double *ks, int *count, void *stream) {
+    try {
+        if (!spectrum || !pk || !ks || !count) axs::fail(AXS_ERR_ARG, "null pointer argument");
+        if (NDIMS != 2 && NDIMS != 3) axs::fail(AXS_ERR_ARG, "NDIMS must be 2 or 3 (got %d)", NDIMS);
+        if (N < 4 || (N % 2) != 0) axs::fail(AXS_ERR_ARG, "N must be even and >= 4 (got %d)", N);
+        if (N / 2 > axs::kNoAllocMaxBins)
+            axs::fail(AXS_ERR_ARG, "N=%d needs %d bins; the allocation-free binner holds at most %d (N <= %d)", N,
+                      N / 2, axs::kNoAllocMaxBins, 2 * axs::kNoAllocMaxBins);
+        if (precision != AXS_F32 && precision != AXS_F64) axs::fail(AXS_ERR_ARG, "precision must be 32 or 64");
+        if (!(space_step > 0.0f)) axs::fail(AXS_ERR_ARG, "space_step must be positive");
+        float Lf = N * space_step;
+        cudaStream_t st = (cudaStream_t)stream;
+        if (precision == AXS_F32) axs::noalloc_bin<float>(spectrum, NDIMS, N, Lf, pk, ks, count, st);
+        else axs::noalloc_bin<double>(spectrum, NDIMS, N, Lf, pk, ks, count, st);
+    } catch (const axs::Error &e) {
+        axs::set_last_error(e.code, e.msg);
+        return e.code;
+    } catch (...) {
+        axs::set_last_error(AXS_ERR_CUDA, "unexpected internal error");
+        return AXS_ERR_CUDA;
+    }
+    return AXS_OK;
+}

@@ -173,6 +173,30 @@ int axs_powerspec(axs_lattice *h, int field, double *pk, double *ks, int *count)
  * 2 pi / L to sqrt(NDIMS) pi / dx; pk = L^d / N^(2d) <|F|^2>_bin. FP64 sums. */
 int axs_axion_spectrum(axs_lattice *h, int nbins, double *kmean, double *pk, int64_t *count);
 
+/* Allocation-free variant of the spectrum binning in axs_powerspec. No
+ * counterpart in the reference: it exists for callers that own all device
+ * memory and cannot let this library call cudaMalloc or cudaFree (hosts that
+ * budget the device up front, frameworks whose caching allocator must be the
+ * only source of device memory, codes that cannot absorb the device-wide
+ * synchronisation of a cudaFree).
+ *   spectrum   device pointer to the R2C half spectrum of a real N^NDIMS field
+ *              as cuFFT writes it (cufftComplex for AXS_F32, cufftDoubleComplex
+ *              for AXS_F64; [N][N/2+1] in 2D, [N][N][N/2+1] in 3D)
+ *   pk, ks, count   device arrays of N/2 entries, filled as axs_powerspec fills
+ *              its host arrays (output_powerspec's bins and normalisation)
+ *   stream     cudaStream_t to run on (NULL: the legacy default stream); the
+ *              call is asynchronous on it
+ * It allocates nothing: its scratch is a static device array of 2 MiB + 8 KiB
+ * per GPU, held from library load to process exit, which limits it to N <= 2048
+ * (larger N is rejected with AXS_ERR_ARG). The first call on each device does
+ * a one-time set-up with that device current (it looks up the array's device
+ * address); make that first call before any stream capture. All calls share
+ * the array, which keeps the last call's contents (the counts are cleared on
+ * every call): calls in order on one stream are independent; calls that
+ * overlap on the GPU race and give wrong results. */
+int axs_powerspec_noalloc(const void *spectrum, int NDIMS, int N, int precision, float space_step,
+                          double *pk, double *ks, int *count, void *stream);
+
 /* ---- reductions -------------------------------------------------------------------- */
 
 /* The six background means of s_run.cpp:135-150: phi1, phi2, phidot1, phidot2,
