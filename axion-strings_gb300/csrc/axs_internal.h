@@ -58,6 +58,7 @@ struct ZLat {
     CUtensorMap tm_row[2];   // box {tx, 1, 1} over psi[b]
     CUtensorMap tm_main[2];  // box {tx, TY, 1}
     CUtensorMap tm_xh[2];    // box {16-byte halo, TY, 1}
+    CUtensorMap tm_pih;      // box {tx, TY, 1} over pih
     void *psi[2];
     void *pih;
     double *clock;           // [2] tau at the parity of psi

@@ -407,6 +407,251 @@ __global__ void __launch_bounds__(256) k_zmarch(const ZLat *__restrict__ lats, i
     }
 }
 
+// ============================================================== z-march, warp-specialised
+//
+// Same work items and halo boxes as k_zmarch, organised as a producer /
+// consumer pipeline with no CTA-wide barrier in the steady state:
+//  * warp NCW (one lane) is the producer: it takes items from the global
+//    counter one item ahead of the consumers and issues, per plane, the TMA
+//    loads of psi (tile + periodic halos) AND of pih (tile) into a ring slot,
+//    after waiting on that slot's `empty` mbarrier;
+//  * warps 0..NCW-1 are consumers: they wait on the slot's `full` mbarrier,
+//    compute the plane, store psi_new and pih with 16-byte stores, and arrive
+//    on `empty` when they are done with a plane.
+// Items reach the consumers through a two-entry queue guarded by mbarriers.
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Warp-uniform bounded wait: 0 = completed, 1 = this warp timed out,
+// 2 = another warp or the producer aborted. Every lane gets the same answer,
+// so the warp never diverges around __syncwarp / the final barrier.
+__device__ __forceinline__ int warp_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag) {
+    const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(bar, parity));
+    if (!ok) return 1;
+    return __any_sync(0xffffffffu, *abort_flag != 0) ? 2 : 0;
+}
+
+template <typename T, int TY, int TXMAX, int S>
+struct Z2Cfg {
+    static constexpr int CS = 2 * (int)sizeof(T);
+    static constexpr int VS = 16 / CS;
+    static constexpr int EU = CS / 8;
+    static constexpr int NCW = 8;                              // consumer warps
+    static constexpr int NT = (NCW + 1) * 32;
+    static constexpr int NC = NCW * 32;                        // consumer threads
+    static constexpr int MAXV = (TXMAX * TY / VS + NC - 1) / NC;
+    static constexpr int C_BYTES = (TY + 2) * TXMAX * CS;      // psi rows y0-1 .. y0+TY
+    static constexpr int H_PAD = (TY * 16 + 127) / 128 * 128;  // one x-halo strip
+    static constexpr int P_OFF = C_BYTES + 2 * H_PAD;          // pih tile
+    static constexpr int SLOT = (P_OFF + TY * TXMAX * CS + 127) / 128 * 128;
+    static constexpr int BAR_OFF = S * SLOT;
+    static constexpr int SMEM = BAR_OFF + 256;
+};
+
+template <typename T, int TY, int TXMAX, int S>
+__global__ void __launch_bounds__(Z2Cfg<T, TY, TXMAX, S>::NT)
+    k_zmarch2(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity, int *derr) {
+    typedef Z2Cfg<T, TY, TXMAX, S> K;
+    typedef typename Cplx<T>::type C;
+    typedef typename Vec16<T>::type V;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + K::BAR_OFF);
+    uint64_t *empty = full + S;
+    uint64_t *ifull = empty + S;                                 // [2]
+    uint64_t *iempty = ifull + 2;                                // [2]
+    volatile int64_t *items = reinterpret_cast<volatile int64_t *>(iempty + 2);   // [2]
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(items + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), K::NCW);
+        }
+        for (int k = 0; k < 2; ++k) {
+            mbar_init(smem_u32(&ifull[k]), 1);
+            mbar_init(smem_u32(&iempty[k]), K::NCW);
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp == K::NCW) {
+        // ------------------------------------------------------------ producer
+        if (lane == 0) {
+            int64_t q = 0;
+            bool ok = true;
+            for (int64_t k = 0; ok; ++k) {
+                if (k >= 2) ok = mbar_wait_bounded(smem_u32(&iempty[k & 1]), (uint32_t)(((k >> 1) - 1) & 1));
+                if (!ok || *abort_flag) break;
+                const int64_t item = (int64_t)atomicAdd(&counters[0], 1);
+                items[k & 1] = item;
+                mbar_arrive(smem_u32(&ifull[k & 1]));
+                if (item >= total_items) break;
+                int li = 0;
+                while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+                const ZLat &Lt = lats[li];
+                const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
+                const int64_t local = item - Lt.item_base;
+                const int ncols = ntx * nty;
+                const int zq = (int)(local / ncols), col = (int)(local % ncols);
+                const int x0 = (col % ntx) * tx, y0 = (col / ntx) * TY;
+                const int za = (int)((int64_t)zq * N / nzc), zb = (int)((int64_t)(zq + 1) * N / nzc);
+                const int nload = zb - za + 2;
+                const int bin = Lt.a_index ^ parity;
+                const bool xhalo = tx < N;
+                const uint32_t psi_bytes = (uint32_t)((TY + 2) * tx * K::CS + (xhalo ? 2 * TY * 16 : 0));
+                const uint32_t pih_bytes = (uint32_t)(TY * tx * K::CS);
+                const int ym = y0 == 0 ? N - 1 : y0 - 1;
+                const int yp = (y0 + TY == N) ? 0 : y0 + TY;
+                for (int i = 0; i < nload; ++i, ++q) {
+                    const int s = (int)(q % S);
+                    if (q >= S) {
+                        ok = mbar_wait_bounded(smem_u32(&empty[s]), (uint32_t)(((q / S) - 1) & 1));
+                        if (!ok || *abort_flag) break;
+                    }
+                    int z = za - 1 + i;
+                    z = z < 0 ? z + N : (z >= N ? z - N : z);
+                    unsigned char *slot = smem + s * K::SLOT;
+                    const uint32_t bar = smem_u32(&full[s]);
+                    const bool with_pih = i >= 1 && i <= nload - 2;
+                    mbar_expect_tx(bar, psi_bytes + (with_pih ? pih_bytes : 0u));
+                    tma_load_3d(smem_u32(slot), &Lt.tm_row[bin], x0 * K::EU, ym, z, bar);
+                    tma_load_3d(smem_u32(slot + tx * K::CS), &Lt.tm_main[bin], x0 * K::EU, y0, z, bar);
+                    tma_load_3d(smem_u32(slot + (TY + 1) * tx * K::CS), &Lt.tm_row[bin], x0 * K::EU, yp, z, bar);
+                    if (xhalo) {
+                        const int xl = (x0 - K::VS + N) % N, xr = (x0 + tx) % N;
+                        tma_load_3d(smem_u32(slot + K::C_BYTES), &Lt.tm_xh[bin], xl * K::EU, y0, z, bar);
+                        tma_load_3d(smem_u32(slot + K::C_BYTES + K::H_PAD), &Lt.tm_xh[bin], xr * K::EU, y0, z, bar);
+                    }
+                    if (with_pih) tma_load_3d(smem_u32(slot + K::P_OFF), &Lt.tm_pih, x0 * K::EU, y0, z, bar);
+                }
+            }
+            if (!ok) {
+                atomicOr(derr, DEVERR_TIMEOUT);
+                *abort_flag = 1;
+            }
+            // Drain: wait (bounded) for this CTA's last loads still in flight.
+            for (int64_t d = q > S ? q - S : 0; d < q; ++d)
+                mbar_wait_bounded(smem_u32(&full[d % S]), (uint32_t)((d / S) & 1));
+        }
+    } else {
+        // ------------------------------------------------------------ consumers
+        const int cid = tid;   // 0 .. NC-1
+        int64_t q0 = 0;
+        for (int64_t k = 0;; ++k) {
+            const int w0 = warp_wait(smem_u32(&ifull[k & 1]), (uint32_t)((k >> 1) & 1), abort_flag);
+            if (w0) {
+                if (w0 == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
+                break;
+            }
+            bool ok = true;
+            const int64_t item = items[k & 1];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&iempty[k & 1]));
+            if (item >= total_items) break;
+            int li = 0;
+            while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+            const ZLat &Lt = lats[li];
+            const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
+            const int64_t local = item - Lt.item_base;
+            const int ncols = ntx * nty;
+            const int zq = (int)(local / ncols), col = (int)(local % ncols);
+            const int x0 = (col % ntx) * tx, y0 = (col / ntx) * TY;
+            const int za = (int)((int64_t)zq * N / nzc), zb = (int)((int64_t)(zq + 1) * N / nzc);
+            const int T_steps = zb - za;
+            const int bin = Lt.a_index ^ parity;
+            C *psi_out = reinterpret_cast<C *>(Lt.psi[bin ^ 1]);
+            C *pih = reinterpret_cast<C *>(Lt.pih);
+            const double tau = Lt.clock[bin];
+            const StepCoefs<T> cf = make_coefs<T>(tau, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs);
+            if (local == 0 && cid == 0) Lt.clock[bin ^ 1] = tau + Lt.dt;   // tau += dt, s_integrate.cpp:317
+            const bool xhalo = tx < N;
+            const int nvx = tx / K::VS;
+            const int nvec = nvx * TY;
+            for (int t = 0; t < T_steps && ok; ++t) {
+                const int64_t qn = q0 + t + 2;
+                int w = 0;
+                if (t == 0) {
+                    w = warp_wait(smem_u32(&full[q0 % S]), (uint32_t)((q0 / S) & 1), abort_flag);
+                    if (!w) w = warp_wait(smem_u32(&full[(q0 + 1) % S]), (uint32_t)(((q0 + 1) / S) & 1), abort_flag);
+                }
+                if (!w) w = warp_wait(smem_u32(&full[qn % S]), (uint32_t)((qn / S) & 1), abort_flag);
+                if (w) {
+                    if (w == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
+                    ok = false;
+                    break;
+                }
+                const int z = za + t;
+                const unsigned char *sz = smem + ((q0 + t + 1) % S) * K::SLOT;
+                const C *Cm = reinterpret_cast<const C *>(smem + ((q0 + t) % S) * K::SLOT);
+                const C *Cz = reinterpret_cast<const C *>(sz);
+                const C *Cp = reinterpret_cast<const C *>(smem + (qn % S) * K::SLOT);
+                const C *Lh = reinterpret_cast<const C *>(sz + K::C_BYTES);
+                const C *Rh = reinterpret_cast<const C *>(sz + K::C_BYTES + K::H_PAD);
+                const C *Ph = reinterpret_cast<const C *>(sz + K::P_OFF);
+#pragma unroll
+                for (int j = 0; j < K::MAXV; ++j) {
+                    const int v = cid + j * K::NC;
+                    if (v >= nvec) continue;
+                    const int yy = v / nvx, xx = (v % nvx) * K::VS;
+                    const int r = (1 + yy) * tx + xx;
+                    C ctr[K::VS], up[K::VS], dn[K::VS], zm[K::VS], zp[K::VS];
+                    *reinterpret_cast<V *>(ctr) = *reinterpret_cast<const V *>(&Cz[r]);
+                    *reinterpret_cast<V *>(up) = *reinterpret_cast<const V *>(&Cz[r - tx]);
+                    *reinterpret_cast<V *>(dn) = *reinterpret_cast<const V *>(&Cz[r + tx]);
+                    *reinterpret_cast<V *>(zm) = *reinterpret_cast<const V *>(&Cm[r]);
+                    *reinterpret_cast<V *>(zp) = *reinterpret_cast<const V *>(&Cp[r]);
+                    C left, right;
+                    if (xx > 0) left = Cz[r - 1];
+                    else left = xhalo ? Lh[yy * K::VS + K::VS - 1] : Cz[(1 + yy) * tx + tx - 1];
+                    if (xx + K::VS < tx) right = Cz[r + K::VS];
+                    else right = xhalo ? Rh[yy * K::VS] : Cz[(1 + yy) * tx];
+                    T pv[2 * K::VS];
+                    *reinterpret_cast<V *>(pv) = *reinterpret_cast<const V *>(&Ph[yy * tx + xx]);
+                    C outv[K::VS];
+#pragma unroll
+                    for (int jj = 0; jj < K::VS; ++jj) {
+                        const C xm = (jj == 0) ? left : ctr[jj - 1];
+                        const C xp = (jj == K::VS - 1) ? right : ctr[jj + 1];
+                        const T L1 = lap7<T>(ctr[jj].x, xm.x, xp.x, up[jj].x, dn[jj].x, zm[jj].x, zp[jj].x);
+                        const T L2 = lap7<T>(ctr[jj].y, xm.y, xp.y, up[jj].y, dn[jj].y, zm[jj].y, zp[jj].y);
+                        site_update<T>(ctr[jj].x, ctr[jj].y, L1, L2, pv[2 * jj], pv[2 * jj + 1], outv[jj].x, outv[jj].y, cf);
+                    }
+                    const int64_t off = ((int64_t)z * N + (y0 + yy)) * N + (x0 + xx);
+                    *reinterpret_cast<V *>(&pih[off]) = *reinterpret_cast<V *>(pv);
+                    *reinterpret_cast<V *>(&psi_out[off]) = *reinterpret_cast<V *>(outv);
+                }
+                // this warp is done with plane z-1 (load q0+t); at the last step
+                // also with the item's last two planes
+                __syncwarp();
+                if (lane == 0) {
+                    mbar_arrive(smem_u32(&empty[(q0 + t) % S]));
+                    if (t == T_steps - 1) {
+                        mbar_arrive(smem_u32(&empty[(q0 + T_steps) % S]));
+                        mbar_arrive(smem_u32(&empty[(q0 + T_steps + 1) % S]));
+                    }
+                }
+            }
+            if (!ok) break;
+            q0 += T_steps + 2;
+        }
+    }
+    __syncwarp();      // reconverge every warp (the producer's lane 0 ran alone) before the barrier
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&counters[1], 1) == (int)gridDim.x - 1) {
+            counters[0] = 0;
+            counters[1] = 0;
+            __threadfence();
+        }
+    }
+}
+
 // ============================================================== host side
 
 static int g_num_sms = 0;
@@ -428,16 +673,17 @@ static int grid_for(int64_t len, int threads = 256) {
 std::string StepConfig::describe() const {
     char b[160];
     if (kind == 0) snprintf(b, sizeof b, "generic per-site kernel");
-    else snprintf(b, sizeof b, "TMA z-march variant %d, tx=%d, zchunk=%d, %d CTA/SM", variant, tx, zchunk, ctas_per_sm);
+    else snprintf(b, sizeof b, "TMA z-march variant %d, tx=%d, zchunk=%d", variant, tx, zchunk);
     return b;
 }
 
 // ---- z-march variants -------------------------------------------------------
 struct ZVariant {
-    int ty, txmax, slots;
+    int gen, ty, txmax, slots;   // gen 1: k_zmarch (CTA barriers), gen 2: k_zmarch2 (producer warp)
 };
 static const ZVariant kZVariants[] = {
-    {8, 128, 4}, {8, 128, 5}, {16, 128, 4}, {4, 256, 4}, {8, 256, 4},
+    {1, 8, 128, 4}, {1, 8, 128, 5}, {1, 16, 128, 4}, {1, 4, 256, 4}, {1, 8, 256, 4},
+    {2, 8, 128, 4}, {2, 8, 128, 5}, {2, 4, 256, 5}, {2, 8, 256, 5}, {2, 4, 128, 6},
 };
 static const int kNumZVariants = sizeof(kZVariants) / sizeof(kZVariants[0]);
 
@@ -469,6 +715,32 @@ static void launch_zmarch_t(const ZLat *d, int nlat, int64_t items, int *counter
     count_launches(1);
 }
 
+template <typename T, int TY, int TXMAX, int S>
+static int prepare_zmarch2_t() {
+    typedef Z2Cfg<T, TY, TXMAX, S> K;
+    static int occ = -1;
+    if (occ < 0) {
+        AXS_CUDA(cudaFuncSetAttribute(k_zmarch2<T, TY, TXMAX, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
+        int o = 0;
+        AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_zmarch2<T, TY, TXMAX, S>, K::NT, K::SMEM));
+        if (o < 1) fail(AXS_ERR_CUDA, "z-march kernel does not fit on an SM");
+        occ = o;
+    }
+    return occ;
+}
+
+template <typename T, int TY, int TXMAX, int S>
+static void launch_zmarch2_t(const ZLat *d, int nlat, int64_t items, int *counters, int parity, int *derr,
+                             cudaStream_t st, int ctas_per_sm) {
+    typedef Z2Cfg<T, TY, TXMAX, S> K;
+    int occ = prepare_zmarch2_t<T, TY, TXMAX, S>();
+    int per = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ) : occ;
+    int64_t grid = std::min<int64_t>((int64_t)per * num_sms(), items);
+    k_zmarch2<T, TY, TXMAX, S><<<(int)grid, K::NT, K::SMEM, st>>>(d, nlat, items, counters, parity, derr);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+
 static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t items, int *counters, int parity,
                           int *derr, cudaStream_t st, int ctas_per_sm) {
 #define AXS_ZV(I, TY, TX, S)                                                                                    \
@@ -476,15 +748,26 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
         if (esz == 4) launch_zmarch_t<float, TY, TX, S>(d, nlat, items, counters, parity, derr, st, ctas_per_sm); \
         else launch_zmarch_t<double, TY, TX, S>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);         \
         break;
+#define AXS_ZV2(I, TY, TX, S)                                                                                    \
+    case I:                                                                                                      \
+        if (esz == 4) launch_zmarch2_t<float, TY, TX, S>(d, nlat, items, counters, parity, derr, st, ctas_per_sm); \
+        else launch_zmarch2_t<double, TY, TX, S>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);         \
+        break;
     switch (variant) {
         AXS_ZV(0, 8, 128, 4)
         AXS_ZV(1, 8, 128, 5)
         AXS_ZV(2, 16, 128, 4)
         AXS_ZV(3, 4, 256, 4)
         AXS_ZV(4, 8, 256, 4)
+        AXS_ZV2(5, 8, 128, 4)
+        AXS_ZV2(6, 8, 128, 5)
+        AXS_ZV2(7, 4, 256, 5)
+        AXS_ZV2(8, 8, 256, 5)
+        AXS_ZV2(9, 4, 128, 6)
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
 #undef AXS_ZV
+#undef AXS_ZV2
 }
 
 static void prepare_zmarch(int esz, int variant) {
@@ -493,15 +776,45 @@ static void prepare_zmarch(int esz, int variant) {
         if (esz == 4) prepare_zmarch_t<float, TY, TX, S>();       \
         else prepare_zmarch_t<double, TY, TX, S>();               \
         break;
+#define AXS_ZP2(I, TY, TX, S)                                     \
+    case I:                                                       \
+        if (esz == 4) prepare_zmarch2_t<float, TY, TX, S>();      \
+        else prepare_zmarch2_t<double, TY, TX, S>();              \
+        break;
     switch (variant) {
         AXS_ZP(0, 8, 128, 4)
         AXS_ZP(1, 8, 128, 5)
         AXS_ZP(2, 16, 128, 4)
         AXS_ZP(3, 4, 256, 4)
         AXS_ZP(4, 8, 256, 4)
+        AXS_ZP2(5, 8, 128, 4)
+        AXS_ZP2(6, 8, 128, 5)
+        AXS_ZP2(7, 4, 256, 5)
+        AXS_ZP2(8, 8, 256, 5)
+        AXS_ZP2(9, 4, 128, 6)
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
 #undef AXS_ZP
+#undef AXS_ZP2
+}
+
+// Dynamic shared memory of a variant (mirrors ZCfg / Z2Cfg).
+static int variant_smem(const ZVariant &v, int esz) {
+    int cs = 2 * esz;
+    int c_bytes = (v.ty + 2) * v.txmax * cs;
+    int h_pad = (v.ty * 16 + 127) / 128 * 128;
+    if (v.gen == 1) return v.slots * ((c_bytes + 2 * h_pad + 127) / 128 * 128) + 128;
+    return v.slots * ((c_bytes + 2 * h_pad + v.ty * v.txmax * cs + 127) / 128 * 128) + 256;
+}
+
+static int max_smem_optin() {
+    static int m = 0;
+    if (!m) {
+        int dev = 0;
+        AXS_CUDA(cudaGetDevice(&dev));
+        AXS_CUDA(cudaDeviceGetAttribute(&m, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    }
+    return m;
 }
 
 // The tx a variant would use for an N (largest admissible divisor), or 0.
@@ -510,6 +823,7 @@ static int variant_tx(const ZVariant &v, int N, int esz) {
     int vs = 16 / cs;
     int txmax = v.txmax;
     if (esz == 8) txmax = std::min(txmax, 128);   // box inner dim: 2*tx doubles <= 256
+    if (variant_smem(v, esz) > max_smem_optin()) return 0;
     if (N % v.ty != 0 || N < 4) return 0;
     for (int tx = std::min(txmax, N); tx >= vs; --tx) {
         if (N % tx) continue;
@@ -571,6 +885,7 @@ static int64_t fill_zlat(ZLat &z, Lattice *L, int variant, int zchunk, int64_t i
         encode_map(&z.tm_xh[b], L->psi[b], N, L->esz, vs, v.ty);
         z.psi[b] = L->psi[b];
     }
+    encode_map(&z.tm_pih, L->pih, N, L->esz, tx, v.ty);
     z.pih = L->pih;
     z.clock = L->dclock;
     z.N = N;

@@ -60,7 +60,8 @@ def test_kernel_variants_bit_identical(axs, oracle, precision):
     op = orc(p)
     f = oracle.init_thermal(op, 5)
     outs = []
-    for force in ["0,0,64", "1,0,32", "1,1,64", "1,2,64", "1,3,128", "1,4,32"]:
+    for force in ["0,0,64", "1,0,32", "1,1,64", "1,2,64", "1,3,128", "1,4,32",
+                  "1,5,64", "1,6,32", "1,7,64", "1,8,128", "1,9,16"]:
         os.environ["AXS_FORCE_CONFIG"] = force
         try:
             with axs.Lattice(p) as L:
