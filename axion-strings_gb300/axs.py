@@ -89,6 +89,7 @@ _sig("axs_axion_spectrum", [_vp, ctypes.c_int, _vp, _vp, _vp])
 _sig("axs_background", [_vp, _vp])
 _sig("axs_energies", [_vp, _vp])
 _sig("axs_check_finite", [_vp, ctypes.POINTER(ctypes.c_int)])
+_sig("axs_field_distance", [_vp, _vp, _vp])
 _sig("axs_checkpoint_size", [_vp, ctypes.POINTER(ctypes.c_size_t)])
 _sig("axs_checkpoint", [_vp, _vp, ctypes.c_size_t])
 _sig("axs_restore", [_vp, _vp, ctypes.c_size_t])
@@ -135,6 +136,14 @@ def xi(params, n_plaquettes, num_cores, tau):
     out = ctypes.c_float()
     _check(_lib.axs_xi(ctypes.byref(params), int(n_plaquettes), int(num_cores), float(tau), ctypes.byref(out)))
     return out.value
+
+
+def field_distance(a, b):
+    """Relative L2 distance per field (phi1, phi2, phidot1, phidot2) of lattice
+    a from lattice b: sqrt(sum (a-b)^2 / sum b^2), computed on the device."""
+    out = np.empty(8)
+    _check(_lib.axs_field_distance(a._h, b._h, _ptr(out)))
+    return np.sqrt(out[0::2] / np.where(out[1::2] > 0, out[1::2], 1.0))
 
 
 def kernel_launches():

@@ -873,3 +873,53 @@ extern "C" int axs_powerspec_noalloc(const void *spectrum, int NDIMS, int N, int
     }
     return AXS_OK;
 }
+
+namespace axs {
+
+// ============================================================== lattice distance
+//
+// Per field f of (phi1, phi2, phidot1, phidot2): sum (a_f - b_f)^2 and sum b_f^2
+// over the lattice, both in FP64 with a fixed reduction order. a and b are the
+// synchronised states (psi and pi_n) of two lattices of the same shape, any
+// precision each.
+template <typename TA, typename TB>
+__global__ void __launch_bounds__(256) k_distance(const typename Cplx<TA>::type *__restrict__ pa,
+                                                  const typename Cplx<TA>::type *__restrict__ qa,
+                                                  const typename Cplx<TB>::type *__restrict__ pb,
+                                                  const typename Cplx<TB>::type *__restrict__ qb, int64_t len,
+                                                  double *__restrict__ partials) {
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        auto a0 = pa[m], a1 = qa[m];
+        auto b0 = pb[m], b1 = qb[m];
+        double av[4] = {(double)a0.x, (double)a0.y, (double)a1.x, (double)a1.y};
+        double bv[4] = {(double)b0.x, (double)b0.y, (double)b1.x, (double)b1.y};
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+            double d = av[f] - bv[f];
+            acc[2 * f] += d * d;
+            acc[2 * f + 1] += bv[f] * bv[f];
+        }
+    }
+    block_reduce_store<8>(acc, partials);
+}
+
+void field_distance(Lattice *A, Lattice *B, double out[8]) {
+    if (A->p.NDIMS != B->p.NDIMS || A->p.N != B->p.N) fail(AXS_ERR_ARG, "lattices differ in shape");
+    launch_sync_pi(A);
+    launch_sync_pi(B);
+    AXS_CUDA(cudaStreamSynchronize(A->stream));   // B's kernels below run on B's stream
+    int g = reduce_grid(A->length);
+    double *part = ensure_partials(B, g, 8);
+    const void *pa = A->psi[A->cur], *qa = A->scratch, *pb = B->psi[B->cur], *qb = B->scratch;
+    if (A->esz == 4 && B->esz == 4) k_distance<float, float><<<g, 256, 0, B->stream>>>((const float2 *)pa, (const float2 *)qa, (const float2 *)pb, (const float2 *)qb, A->length, part);
+    else if (A->esz == 4) k_distance<float, double><<<g, 256, 0, B->stream>>>((const float2 *)pa, (const float2 *)qa, (const double2 *)pb, (const double2 *)qb, A->length, part);
+    else if (B->esz == 4) k_distance<double, float><<<g, 256, 0, B->stream>>>((const double2 *)pa, (const double2 *)qa, (const float2 *)pb, (const float2 *)qb, A->length, part);
+    else k_distance<double, double><<<g, 256, 0, B->stream>>>((const double2 *)pa, (const double2 *)qa, (const double2 *)pb, (const double2 *)qb, A->length, part);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+    sum_partials(part, g, 8, out, B->stream);
+}
+
+}  // namespace axs

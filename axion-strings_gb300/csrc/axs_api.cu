@@ -452,6 +452,13 @@ int axs_check_finite(axs_lattice *h, int *finite) {
     API_END
 }
 
+int axs_field_distance(axs_lattice *a, axs_lattice *b, double out[8]) {
+    API_BEGIN
+    if (!a || !b || !out) fail(AXS_ERR_ARG, "null argument");
+    field_distance(&a->L, &b->L, out);
+    API_END
+}
+
 int axs_checkpoint_size(axs_lattice *h, size_t *bytes) {
     API_BEGIN
     CHECK_HANDLE(h);

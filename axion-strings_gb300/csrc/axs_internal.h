@@ -155,6 +155,7 @@ void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *c
 void background(Lattice *L, double out[6]);
 void energies(Lattice *L, double out[3]);
 int check_finite(Lattice *L);
+void field_distance(Lattice *A, Lattice *B, double out[8]);
 void analysis_release(Lattice *L);
 
 // helpers

@@ -290,18 +290,18 @@ def gpu_arm(args, dist):
     axs.set_device(dist.local)
     hbm, peak_note = peaks()
     sampler = ClockSampler(dist.local)
-    main = run_lattice(axs, dist, 32, args.steps, args.warmup, with_e2e=not args.no_e2e, sampler=sampler, n=args.n)
+    main = run_lattice(axs, dist, args.precision, args.steps, args.warmup, with_e2e=not args.no_e2e, sampler=sampler,
+                       n=args.n)
     sites_all = dist.sum(main["sites"])
     value = sites_all * args.steps / (main["ms"] * 1e-3)
     per_launch_ms = main["ms"] / args.steps
-    achieved = BYTES_PER_SITE[32] * main["sites"] / (per_launch_ms * 1e-3) / 1e9
+    achieved = BYTES_PER_SITE[args.precision] * main["sites"] / (per_launch_ms * 1e-3) / 1e9
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tfile):
-        try:
-            traffic = json.load(open(tfile)).get("zmarch_fp32_1024_per_launch_bytes")
-        except Exception:
-            traffic = None
+    tfile = os.path.join(ROOT, "profiles", "k_zmarch_traffic.txt")
+    if args.precision == 32 and args.n == N_MAIN and os.path.exists(tfile):
+        for line in open(tfile):
+            if line.startswith("zmarch_fp32_1024_per_launch_bytes:"):
+                traffic = float(line.split(":", 1)[1]) / 1e9     # GB per launch, like `achieved`'s bytes
     fp64 = ens = None
     if not args.quick:
         f64 = run_lattice(axs, dist, 64, max(3, args.steps // 2), args.warmup, with_e2e=False, n=args.n)
@@ -331,14 +331,17 @@ def gpu_arm(args, dist):
     line = {
         "metric": "site-updates/s", "value": value, "unit": "site-updates/s", "n_gpus": dist.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": main["ms"] / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "3D %d^3 FP32 leapfrog step, 7-point stencil, prs=0, lambda=1, dx=0.5, dt=0.1, "
-                               "flat k_cut=1 start" % args.n, "N": args.n, "precision": "fp32 fields, fp64 tau",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic",
+        "config": {"workload": "3D %d^3 FP%d leapfrog step, 7-point stencil, prs=0, lambda=1, dx=0.5, dt=0.1, "
+                               "flat k_cut=1 start" % (args.n, args.precision), "N": args.n, "precision": "fp32 fields, fp64 tau",
                    "parallelism": "replicas" if dist.world > 1 else "single",
                    "l2": "state 25.8 GB >> 129 MB L2; no flush needed", "kernel": main["desc"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "peak_source": peak_note,
-                     "algorithmic_bytes_per_site_update": BYTES_PER_SITE[32]},
+                     "traffic": traffic, "traffic_unit": "GB per launch (ncu dram read+write)",
+                     "algorithmic_gb_per_launch": BYTES_PER_SITE[args.precision] * main["sites"] / 1e9,
+                     "peak_source": peak_note,
+                     "algorithmic_bytes_per_site_update": BYTES_PER_SITE[args.precision]},
         "cpu_baseline": cpu,
         "e2e": e2e_line,
         "gpu_launches": main["launches"],
@@ -359,6 +362,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     ap.add_argument("--n", type=int, default=N_MAIN, help="lattice side (profiling cases use smaller N)")
+    ap.add_argument("--precision", type=int, default=32, choices=[32, 64],
+                    help="headline leg precision (64 only for profiling the FP64 step)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -209,6 +209,12 @@ int axs_energies(axs_lattice *h, double out[3]);
 /* *finite = 1 when no NaN/Inf is in the fields (the check of s_run.cpp:4-12). */
 int axs_check_finite(axs_lattice *h, int *finite);
 
+/* Distance between the synchronised states of two lattices of the same shape
+ * (any precisions; no reference counterpart): for each field f of (phi1, phi2,
+ * phidot1, phidot2), out[2f] = sum (a_f - b_f)^2 and out[2f+1] = sum b_f^2,
+ * FP64 with a fixed reduction order. Used to state FP32 errors against FP64. */
+int axs_field_distance(axs_lattice *a, axs_lattice *b, double out[8]);
+
 /* ---- checkpoint / resume (no reference counterpart on the standard path) ----------- */
 
 /* Bytes needed for a checkpoint of this lattice. */
