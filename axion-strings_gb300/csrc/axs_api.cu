@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <cmath>
+#include <map>
 #include <new>
 #include <vector>
 #include <algorithm>
@@ -121,8 +122,11 @@ static void lattice_init(Lattice *L, const axs_params &p, cudaStream_t shared) {
     AXS_CUDA(cudaStreamSynchronize(L->stream));
 }
 
+static void xfer_release(Lattice *L);
+
 static void lattice_free(Lattice *L) {
     if (L->stream) cudaStreamSynchronize(L->stream);
+    xfer_release(L);
     step_release(L);
     analysis_release(L);
     dfree(L->psi[0]);
@@ -141,15 +145,136 @@ static void *stage(Lattice *L) {
     return L->dstage;
 }
 
+// Device-addressable alias of a caller buffer (device or managed memory, or
+// page-locked host memory, which the GPU reads and writes over NVLink-C2C /
+// PCIe), or nullptr for pageable host memory.
+static void *device_alias(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return const_cast<void *>(p);
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+    return nullptr;
+}
+
+// Chunked, double-buffered staging of pageable host arrays: copies run on a
+// second stream and overlap the (un)packing kernels on the lattice stream.
+static const int64_t kXferChunk = (int64_t)1 << 25;   // elements per chunk
+
+struct Xfer {
+    cudaStream_t copy = nullptr;
+    cudaEvent_t copied[2] = {nullptr, nullptr}, done[2] = {nullptr, nullptr}, entry = nullptr;
+    char *buf = nullptr;   // [2 slots][2 arrays][chunk] of 8-byte elements
+    int64_t chunk = 0;     // elements per chunk (<= kXferChunk, <= the lattice length)
+};
+static std::map<Lattice *, Xfer> g_xfer;
+
+static Xfer &xfer(Lattice *L) {
+    Xfer &x = g_xfer[L];
+    if (!x.buf) {
+        AXS_CUDA(cudaStreamCreateWithFlags(&x.copy, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; ++i) {
+            AXS_CUDA(cudaEventCreateWithFlags(&x.copied[i], cudaEventDisableTiming));
+            AXS_CUDA(cudaEventCreateWithFlags(&x.done[i], cudaEventDisableTiming));
+        }
+        AXS_CUDA(cudaEventCreateWithFlags(&x.entry, cudaEventDisableTiming));
+        x.chunk = std::min(kXferChunk, L->length);
+        x.buf = (char *)dalloc((size_t)4 * x.chunk * sizeof(double));
+    }
+    return x;
+}
+static void xfer_release(Lattice *L) {
+    auto it = g_xfer.find(L);
+    if (it == g_xfer.end()) return;
+    Xfer &x = it->second;
+    if (x.copy) { cudaStreamSynchronize(x.copy); cudaStreamDestroy(x.copy); }
+    for (int i = 0; i < 2; ++i) {
+        if (x.copied[i]) cudaEventDestroy(x.copied[i]);
+        if (x.done[i]) cudaEventDestroy(x.done[i]);
+    }
+    if (x.entry) cudaEventDestroy(x.entry);
+    dfree(x.buf);
+    g_xfer.erase(it);
+}
+
+template <typename S>
+static void upload_pair(Lattice *L, const S *a, const S *b, void *dst) {
+    const int is_d = sizeof(S) == 8;
+    void *da = device_alias(a), *db = device_alias(b);
+    if (da && db) {
+        launch_pack2(L, da, db, is_d, dst, L->length, L->stream);
+        return;
+    }
+    Xfer &x = xfer(L);
+    // the staging slots may still be read by packing kernels of an earlier
+    // transfer on the lattice stream: copies start after them
+    AXS_CUDA(cudaEventRecord(x.entry, L->stream));
+    AXS_CUDA(cudaStreamWaitEvent(x.copy, x.entry, 0));
+    const size_t cs = (size_t)2 * L->esz;
+    int64_t nch = (L->length + x.chunk - 1) / x.chunk;
+    for (int64_t c = 0; c < nch; ++c) {
+        int s = (int)(c & 1);
+        int64_t off = c * x.chunk, n = std::min(x.chunk, L->length - off);
+        char *sa = x.buf + (size_t)(2 * s) * x.chunk * sizeof(double);
+        char *sb = sa + (size_t)x.chunk * sizeof(double);
+        if (c >= 2) AXS_CUDA(cudaStreamWaitEvent(x.copy, x.done[s], 0));
+        AXS_CUDA(cudaMemcpyAsync(sa, a + off, (size_t)n * sizeof(S), cudaMemcpyHostToDevice, x.copy));
+        AXS_CUDA(cudaMemcpyAsync(sb, b + off, (size_t)n * sizeof(S), cudaMemcpyHostToDevice, x.copy));
+        AXS_CUDA(cudaEventRecord(x.copied[s], x.copy));
+        AXS_CUDA(cudaStreamWaitEvent(L->stream, x.copied[s], 0));
+        launch_pack2(L, sa, sb, is_d, (char *)dst + (size_t)off * cs, n, L->stream);
+        AXS_CUDA(cudaEventRecord(x.done[s], L->stream));
+    }
+}
+
+template <typename S>
+static void download_pair(Lattice *L, const void *src, S *a, S *b) {
+    const int is_d = sizeof(S) == 8;
+    void *da = device_alias(a), *db = device_alias(b);
+    if (da && db) {
+        launch_unpack2(L, src, da, db, is_d, L->length, L->stream);
+        return;
+    }
+    Xfer &x = xfer(L);
+    // unpacking into the staging slots starts after earlier copies out of them
+    AXS_CUDA(cudaEventRecord(x.entry, x.copy));
+    AXS_CUDA(cudaStreamWaitEvent(L->stream, x.entry, 0));
+    const size_t cs = (size_t)2 * L->esz;
+    int64_t nch = (L->length + x.chunk - 1) / x.chunk;
+    for (int64_t c = 0; c < nch; ++c) {
+        int s = (int)(c & 1);
+        int64_t off = c * x.chunk, n = std::min(x.chunk, L->length - off);
+        char *sa = x.buf + (size_t)(2 * s) * x.chunk * sizeof(double);
+        char *sb = sa + (size_t)x.chunk * sizeof(double);
+        if (c >= 2) AXS_CUDA(cudaStreamWaitEvent(L->stream, x.done[s], 0));
+        launch_unpack2(L, (const char *)src + (size_t)off * cs, sa, sb, is_d, n, L->stream);
+        AXS_CUDA(cudaEventRecord(x.copied[s], L->stream));
+        AXS_CUDA(cudaStreamWaitEvent(x.copy, x.copied[s], 0));
+        AXS_CUDA(cudaMemcpyAsync(a + off, sa, (size_t)n * sizeof(S), cudaMemcpyDeviceToHost, x.copy));
+        AXS_CUDA(cudaMemcpyAsync(b + off, sb, (size_t)n * sizeof(S), cudaMemcpyDeviceToHost, x.copy));
+        AXS_CUDA(cudaEventRecord(x.done[s], x.copy));
+    }
+    AXS_CUDA(cudaStreamSynchronize(x.copy));
+}
+
 template <typename S>
 static void upload_fields(Lattice *L, const S *f0, const S *f1, const S *f2, const S *f3) {
     const S *src[4] = {f0, f1, f2, f3};
-    void *st = stage(L);
     const int is_d = sizeof(S) == 8;
-    for (int f = 0; f < 4; ++f) {
-        if (!src[f]) continue;
-        AXS_CUDA(cudaMemcpyAsync(st, src[f], (size_t)L->length * sizeof(S), cudaMemcpyHostToDevice, L->stream));
-        launch_pack(L, st, is_d, f >= 2 ? 1 : 0, f & 1);
+    for (int pr = 0; pr < 2; ++pr) {
+        void *dst = pr == 0 ? L->psi[L->cur] : L->pih;
+        if (src[2 * pr] && src[2 * pr + 1]) {
+            upload_pair<S>(L, src[2 * pr], src[2 * pr + 1], dst);
+            continue;
+        }
+        for (int f = 2 * pr; f < 2 * pr + 2; ++f) {   // one component of the pair
+            if (!src[f]) continue;
+            void *st = stage(L);
+            AXS_CUDA(cudaMemcpyAsync(st, src[f], (size_t)L->length * sizeof(S), cudaMemcpyHostToDevice, L->stream));
+            launch_pack(L, st, is_d, pr, f & 1);
+        }
     }
     L->fresh = 1;
     L->last_nplaq = -1;
@@ -161,14 +286,21 @@ static void upload_fields(Lattice *L, const S *f0, const S *f1, const S *f2, con
 template <typename S>
 static void download_fields(Lattice *L, S *f0, S *f1, S *f2, S *f3) {
     S *dst[4] = {f0, f1, f2, f3};
-    void *st = stage(L);
     const int is_d = sizeof(S) == 8;
     if (f2 || f3) launch_sync_pi(L);
-    for (int f = 0; f < 4; ++f) {
-        if (!dst[f]) continue;
-        const void *src = f >= 2 ? L->scratch : L->psi[L->cur];
-        launch_unpack(L, src, 0, f & 1, st, is_d);
-        AXS_CUDA(cudaMemcpyAsync(dst[f], st, (size_t)L->length * sizeof(S), cudaMemcpyDeviceToHost, L->stream));
+    for (int pr = 0; pr < 2; ++pr) {
+        const void *src = pr == 1 ? L->scratch : L->psi[L->cur];
+        if (dst[2 * pr] && dst[2 * pr + 1]) {
+            download_pair<S>(L, src, dst[2 * pr], dst[2 * pr + 1]);
+            continue;
+        }
+        for (int f = 2 * pr; f < 2 * pr + 2; ++f) {
+            if (!dst[f]) continue;
+            void *st = stage(L);
+            launch_unpack(L, src, 0, f & 1, st, is_d);
+            AXS_CUDA(cudaMemcpyAsync(dst[f], st, (size_t)L->length * sizeof(S), cudaMemcpyDeviceToHost, L->stream));
+            AXS_CUDA(cudaStreamSynchronize(L->stream));
+        }
     }
     AXS_CUDA(cudaStreamSynchronize(L->stream));
     check_device_errors(L);

@@ -141,6 +141,9 @@ void launch_sync_pi(Lattice *L);                      // scratch <- pi_n
 void launch_laplacian(Lattice *L, int comp, double *dout);
 void launch_unpack(Lattice *L, const void *src, int which, int comp, void *dst_real, int dst_is_double);
 void launch_pack(Lattice *L, const void *src_real, int src_is_double, int which, int comp);
+void launch_pack2(Lattice *L, const void *a, const void *b, int src_is_double, void *dst_cplx, int64_t n,
+                  cudaStream_t st);
+void launch_unpack2(Lattice *L, const void *src_cplx, void *a, void *b, int dst_is_double, int64_t n, cudaStream_t st);
 void check_device_errors(Lattice *L);
 void check_device_error_flag(int *derr, cudaStream_t s);
 

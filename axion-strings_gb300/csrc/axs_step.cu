@@ -165,6 +165,31 @@ __global__ void k_unpack(const T *__restrict__ src_cplx, S *__restrict__ dst, in
         dst[m] = (S)src_cplx[2 * m + comp];
 }
 
+// Two real host-order arrays <-> a complex device array (whole 8/16-byte
+// sites, so no partial-sector writes). Either side may be host memory the
+// device can address (page-locked, reached over NVLink-C2C) or device memory.
+template <typename T, typename S>
+__global__ void k_pack2(const S *__restrict__ a, const S *__restrict__ b, typename Cplx<T>::type *__restrict__ dst,
+                        int64_t len) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        typename Cplx<T>::type v;
+        v.x = (T)a[m];
+        v.y = (T)b[m];
+        dst[m] = v;
+    }
+}
+template <typename T, typename S>
+__global__ void k_unpack2(const typename Cplx<T>::type *__restrict__ src, S *__restrict__ a, S *__restrict__ b,
+                          int64_t len) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        typename Cplx<T>::type v = src[m];
+        a[m] = (S)v.x;
+        b[m] = (S)v.y;
+    }
+}
+
 // ============================================================== z-march kernel
 //
 // 3D, radius 1. A work item is (lattice, x-y tile of tx * TY sites, z-chunk).
@@ -1451,6 +1476,34 @@ void launch_unpack(Lattice *L, const void *src, int which, int comp, void *dst_r
     } else {
         if (dst_is_double) k_unpack<double, double><<<g, 256, 0, L->stream>>>((const double *)src, (double *)dst_real, comp, L->length);
         else k_unpack<double, float><<<g, 256, 0, L->stream>>>((const double *)src, (float *)dst_real, comp, L->length);
+    }
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+
+// Pair transfers: dst/src complex array <-> (a, b) real arrays reachable by
+// the device (device pointers or device aliases of page-locked host memory).
+void launch_pack2(Lattice *L, const void *a, const void *b, int src_is_double, void *dst_cplx, int64_t n,
+                  cudaStream_t st) {
+    int g = grid_for(n);
+    if (L->esz == 4) {
+        if (src_is_double) k_pack2<float, double><<<g, 256, 0, st>>>((const double *)a, (const double *)b, (float2 *)dst_cplx, n);
+        else k_pack2<float, float><<<g, 256, 0, st>>>((const float *)a, (const float *)b, (float2 *)dst_cplx, n);
+    } else {
+        if (src_is_double) k_pack2<double, double><<<g, 256, 0, st>>>((const double *)a, (const double *)b, (double2 *)dst_cplx, n);
+        else k_pack2<double, float><<<g, 256, 0, st>>>((const float *)a, (const float *)b, (double2 *)dst_cplx, n);
+    }
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+void launch_unpack2(Lattice *L, const void *src_cplx, void *a, void *b, int dst_is_double, int64_t n, cudaStream_t st) {
+    int g = grid_for(n);
+    if (L->esz == 4) {
+        if (dst_is_double) k_unpack2<float, double><<<g, 256, 0, st>>>((const float2 *)src_cplx, (double *)a, (double *)b, n);
+        else k_unpack2<float, float><<<g, 256, 0, st>>>((const float2 *)src_cplx, (float *)a, (float *)b, n);
+    } else {
+        if (dst_is_double) k_unpack2<double, double><<<g, 256, 0, st>>>((const double2 *)src_cplx, (double *)a, (double *)b, n);
+        else k_unpack2<double, float><<<g, 256, 0, st>>>((const double2 *)src_cplx, (float *)a, (float *)b, n);
     }
     AXS_CUDA(cudaGetLastError());
     count_launches(1);
