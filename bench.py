@@ -235,10 +235,15 @@ def e2e_leg(axs, L, dist, steps):
             "string_count": int(n), "site_updates_per_s": sites * steps / wall}
 
 
+def ensemble_shard(n_total, rank, world):
+    """Realisations owned by `rank`: round-robin, disjoint, covering all."""
+    return [i for i in range(n_total) if i % world == rank]
+
+
 def run_ensemble(axs, dist, steps, warmup, master_seed=2026):
     rng = np.random.default_rng(master_seed)
     n_total = 96
-    mine = [i for i in range(n_total) if i % dist.world == dist.rank]   # realisations shard across ranks
+    mine = ensemble_shard(n_total, dist.rank, dist.world)   # no data-path collective between ranks
     sizes = rng.choice(ENSEMBLE_SIZES, size=n_total)
     lams = np.exp(rng.uniform(np.log(0.5), np.log(4.0), size=n_total))
     seeds = rng.integers(1, 2 ** 31, size=n_total)
