@@ -98,6 +98,7 @@ _sig("axs_ensemble_destroy", [_vp])
 _sig("axs_ensemble_member", [_vp, ctypes.c_int, ctypes.POINTER(_vp)])
 _sig("axs_ensemble_evolve", [_vp, ctypes.c_int])
 _sig("axs_ensemble_evolve_timed", [_vp, ctypes.c_int, _dp])
+_sig("axs_inject_wait_timeout", [_vp])
 _sig("axs_autotune", [_vp])
 _sig("axs_describe", [_vp, ctypes.c_char_p, ctypes.c_size_t])
 _sig("axs_kernel_launches", [], ctypes.c_int64)
@@ -323,6 +324,10 @@ class Lattice:
     def restore(self, buf):
         buf = np.ascontiguousarray(buf, dtype=np.uint8)
         _check(_lib.axs_restore(self._h, _ptr(buf), buf.size))
+
+    def inject_wait_timeout(self):
+        """Test-only: make the next step's device-side waits run out."""
+        _check(_lib.axs_inject_wait_timeout(self._h))
 
     # tuning
     def autotune(self):

@@ -118,6 +118,75 @@ __global__ void __launch_bounds__(256) k_cores(const typename Cplx<T>::type *__r
     if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
 }
 
+// 3D finder from psi, tiled: a block owns a CX x CY tile of cells and marches a
+// z-chunk; the normalised angles n = (theta+pi)/(2pi) of the tile's sites (one
+// site of halo in +x and +y) are computed once per site into a two-plane
+// shared ring (k_cores evaluates them once per corner, six times per site).
+// Same float n, same margin test, same double replay: same decisions.
+static constexpr int kCX = 32, kCY = 8, kCZ = 32;
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_cores3_tiled(const typename Cplx<T>::type *__restrict__ psi,
+                                                      uint8_t *__restrict__ mask, int N, double accept,
+                                                      unsigned long long *count) {
+    __shared__ float nsm[2][kCY + 1][kCX + 1];
+    Corner<T, false> cn{psi, nullptr};
+    const float acc_f = (float)accept;
+    const int64_t NN = (int64_t)N * N;
+    const int x0 = blockIdx.x * kCX, y0 = blockIdx.y * kCY, z0 = blockIdx.z * kCZ;
+    const int z1 = min(N, z0 + kCZ);
+    const int tid = threadIdx.x;
+    const int cx = tid % kCX, cy = tid / kCX;
+    unsigned long long local = 0;
+    auto fill = [&](int buf, int z) {   // n of plane z (wrapped) for the tile + halo
+        const int64_t zb = (int64_t)(z == N ? 0 : z) * NN;
+        for (int s = tid; s < (kCX + 1) * (kCY + 1); s += 256) {
+            int sx = s % (kCX + 1), sy = s / (kCX + 1);
+            int gx = x0 + sx, gy = y0 + sy;
+            if (gx > N || gy > N) continue;
+            gx = gx >= N ? gx - N : gx;
+            gy = gy >= N ? gy - N : gy;
+            nsm[buf][sy][sx] = cn.nf(zb + (int64_t)gy * N + gx);
+        }
+    };
+    fill(0, z0);
+    for (int z = z0; z < z1; ++z) {
+        const int cur = (z - z0) & 1;
+        fill(cur ^ 1, z + 1);
+        __syncthreads();
+        const int x = x0 + cx, y = y0 + cy;
+        if (x < N && y < N) {
+            const float f000 = nsm[cur][cy][cx], f100 = nsm[cur ^ 1][cy][cx], f110 = nsm[cur ^ 1][cy + 1][cx],
+                        f010 = nsm[cur][cy + 1][cx], f011 = nsm[cur][cy + 1][cx + 1], f001 = nsm[cur][cy][cx + 1];
+            const float e_000_100 = circf(f000, f100);
+            const float e_011_001 = circf(f011, f001);
+            const float sa = e_000_100 + circf(f100, f110) + circf(f110, f010);
+            const float sb = e_000_100 + circf(f100, f011) + e_011_001;   // plaquette b, string_finding.cpp:54-57
+            const float sc = circf(f000, f010) + circf(f010, f011) + e_011_001;
+            const float mx = fmaxf(sa, fmaxf(sb, sc));
+            int flag;
+            const int64_t m = (int64_t)z * NN + (int64_t)y * N + x;
+            if (mx > acc_f + kMargin) flag = 1;
+            else if (mx < acc_f - kMargin) flag = 0;
+            else {
+                const int64_t xp = x + 1 == N ? 0 : x + 1, yp = y + 1 == N ? 0 : y + 1, zp = z + 1 == N ? 0 : z + 1;
+                const double d000 = cn.nd(m), d100 = cn.nd(zp * NN + (int64_t)y * N + x),
+                             d110 = cn.nd(zp * NN + yp * N + x), d010 = cn.nd((int64_t)z * NN + yp * N + x),
+                             d011 = cn.nd((int64_t)z * NN + yp * N + xp), d001 = cn.nd((int64_t)z * NN + (int64_t)y * N + xp);
+                const double ta = sum3(circd(d000, d100), circd(d100, d110), circd(d110, d010));
+                const double tb = sum3(circd(d000, d100), circd(d100, d011), circd(d011, d001));
+                const double tc = sum3(circd(d000, d010), circd(d010, d011), circd(d011, d001));
+                flag = (ta > accept || tb > accept || tc > accept);
+            }
+            mask[m] = (uint8_t)flag;
+            local += flag;
+        }
+        __syncthreads();   // the plane just used as z+1 becomes z; the other buffer is refilled next
+    }
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
+}
+
 // ---- ordered compaction of the mask: chunk counts, scan, ordered write
 static constexpr int kChunk = 4096;   // cells per block
 
@@ -248,7 +317,10 @@ static void launch_cores(Lattice *L, bool from_theta, double accept, unsigned lo
         else k_cores<T, 2, false><<<g, 256, 0, L->stream>>>(psi, nullptr, L->dmask, N, L->length, accept, cnt);
     } else {
         if (from_theta) k_cores<T, 3, true><<<g, 256, 0, L->stream>>>(psi, L->dtheta, L->dmask, N, L->length, accept, cnt);
-        else k_cores<T, 3, false><<<g, 256, 0, L->stream>>>(psi, nullptr, L->dmask, N, L->length, accept, cnt);
+        else {
+            dim3 grid((N + kCX - 1) / kCX, (N + kCY - 1) / kCY, (N + kCZ - 1) / kCZ);
+            k_cores3_tiled<T><<<grid, 256, 0, L->stream>>>(psi, L->dmask, N, accept, cnt);
+        }
     }
     AXS_CUDA(cudaGetLastError());
     count_launches(1);

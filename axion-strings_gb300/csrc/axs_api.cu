@@ -729,6 +729,20 @@ int axs_ensemble_evolve_timed(axs_ensemble *e, int nsteps, double *ms) {
     API_END
 }
 
+int axs_inject_wait_timeout(axs_lattice *h) {
+    API_BEGIN
+    CHECK_HANDLE(h);
+    Lattice *L = &h->L;
+    if (L->in_ensemble) fail(AXS_ERR_STATE, "inject on a lattice that is not an ensemble member");
+    if (!L->tuned) lattice_autotune(L);
+    if (L->cfg.kind != 1) fail(AXS_ERR_STATE, "the step kernel in use (%s) has no device-side waits", L->cfg.describe().c_str());
+    L->debug_tx_excess = 16;
+    L->zlat_variant = -1;
+    for (auto &g : L->graphs) cudaGraphExecDestroy(g.second);
+    L->graphs.clear();
+    API_END
+}
+
 int axs_autotune(axs_lattice *h) {
     API_BEGIN
     CHECK_HANDLE(h);

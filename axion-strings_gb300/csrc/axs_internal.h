@@ -66,7 +66,8 @@ struct ZLat {
     int a_index;             // which of psi[0]/psi[1] is "current" at launch parity 0
     int64_t item_base;
     double dt, inv_dx2, lambda, T0sq3;
-    int prs, pad_;
+    int prs;
+    int debug_tx_excess;     // test-only: bytes the first load of each item expects but never gets
 };
 
 struct GraphKey {
@@ -96,6 +97,7 @@ struct Lattice {
     // z-march launch table for this lattice alone
     ZLat *dzlat = nullptr;
     int zlat_variant = -1, zlat_tx = -1, zlat_zchunk = -1, zlat_a_index = 0;
+    int debug_tx_excess = 0;  // set by axs_inject_wait_timeout for one step
     int64_t zitems = 0;
     // analysis buffers (lazily allocated)
     uint8_t *dmask = nullptr;

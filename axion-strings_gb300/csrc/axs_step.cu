@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(256) k_zmarch(const ZLat *__restrict__ lats, i
             const int s = (int)(q % S);
             unsigned char *slot = smem + s * K::SLOT;
             const uint32_t bar = smem_u32(&bars[s]);
-            mbar_expect_tx(bar, slot_bytes_tx);
+            mbar_expect_tx(bar, slot_bytes_tx + (i == 0 ? (uint32_t)Lt.debug_tx_excess : 0u));
             const int ym = y0 == 0 ? N - 1 : y0 - 1;
             const int yp = (y0 + TY == N) ? 0 : y0 + TY;
             tma_load_3d(smem_u32(slot), &Lt.tm_row[bin], x0 * K::EU, ym, z, bar);
@@ -543,7 +543,8 @@ __global__ void __launch_bounds__(Z2Cfg<T, TY, TXMAX, S>::NT)
                     unsigned char *slot = smem + s * K::SLOT;
                     const uint32_t bar = smem_u32(&full[s]);
                     const bool with_pih = i >= 1 && i <= nload - 2;
-                    mbar_expect_tx(bar, psi_bytes + (with_pih ? pih_bytes : 0u));
+                    mbar_expect_tx(bar, psi_bytes + (with_pih ? pih_bytes : 0u) +
+                                            (i == 0 ? (uint32_t)Lt.debug_tx_excess : 0u));
                     tma_load_3d(smem_u32(slot), &Lt.tm_row[bin], x0 * K::EU, ym, z, bar);
                     tma_load_3d(smem_u32(slot + tx * K::CS), &Lt.tm_main[bin], x0 * K::EU, y0, z, bar);
                     tma_load_3d(smem_u32(slot + (TY + 1) * tx * K::CS), &Lt.tm_row[bin], x0 * K::EU, yp, z, bar);
@@ -927,6 +928,7 @@ static int64_t fill_zlat(ZLat &z, Lattice *L, int variant, int zchunk, int64_t i
     double T0 = (double)L->p.T_initial;
     z.T0sq3 = (T0 * T0) / 3.0;
     z.prs = L->p.prs;
+    z.debug_tx_excess = L->debug_tx_excess;
     return (int64_t)z.ntx * z.nty * z.nzc;
 }
 
@@ -1023,6 +1025,10 @@ void lattice_step_once(Lattice *L) {
         int parity = L->cur ^ L->zlat_a_index;
         launch_zmarch(L->esz, L->cfg.variant, L->dzlat, 1, L->zitems, L->dcounter, parity, L->derr, L->stream,
                       L->cfg.ctas_per_sm);
+        if (L->debug_tx_excess) {   // an injected stall lasts one step: rebuild the table before the next
+            L->debug_tx_excess = 0;
+            L->zlat_variant = -1;
+        }
     } else {
         if (L->esz == 4) launch_generic_dispatch<float>(L, cin, cout);
         else launch_generic_dispatch<double>(L, cin, cout);

@@ -200,6 +200,17 @@ def run_lattice(axs, dist, precision, steps, warmup, with_e2e, sampler=None, n=N
     ms_max = dist.max(ms)
     rec = {"ms": ms_max, "launches": launches, "desc": L.describe(), "clocks": clocks,
            "sites": p.N ** 3, "finite": L.check_finite()}
+    # per-output analysis on the same lattice (wall time of the synchronising calls)
+    L.find_strings()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        L.find_strings()
+    t_str = (time.perf_counter() - t0) / 3
+    L.axion_spectrum(128)
+    t0 = time.perf_counter()
+    L.axion_spectrum(128)
+    t_spec = time.perf_counter() - t0
+    rec["analysis_ms"] = {"find_strings": 1e3 * t_str, "axion_spectrum_128": 1e3 * t_spec}
     if with_e2e:
         rec["e2e"] = e2e_leg(axs, L, dist, steps)
     L.close()
@@ -350,6 +361,7 @@ def gpu_arm(args, dist):
         "cpu_baseline": cpu,
         "e2e": e2e_line,
         "gpu_launches": main["launches"],
+        "analysis_ms": main.get("analysis_ms"),
         "clocks": main["clocks"],
         "fp64": fp64,
         "ensemble": ens,

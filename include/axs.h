@@ -245,6 +245,15 @@ int axs_ensemble_evolve_timed(axs_ensemble *e, int nsteps, double *ms);
  * dt = 0 steps (the state is unchanged) and keep the fastest. Runs once
  * automatically before the first step unless AXS_AUTOTUNE=0. */
 int axs_autotune(axs_lattice *h);
+/* Fault injection for tests of the failure path (no reference counterpart):
+ * the next step's TMA loads expect 16 bytes more than they deliver, so the
+ * step kernel's bounded mbarrier waits (about a second each) run out; the
+ * kernel records the timeout, drains its own copies and returns, and the next
+ * synchronising call (axs_evolve_timed, axs_download, ...) returns
+ * AXS_ERR_TIMEOUT. The CUDA context stays usable; the lattice's state after
+ * that step is undefined. Requires the TMA step kernel (AXS_ERR_STATE
+ * otherwise). */
+int axs_inject_wait_timeout(axs_lattice *h);
 /* Describe the step kernel configuration in use (for logs and benches). */
 int axs_describe(axs_lattice *h, char *buf, size_t len);
 /* Number of kernels this library launched since load (graph replays count

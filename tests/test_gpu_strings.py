@@ -52,11 +52,13 @@ def test_golden_theta_snapshots(axs):
 
 
 @pytest.mark.parametrize("precision", [32, 64])
-def test_from_field_agrees_with_host_atan2(axs, oracle, precision):
-    """theta computed on the device from psi: compared with the oracle on
-    numpy's atan2 of the same (rounded) field. atan2 implementations may
-    differ by an ulp, so the mismatch count is reported and must stay tiny."""
-    p = params(axs, 3, 48, precision)
+@pytest.mark.parametrize("N", [48, 40, 72])
+def test_from_field_agrees_with_host_atan2(axs, oracle, precision, N):
+    """theta computed on the device from psi (tiled finder; N = 40, 72 leave
+    partial tiles): compared with the oracle on numpy's atan2 of the same
+    (rounded) field. atan2 implementations may differ by an ulp, so the
+    mismatch count is reported and must stay tiny."""
+    p = params(axs, 3, N, precision)
     with axs.Lattice(p) as L:
         L.init_flat(3, 1.0)
         L.evolve(30)
