@@ -123,12 +123,15 @@ __global__ void __launch_bounds__(256) k_cores(const typename Cplx<T>::type *__r
 // site of halo in +x and +y) are computed once per site into a two-plane
 // shared ring (k_cores evaluates them once per corner, six times per site).
 // Same float n, same margin test, same double replay: same decisions.
-static constexpr int kCX = 32, kCY = 8, kCZ = 32;
+static constexpr int kCX = 64, kCY = 8, kCZ = 32;   // cells per block tile; 256 threads x 2 cells
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_cores3_tiled(const typename Cplx<T>::type *__restrict__ psi,
                                                       uint8_t *__restrict__ mask, int N, double accept,
                                                       unsigned long long *count) {
+    typedef typename Cplx<T>::type C;
+    constexpr int NS = (kCX + 1) * (kCY + 1);   // sites of a plane tile with its +x/+y halo
+    constexpr int PER = (NS + 255) / 256;
     __shared__ float nsm[2][kCY + 1][kCX + 1];
     Corner<T, false> cn{psi, nullptr};
     const float acc_f = (float)accept;
@@ -136,28 +139,46 @@ __global__ void __launch_bounds__(256) k_cores3_tiled(const typename Cplx<T>::ty
     const int x0 = blockIdx.x * kCX, y0 = blockIdx.y * kCY, z0 = blockIdx.z * kCZ;
     const int z1 = min(N, z0 + kCZ);
     const int tid = threadIdx.x;
-    const int cx = tid % kCX, cy = tid / kCX;
+    const int cx = tid % 32, cy = tid / 32;
     unsigned long long local = 0;
-    auto fill = [&](int buf, int z) {   // n of plane z (wrapped) for the tile + halo
-        const int64_t zb = (int64_t)(z == N ? 0 : z) * NN;
-        for (int s = tid; s < (kCX + 1) * (kCY + 1); s += 256) {
-            int sx = s % (kCX + 1), sy = s / (kCX + 1);
+    C pre[PER];   // psi of the next plane's tile, loaded one plane ahead
+    auto load = [&](int z) {
+        const int64_t zb = (int64_t)(z >= N ? z - N : z) * NN;
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int s = tid + k * 256;
+            const int sx = s % (kCX + 1), sy = s / (kCX + 1);
             int gx = x0 + sx, gy = y0 + sy;
-            if (gx > N || gy > N) continue;
+            if (s >= NS || gx > N || gy > N) continue;
             gx = gx >= N ? gx - N : gx;
             gy = gy >= N ? gy - N : gy;
-            nsm[buf][sy][sx] = cn.nf(zb + (int64_t)gy * N + gx);
+            pre[k] = psi[zb + (int64_t)gy * N + gx];
         }
     };
-    fill(0, z0);
+    auto store = [&](int buf) {
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int s = tid + k * 256;
+            const int sx = s % (kCX + 1), sy = s / (kCX + 1);
+            if (s >= NS || x0 + sx > N || y0 + sy > N) continue;
+            nsm[buf][sy][sx] = fmaf(atan2f((float)pre[k].x, (float)pre[k].y), 0.15915494309189535f, 0.5f);
+        }
+    };
+    load(z0);
+    store(0);
+    load(z0 + 1);
     for (int z = z0; z < z1; ++z) {
         const int cur = (z - z0) & 1;
-        fill(cur ^ 1, z + 1);
+        store(cur ^ 1);                 // plane z+1
+        if (z + 2 <= z1) load(z + 2);   // in flight while plane z is evaluated
         __syncthreads();
-        const int x = x0 + cx, y = y0 + cy;
-        if (x < N && y < N) {
-            const float f000 = nsm[cur][cy][cx], f100 = nsm[cur ^ 1][cy][cx], f110 = nsm[cur ^ 1][cy + 1][cx],
-                        f010 = nsm[cur][cy + 1][cx], f011 = nsm[cur][cy + 1][cx + 1], f001 = nsm[cur][cy][cx + 1];
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const int lx = cx + 32 * c;
+            const int x = x0 + lx, y = y0 + cy;
+            if (x >= N || y >= N) continue;
+            const float f000 = nsm[cur][cy][lx], f100 = nsm[cur ^ 1][cy][lx], f110 = nsm[cur ^ 1][cy + 1][lx],
+                        f010 = nsm[cur][cy + 1][lx], f011 = nsm[cur][cy + 1][lx + 1], f001 = nsm[cur][cy][lx + 1];
             const float e_000_100 = circf(f000, f100);
             const float e_011_001 = circf(f011, f001);
             const float sa = e_000_100 + circf(f100, f110) + circf(f110, f010);
@@ -181,7 +202,7 @@ __global__ void __launch_bounds__(256) k_cores3_tiled(const typename Cplx<T>::ty
             mask[m] = (uint8_t)flag;
             local += flag;
         }
-        __syncthreads();   // the plane just used as z+1 becomes z; the other buffer is refilled next
+        __syncthreads();   // plane z's buffer is refilled with plane z+2 next
     }
     for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
     if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
@@ -398,6 +419,8 @@ void string_positions(Lattice *L, int32_t *pos, int64_t cap, int64_t *n) {
 
 struct RefBins {     // pk_estimation.cpp:92-100: floor(|n|) - 1 for 0 < |n| < N/2
     int half;
+    __device__ __forceinline__ RefBins staged(double *) const { return *this; }
+    static constexpr int kSmemTable = 0;
     __device__ __forceinline__ int bin(int64_t n2) const {
         double kmag = sqrt((double)n2);
         if (kmag == 0.0 || kmag >= half) return -1;
@@ -407,6 +430,12 @@ struct RefBins {     // pk_estimation.cpp:92-100: floor(|n|) - 1 for 0 < |n| < N
 struct LogBins {     // nbins log-spaced in |n| between 1 and sqrt(d) N/2
     const double *edge2;   // edge2[b] = t_b^2, b = 1..nbins-1
     int nbins;
+    // copy of the edge table in shared memory (s: nbins doubles)
+    __device__ __forceinline__ LogBins staged(double *s) const {
+        for (int i = threadIdx.x; i < nbins; i += blockDim.x) s[i] = edge2[i];
+        return LogBins{s, nbins};
+    }
+    static constexpr int kSmemTable = 1;
     __device__ __forceinline__ int bin(int64_t n2) const {
         if (n2 == 0) return -1;
         double v = (double)n2;
@@ -419,15 +448,20 @@ struct LogBins {     // nbins log-spaced in |n| between 1 and sqrt(d) N/2
     }
 };
 
-template <typename T, typename B>
+// ROWS = 2: per-bin counts by global integer atomics (the allocation-free
+// binner's layout); ROWS = 3: counts accumulated like the sums, as a third
+// per-warp row (exact: integer-valued doubles), one partial row each.
+template <typename T, typename B, int ROWS = 2>
 __global__ void __launch_bounds__(128) k_bin(const typename Cplx<T>::type *__restrict__ F, int N, int ndims, B binner,
                                              int nbins, double *__restrict__ partials, unsigned long long *__restrict__ counts) {
-    extern __shared__ double hist[];   // [4 warps][2][nbins]
+    extern __shared__ double hist[];   // [4 warps][ROWS][nbins], then the bin table if the binner has one
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < 4 * 2 * nbins; i += blockDim.x) hist[i] = 0.0;
+    for (int i = threadIdx.x; i < 4 * ROWS * nbins; i += blockDim.x) hist[i] = 0.0;
+    const B bins = binner.staged(hist + 4 * ROWS * nbins);
     __syncthreads();
-    double *hp = hist + (size_t)w * 2 * nbins;
+    double *hp = hist + (size_t)w * ROWS * nbins;
     double *hk = hp + nbins;
+    double *hc = hk + nbins;   // ROWS == 3 only
     const int nh = N / 2 + 1;
     const int64_t rows = ndims == 2 ? (int64_t)N : (int64_t)N * N;
     const int64_t total = rows * nh;
@@ -450,7 +484,7 @@ __global__ void __launch_bounds__(128) k_bin(const typename Cplx<T>::type *__res
                 int64_t fz = iz < N / 2 ? iz : iz - N, fy = iy < N / 2 ? iy : iy - N;
                 n2 = fx * fx + fy * fy + fz * fz;
             }
-            b = binner.bin(n2);
+            b = bins.bin(n2);
             if (b >= 0) {
                 auto f = F[q];
                 wt = (ix == 0 || 2 * ix == N) ? 1.0 : 2.0;
@@ -476,30 +510,201 @@ __global__ void __launch_bounds__(128) k_bin(const typename Cplx<T>::type *__res
             if (lane == 0) {
                 hp[bl] += sv;
                 hk[bl] += sk;
-                atomicAdd(&counts[bl], sc);
+                if (ROWS == 3) hc[bl] += (double)sc;
+                else atomicAdd(&counts[bl], sc);
             }
             active &= ~same;
         }
     }
     __syncthreads();
     for (int bn = threadIdx.x; bn < nbins; bn += blockDim.x) {
-        double sp = 0.0, sk = 0.0;
-        for (int ww = 0; ww < 4; ++ww) { sp += hist[(size_t)ww * 2 * nbins + bn]; sk += hist[(size_t)ww * 2 * nbins + nbins + bn]; }
-        partials[((int64_t)blockIdx.x * 2 + 0) * nbins + bn] = sp;
-        partials[((int64_t)blockIdx.x * 2 + 1) * nbins + bn] = sk;
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            double acc = 0.0;
+            for (int ww = 0; ww < 4; ++ww) acc += hist[(size_t)ww * ROWS * nbins + (size_t)r * nbins + bn];
+            partials[((int64_t)blockIdx.x * ROWS + r) * nbins + bn] = acc;
+        }
     }
 }
 
-__global__ void k_bin_final(const double *__restrict__ partials, int nblocks, int nbins, double *__restrict__ out) {
-    int bn = blockIdx.x * blockDim.x + threadIdx.x;
-    if (bn >= nbins) return;
-    double sp = 0.0, sk = 0.0;
-    for (int b = 0; b < nblocks; ++b) {
-        sp += partials[((int64_t)b * 2 + 0) * nbins + bn];
-        sk += partials[((int64_t)b * 2 + 1) * nbins + bn];
+// One block per bin: strided partial sums over the blocks in a fixed order,
+// then a fixed shuffle tree; out = [pk | |n| | count] rows of nbins.
+__global__ void k_bin_final3(const double *__restrict__ partials, int nblocks, int nbins, double *__restrict__ out) {
+    const int bn = blockIdx.x;
+    double v[3] = {0.0, 0.0, 0.0};
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) v[r] += partials[((int64_t)b * 3 + r) * nbins + bn];
+    __shared__ double red[8][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+        for (int o = 16; o > 0; o >>= 1) v[r] += __shfl_down_sync(0xffffffffu, v[r], o);
+    if ((threadIdx.x & 31) == 0)
+        for (int r = 0; r < 3; ++r) red[threadIdx.x >> 5][r] = v[r];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int r = 0; r < 3; ++r) {
+            double acc = 0.0;
+            for (int w = 0; w < 8; ++w) acc += red[w][r];
+            out[(int64_t)r * nbins + bn] = acc;
+        }
+}
+
+// ---- row-based binner (the allocating spectra)
+//
+// Integer bin rules (n2 = |n|^2 is an integer):
+//   RefBinsI: floor(|n|) - 1 for 0 < n2 < (N/2)^2, floor(|n|) = isqrt(n2) (equal
+//             to floor(sqrt((double)n2)) of pk_estimation.cpp:92-95 for n2 < 2^52)
+//   LogBinsI: b = #{ b' in 1..nbins-1 : n2 >= thr[b'] }, thr = ceil(edge^2),
+//             the same test as n2 >= edge^2 for integer n2.
+struct RefBinsI {
+    int half;
+    __device__ __forceinline__ RefBinsI staged(double *) const { return *this; }
+    static constexpr int kSmemTable = 0;
+    __device__ __forceinline__ int bin(int64_t n2) const {
+        if (n2 == 0 || n2 >= (int64_t)half * half) return -1;
+        int s = (int)sqrtf((float)n2);
+        while ((int64_t)s * s > n2) --s;
+        while ((int64_t)(s + 1) * (s + 1) <= n2) ++s;
+        return s - 1;
     }
-    out[bn] = sp;
-    out[nbins + bn] = sk;
+};
+struct LogBinsI {
+    const int *thr;   // thr[b] for b = 1..nbins-1 (thr[0] = 0)
+    int nbins;
+    __device__ __forceinline__ LogBinsI staged(double *s) const {
+        int *t = reinterpret_cast<int *>(s);
+        for (int i = threadIdx.x; i < nbins; i += blockDim.x) t[i] = thr[i];
+        return LogBinsI{t, nbins};
+    }
+    static constexpr int kSmemTable = 1;   // nbins ints fit in nbins doubles
+    __device__ __forceinline__ int bin(int64_t n2) const {
+        if (n2 == 0) return -1;
+        int lo = 0, hi = nbins - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if ((int64_t)thr[mid] <= n2) lo = mid; else hi = mid - 1;
+        }
+        return lo;
+    }
+};
+
+// Float-float values (hi + lo, about 48 significant bits): the warp-level sums
+// run in FP32, where GB300 issues ~60x more operations per cycle than in FP64.
+// Sums use Knuth's error-free two-sum (TAOCP vol. 2, 4.2.2) in a fixed order.
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    err = __fadd_rn(err, __fadd_rn(a.lo, b.lo));
+    const float hi = __fadd_rn(s, err);
+    return FF{hi, __fsub_rn(err, __fsub_rn(hi, s))};
+}
+__device__ __forceinline__ FF ff_shfl_xor(FF a, int o) {
+    return FF{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+}
+__device__ __forceinline__ double ff_to_double(FF a) { return (double)a.hi + (double)a.lo; }
+
+template <typename T> __device__ __forceinline__ FF mode_power(const typename Cplx<T>::type &f);
+template <> __device__ __forceinline__ FF mode_power<float>(const float2 &f) { return FF{fmaf(f.x, f.x, f.y * f.y), 0.0f}; }
+template <> __device__ __forceinline__ FF mode_power<double>(const double2 &f) {
+    const double v = f.x * f.x + f.y * f.y;
+    const float hi = __double2float_rn(v);
+    return FF{hi, __double2float_rn(v - (double)hi)};
+}
+
+// Same deterministic per-warp histograms and block partial rows as k_bin
+// (three rows: power, |n|, count); warps walk whole rows of the half spectrum
+// (no per-mode division), |n| comes from a float-float table, lanes of one bin
+// are summed in float-float by a fixed shuffle tree and flushed by one lane in
+// FP64.
+template <typename T, typename B>
+__global__ void __launch_bounds__(128) k_bin_rows(const typename Cplx<T>::type *__restrict__ F, int N, int ndims,
+                                                  B binner, int nbins, const float2 *__restrict__ sqrt_tab,
+                                                  double *__restrict__ partials) {
+    extern __shared__ double hist[];   // [4 warps][3][nbins], then the bin table
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < 4 * 3 * nbins; i += blockDim.x) hist[i] = 0.0;
+    const B bins = binner.staged(hist + 4 * 3 * nbins);
+    __syncthreads();
+    double *hp = hist + (size_t)w * 3 * nbins;
+    double *hk = hp + nbins;
+    double *hc = hk + nbins;
+    const int nh = N / 2 + 1;
+    const int64_t rows = ndims == 2 ? (int64_t)N : (int64_t)N * N;
+    const int64_t nwarps = (int64_t)gridDim.x * 4;
+    for (int64_t r = (int64_t)blockIdx.x * 4 + w; r < rows; r += nwarps) {
+        int64_t c2;
+        if (ndims == 2) {
+            const int64_t fy = r < N / 2 ? r : r - N;
+            c2 = fy * fy;
+        } else {
+            const int64_t iz = r / N, iy = r - iz * N;
+            const int64_t fz = iz < N / 2 ? iz : iz - N, fy = iy < N / 2 ? iy : iy - N;
+            c2 = fy * fy + fz * fz;
+        }
+        const typename Cplx<T>::type *row = F + r * nh;
+        for (int ix0 = 0; ix0 < nh; ix0 += 32) {
+            const int ix = ix0 + lane;
+            int b = -1, wt = 0;
+            FF v{0.f, 0.f}, kk{0.f, 0.f};
+            if (ix < nh) {
+                const int64_t n2 = (int64_t)ix * ix + c2;
+                b = bins.bin(n2);
+                if (b >= 0) {
+                    wt = (ix == 0 || 2 * ix == N) ? 1 : 2;
+                    const float fw = (float)wt;   // x1 or x2: exact in float-float
+                    const FF p = mode_power<T>(row[ix]);
+                    const float2 sq = sqrt_tab[n2];
+                    v = FF{fw * p.hi, fw * p.lo};
+                    kk = FF{fw * sq.x, fw * sq.y};
+                }
+            }
+            unsigned active = __ballot_sync(0xffffffffu, b >= 0);
+            while (active) {
+                const int leader = __ffs(active) - 1;
+                const int bl = __shfl_sync(0xffffffffu, b, leader);
+                const unsigned same = __ballot_sync(0xffffffffu, b == bl) & active;
+                const bool mine = (same >> lane) & 1u;
+                FF sv = mine ? v : FF{0.f, 0.f}, sk = mine ? kk : FF{0.f, 0.f};
+                int sc = mine ? wt : 0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    sv = ff_add(sv, ff_shfl_xor(sv, o));
+                    sk = ff_add(sk, ff_shfl_xor(sk, o));
+                    sc += __shfl_xor_sync(0xffffffffu, sc, o);
+                }
+                if (lane == 0) {
+                    hp[bl] += ff_to_double(sv);
+                    hk[bl] += ff_to_double(sk);
+                    hc[bl] += (double)sc;
+                }
+                active &= ~same;
+            }
+        }
+    }
+    __syncthreads();
+    for (int bn = threadIdx.x; bn < nbins; bn += blockDim.x) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            double acc = 0.0;
+            for (int ww = 0; ww < 4; ++ww) acc += hist[(size_t)ww * 3 * nbins + (size_t)q * nbins + bn];
+            partials[((int64_t)blockIdx.x * 3 + q) * nbins + bn] = acc;
+        }
+    }
+}
+
+// sqrt(i) as a float-float pair (IEEE double sqrt, split)
+__global__ void k_sqrt_table(float2 *tab, int64_t n) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double r = sqrt((double)i);
+        const float hi = __double2float_rn(r);
+        tab[i] = make_float2(hi, __double2float_rn(r - (double)hi));
+    }
 }
 
 // gather a real field into fft_in: src = complex array, component comp
@@ -547,33 +752,45 @@ static void bin_spectrum(Lattice *L, const B &binner, int nbins, std::vector<dou
                          std::vector<unsigned long long> &cnt) {
     int N = L->p.N;
     int64_t half = (L->p.NDIMS == 2 ? (int64_t)N : (int64_t)N * N) * (N / 2 + 1);
-    int nblk = grid_cap(half, 128, 2);
-    double *part = (double *)dalloc((size_t)nblk * 2 * nbins * sizeof(double) + (size_t)2 * nbins * sizeof(double) +
-                                    (size_t)nbins * sizeof(unsigned long long));
-    double *out = part + (size_t)nblk * 2 * nbins;
-    unsigned long long *dc = (unsigned long long *)(out + 2 * nbins);
+    size_t sm = (size_t)(4 * 3 + B::kSmemTable) * nbins * sizeof(double);
+    // as many 4-warp blocks as fit on the SMs (up to 16 per SM): the per-warp
+    // histograms leave this kernel latency-bound at low occupancy
+    int per_sm = (int)std::max<size_t>(1, std::min<size_t>(16, (size_t)(200 * 1024) / std::max<size_t>(sm, 1)));
+    const int64_t rows = L->p.NDIMS == 2 ? (int64_t)N : (int64_t)N * N;
+    int nblk = (int)std::min<int64_t>((int64_t)num_sms() * per_sm, (rows + 3) / 4);   // whole rows per warp
+    (void)half;
+    double *part = (double *)dalloc((size_t)nblk * 3 * nbins * sizeof(double) + (size_t)3 * nbins * sizeof(double));
+    double *out = part + (size_t)nblk * 3 * nbins;
     try {
-        AXS_CUDA(cudaMemsetAsync(dc, 0, (size_t)nbins * sizeof(unsigned long long), L->stream));
-        size_t sm = (size_t)4 * 2 * nbins * sizeof(double);
+        const int64_t nsq = (int64_t)L->p.NDIMS * (N / 2) * (N / 2) + 1;   // n2 <= NDIMS (N/2)^2
+        if (!L->dsqrt || L->sqrt_len < nsq) {
+            dfree(L->dsqrt);
+            L->dsqrt = nullptr;
+            L->dsqrt = (double *)dalloc((size_t)nsq * sizeof(double));
+            L->sqrt_len = nsq;
+            k_sqrt_table<<<grid_cap(nsq, 256, 4), 256, 0, L->stream>>>((float2 *)L->dsqrt, nsq);
+            AXS_CUDA(cudaGetLastError());
+            count_launches(1);
+        }
         if (sm > 48 * 1024) {
-            if (L->esz == 4) AXS_CUDA(cudaFuncSetAttribute(k_bin<float, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            else AXS_CUDA(cudaFuncSetAttribute(k_bin<double, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            if (L->esz == 4) AXS_CUDA(cudaFuncSetAttribute(k_bin_rows<float, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            else AXS_CUDA(cudaFuncSetAttribute(k_bin_rows<double, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         }
         if (L->esz == 4)
-            k_bin<float, B><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part, dc);
+            k_bin_rows<float, B><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, (const float2 *)L->dsqrt, part);
         else
-            k_bin<double, B><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part, dc);
+            k_bin_rows<double, B><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, (const float2 *)L->dsqrt, part);
         AXS_CUDA(cudaGetLastError());
-        k_bin_final<<<(nbins + 127) / 128, 128, 0, L->stream>>>(part, nblk, nbins, out);
+        k_bin_final3<<<nbins, 256, 0, L->stream>>>(part, nblk, nbins, out);
         AXS_CUDA(cudaGetLastError());
         count_launches(2);
-        std::vector<double> h(2 * nbins);
-        cnt.assign(nbins, 0);
-        AXS_CUDA(cudaMemcpyAsync(h.data(), out, 2 * nbins * sizeof(double), cudaMemcpyDeviceToHost, L->stream));
-        AXS_CUDA(cudaMemcpyAsync(cnt.data(), dc, nbins * sizeof(unsigned long long), cudaMemcpyDeviceToHost, L->stream));
+        std::vector<double> h(3 * (size_t)nbins);
+        AXS_CUDA(cudaMemcpyAsync(h.data(), out, h.size() * sizeof(double), cudaMemcpyDeviceToHost, L->stream));
         AXS_CUDA(cudaStreamSynchronize(L->stream));
         psum.assign(h.begin(), h.begin() + nbins);
-        nsum.assign(h.begin() + nbins, h.end());
+        nsum.assign(h.begin() + nbins, h.begin() + 2 * nbins);
+        cnt.resize(nbins);
+        for (int b = 0; b < nbins; ++b) cnt[b] = (unsigned long long)h[2 * (size_t)nbins + b];
     } catch (...) {
         dfree(part);
         throw;
@@ -597,7 +814,7 @@ void powerspec(Lattice *L, int field, double *pk, double *ks, int *count) {
     int nb = N / 2;
     std::vector<double> ps, ns;
     std::vector<unsigned long long> c;
-    bin_spectrum(L, RefBins{N / 2}, nb, ps, ns, c);
+    bin_spectrum(L, RefBinsI{N / 2}, nb, ps, ns, c);
     float Lf = N * L->p.space_step;                     // pk_estimation.cpp:41
     for (int b = 0; b < nb; ++b) {                      // pk_estimation.cpp:117-121 / 195-199
         double k = ns[b] / (double)(int)c[b];
@@ -627,14 +844,16 @@ void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *c
     exec_r2c(L);
     int d = L->p.NDIMS, N = L->p.N;
     double ratio = sqrt((double)d) * (double)N / 2.0;
-    std::vector<double> e2(nbins, 0.0);
-    for (int b = 1; b < nbins; ++b) { double t = exp(log(ratio) * (double)b / (double)nbins); e2[b] = t * t; }
-    double *de2 = (double *)dalloc(nbins * sizeof(double));
+    // bin b starts at |n| = t_b = ratio^(b/nbins); for integer n2 the test
+    // n2 >= t_b^2 is n2 >= ceil(t_b^2)
+    std::vector<int> thr(nbins, 0);
+    for (int b = 1; b < nbins; ++b) { double t = exp(log(ratio) * (double)b / (double)nbins); thr[b] = (int)ceil(t * t); }
+    int *de2 = (int *)dalloc(nbins * sizeof(int));
     std::vector<double> ps, ns;
     std::vector<unsigned long long> c;
     try {
-        AXS_CUDA(cudaMemcpyAsync(de2, e2.data(), nbins * sizeof(double), cudaMemcpyHostToDevice, L->stream));
-        bin_spectrum(L, LogBins{de2, nbins}, nbins, ps, ns, c);
+        AXS_CUDA(cudaMemcpyAsync(de2, thr.data(), nbins * sizeof(int), cudaMemcpyHostToDevice, L->stream));
+        bin_spectrum(L, LogBinsI{de2, nbins}, nbins, ps, ns, c);
     } catch (...) {
         dfree(de2);
         throw;
@@ -820,6 +1039,8 @@ void analysis_release(Lattice *L) {
     if (L->have_plan) cufftDestroy(L->plan_r2c);
     L->have_plan = false;
     dfree(L->dpartials); L->dpartials = nullptr;
+    dfree(L->dsqrt); L->dsqrt = nullptr;
+    L->sqrt_len = 0;
 }
 
 }  // namespace axs

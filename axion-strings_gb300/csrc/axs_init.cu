@@ -45,8 +45,10 @@ __global__ void k_fill_kspace(double2 *__restrict__ buf, int N, int ndims, int64
             amp = (k != 0.0 && k < kcut) ? 1.0 : 0.0;
         }
         double2 v;
-        v.x = amp * normal_draw(seed, 2 * pair, m);
-        v.y = amp * normal_draw(seed, 2 * pair + 1, m);
+        double g0 = 0.0, g1 = 0.0;
+        if (amp != 0.0) normal_pair(seed, pair, m, g0, g1);   // zero-amplitude modes need no deviates
+        v.x = amp * g0;
+        v.y = amp * g1;
         buf[m] = v;
     }
 }

@@ -112,6 +112,8 @@ struct Lattice {
     cufftHandle plan_r2c = 0;
     bool have_plan = false;
     double *dpartials = nullptr;     // reduction partials
+    double *dsqrt = nullptr;         // sqrt(n) for n = 0 .. NDIMS (N/2)^2 (spectrum binning)
+    int64_t sqrt_len = 0;
     size_t partials_cap = 0;
     void *dstage = nullptr;          // transfer staging (length reals)
     std::map<GraphKey, cudaGraphExec_t> graphs;
@@ -244,6 +246,31 @@ __device__ __forceinline__ void site_update(T a, T b, T L1, T L2, T &p1, T &p2, 
 
 // Philox-4x32-10 (Salmon et al., SC'11) and Box-Muller; the deviate for
 // array a at offset m. Must agree with the oracle's definition.
+// Both deviates of arrays 2*pair and 2*pair+1 at offset m from one Philox block
+// and one logarithm (the same values as two normal_draw calls).
+__device__ __forceinline__ void normal_pair(uint64_t seed, int pair, int64_t m, double &g0, double &g1) {
+    uint32_t c0 = (uint32_t)((uint64_t)m & 0xffffffffu), c1 = (uint32_t)((uint64_t)m >> 32);
+    uint32_t c2 = (uint32_t)pair, c3 = 0x41585331u;
+    uint32_t k0 = (uint32_t)(seed & 0xffffffffu), k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    uint64_t b1 = (((uint64_t)c0 << 21) ^ (uint64_t)(c1 >> 11)) & ((1ull << 53) - 1);
+    uint64_t b2 = (((uint64_t)c2 << 21) ^ (uint64_t)(c3 >> 11)) & ((1ull << 53) - 1);
+    const double two_m53 = 1.1102230246251565404e-16;
+    double u1 = (double)(b1 + 1) * two_m53;
+    double u2 = (double)b2 * two_m53;
+    double rr = sqrt(-2.0 * log(u1));
+    double ang = 6.283185307179586232 * u2;
+    g0 = rr * cos(ang);
+    g1 = rr * sin(ang);
+}
+
 __device__ __forceinline__ double normal_draw(uint64_t seed, int a, int64_t m) {
     uint32_t c0 = (uint32_t)((uint64_t)m & 0xffffffffu), c1 = (uint32_t)((uint64_t)m >> 32);
     uint32_t c2 = (uint32_t)(a >> 1), c3 = 0x41585331u;
