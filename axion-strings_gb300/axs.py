@@ -101,6 +101,7 @@ _sig("axs_ensemble_evolve_timed", [_vp, ctypes.c_int, _dp])
 _sig("axs_inject_wait_timeout", [_vp])
 _sig("axs_autotune", [_vp])
 _sig("axs_describe", [_vp, ctypes.c_char_p, ctypes.c_size_t])
+_sig("axs_ensemble_describe", [_vp, ctypes.c_char_p, ctypes.c_size_t])
 _sig("axs_kernel_launches", [], ctypes.c_int64)
 _sig("axs_powerspec_noalloc", [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, _vp, _vp, _vp, _vp])
 _sig("axs_set_device", [ctypes.c_int])
@@ -360,6 +361,11 @@ class Ensemble:
         ms = ctypes.c_double()
         _check(_lib.axs_ensemble_evolve_timed(self._h, int(nsteps), ctypes.byref(ms)))
         return ms.value
+
+    def describe(self):
+        b = ctypes.create_string_buffer(256)
+        _check(_lib.axs_ensemble_describe(self._h, b, 256))
+        return b.value.decode()
 
     def close(self):
         if self._h:

@@ -681,7 +681,7 @@ int axs_ensemble_destroy(axs_ensemble *e) {
     API_BEGIN
     if (!e) return AXS_OK;
     cudaStreamSynchronize(e->E.stream);
-    for (auto &g : e->E.graphs) cudaGraphExecDestroy(g.second);
+    clear_graphs(e->E.graphs);
     dfree(e->E.dzlat);
     dfree(e->E.dcounter);
     dfree(e->E.derr);
@@ -738,8 +738,7 @@ int axs_inject_wait_timeout(axs_lattice *h) {
     if (L->cfg.kind != 1) fail(AXS_ERR_STATE, "the step kernel in use (%s) has no device-side waits", L->cfg.describe().c_str());
     L->debug_tx_excess = 16;
     L->zlat_variant = -1;
-    for (auto &g : L->graphs) cudaGraphExecDestroy(g.second);
-    L->graphs.clear();
+    clear_graphs(L->graphs);
     API_END
 }
 
@@ -747,6 +746,13 @@ int axs_autotune(axs_lattice *h) {
     API_BEGIN
     CHECK_HANDLE(h);
     lattice_autotune(&h->L);
+    API_END
+}
+
+int axs_ensemble_describe(axs_ensemble *e, char *buf, size_t len) {
+    API_BEGIN
+    if (!e) fail(AXS_ERR_ARG, "null ensemble");
+    if (buf && len) snprintf(buf, len, "%s", ensemble_describe(&e->E).c_str());
     API_END
 }
 

@@ -58,9 +58,17 @@ struct ZLat {
     CUtensorMap tm_row[2];   // box {tx, 1, 1} over psi[b]
     CUtensorMap tm_main[2];  // box {tx, TY, 1}
     CUtensorMap tm_xh[2];    // box {16-byte halo, TY, 1}
-    CUtensorMap tm_pih;      // box {tx, TY, 1} over pih
+    CUtensorMap tm_pih[2];   // box {tx, TY, 1} over pih[b]
+    // two-step (halo depth 2) kernel only
+    CUtensorMap t2_row2[2];  // box {tx, 2, 1} over psi[b]
+    CUtensorMap t2_str2[2];  // box {16-byte halo, 2, 1} over psi[b]
+    CUtensorMap t2_prow[2];  // box {tx, 1, 1} over pih[b]
+    CUtensorMap t2_pstr[2];  // box {16-byte halo, TY, 1} over pih[b]
     void *psi[2];
-    void *pih;
+    // pih[b]: the half-step momentum that goes with psi[b] as current field.
+    // A launch reads pih[bin] and writes pih[bin ^ 1]; both are the same
+    // buffer when the momentum is updated in place.
+    void *pih[2];
     double *clock;           // [2] tau at the parity of psi
     int N, tx, ntx, nty, nzc;
     int a_index;             // which of psi[0]/psi[1] is "current" at launch parity 0
@@ -70,9 +78,22 @@ struct ZLat {
     int debug_tx_excess;     // test-only: bytes the first load of each item expects but never gets
 };
 
+// A captured interval is keyed by its length and the state it starts from
+// (current psi buffer, and where the momentum lives); it ends in a fixed state.
 struct GraphKey {
     int nsteps, parity;
-    bool operator<(const GraphKey &o) const { return nsteps != o.nsteps ? nsteps < o.nsteps : parity < o.parity; }
+    uint64_t state;   // hash of the members' (cur, pih) pairs
+    bool operator<(const GraphKey &o) const {
+        if (nsteps != o.nsteps) return nsteps < o.nsteps;
+        if (parity != o.parity) return parity < o.parity;
+        return state < o.state;
+    }
+};
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches = 0;             // kernels in the graph
+    std::vector<int> cur_after;       // per member
+    std::vector<uint8_t> swapped;     // per member: pih and scratch exchanged an odd number of times
 };
 
 struct Lattice {
@@ -81,7 +102,10 @@ struct Lattice {
     int esz = 8;          // bytes per real component (4 or 8)
     void *psi[2] = {nullptr, nullptr};
     void *pih = nullptr;  // half-step momentum (or pi_0 when fresh)
-    void *scratch = nullptr;  // complex, length sites: synchronised pi
+    // complex, length sites: synchronised pi for the analysis, and the
+    // destination of the momentum in two-step mode (the two pointers are then
+    // exchanged after every launch; the contents of scratch never outlive a call)
+    void *scratch = nullptr;
     double *dclock = nullptr; // [2]
     int *derr = nullptr;      // device error flags
     int *dcounter = nullptr;  // [2] work counters of the persistent step kernel
@@ -96,7 +120,8 @@ struct Lattice {
     bool tuned = false;
     // z-march launch table for this lattice alone
     ZLat *dzlat = nullptr;
-    int zlat_variant = -1, zlat_tx = -1, zlat_zchunk = -1, zlat_a_index = 0;
+    int zlat_variant = -1, zlat_tx = -1, zlat_zchunk = -1;
+    void *zlat_pih[2] = {nullptr, nullptr};   // host copy of the table's pih[]
     int debug_tx_excess = 0;  // set by axs_inject_wait_timeout for one step
     int64_t zitems = 0;
     // analysis buffers (lazily allocated)
@@ -116,7 +141,7 @@ struct Lattice {
     int64_t sqrt_len = 0;
     size_t partials_cap = 0;
     void *dstage = nullptr;          // transfer staging (length reals)
-    std::map<GraphKey, cudaGraphExec_t> graphs;
+    std::map<GraphKey, GraphEntry> graphs;
 };
 
 struct Ensemble {
@@ -128,19 +153,25 @@ struct Ensemble {
     int64_t zitems = 0;
     int *dcounter = nullptr;
     int *derr = nullptr;
-    std::map<GraphKey, cudaGraphExec_t> graphs;
+    // per member (in members order): its cur when the table was built, and the
+    // table's pih[] for it
+    std::vector<int> tab_cur;
+    std::vector<void *> tab_pih;   // 2 per member
+    std::map<GraphKey, GraphEntry> graphs;
 };
 
 // ---- step module (axs_step.cu)
 void step_setup(Lattice *L);
 void step_release(Lattice *L);
 bool zmarch_supported(const axs_params &p);
-void lattice_step_once(Lattice *L);                   // one step (eager or inside capture)
+int lattice_advance(Lattice *L, int max_steps);       // one launch (eager or inside capture); steps taken
+void clear_graphs(std::map<GraphKey, GraphEntry> &g);
 void lattice_evolve(Lattice *L, int nsteps);          // graph-cached
 void lattice_autotune(Lattice *L);
 void ensemble_setup(Ensemble *E);
 void ensemble_evolve(Ensemble *E, int nsteps);
 void ensemble_autotune(Ensemble *E);
+std::string ensemble_describe(const Ensemble *E);
 void launch_sync_pi(Lattice *L);                      // scratch <- pi_n
 void launch_laplacian(Lattice *L, int comp, double *dout);
 void launch_unpack(Lattice *L, const void *src, int which, int comp, void *dst_real, int dst_is_double);

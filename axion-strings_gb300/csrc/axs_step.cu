@@ -295,7 +295,8 @@ __global__ void __launch_bounds__(256) k_zmarch(const ZLat *__restrict__ lats, i
         const int nload = T_steps + 2;
         const int bin = Lt.a_index ^ parity;   // input psi buffer / clock slot
         C *psi_out = reinterpret_cast<C *>(Lt.psi[bin ^ 1]);
-        C *pih = reinterpret_cast<C *>(Lt.pih);
+        const C *pih = reinterpret_cast<const C *>(Lt.pih[bin]);
+        C *pih_out = reinterpret_cast<C *>(Lt.pih[bin ^ 1]);
         const double tau = Lt.clock[bin];
         const StepCoefs<T> cf = make_coefs<T>(tau, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs);
         if (local == 0 && tid == 0) Lt.clock[bin ^ 1] = tau + Lt.dt;   // tau += dt, s_integrate.cpp:317
@@ -399,7 +400,7 @@ __global__ void __launch_bounds__(256) k_zmarch(const ZLat *__restrict__ lats, i
                     site_update<T>(ctr[j].x, ctr[j].y, L1, L2, pv[2 * j], pv[2 * j + 1], outv[j].x, outv[j].y, cf);
                 }
                 const int64_t off = ((int64_t)z * N + (y0 + yy)) * N + (x0 + xx);
-                *reinterpret_cast<V *>(&pih[off]) = *reinterpret_cast<V *>(pv);
+                *reinterpret_cast<V *>(&pih_out[off]) = *reinterpret_cast<V *>(pv);
                 *reinterpret_cast<V *>(&psi_out[off]) = *reinterpret_cast<V *>(outv);
             }
 #pragma unroll
@@ -553,7 +554,7 @@ __global__ void __launch_bounds__(Z2Cfg<T, TY, TXMAX, S>::NT)
                         tma_load_3d(smem_u32(slot + K::C_BYTES), &Lt.tm_xh[bin], xl * K::EU, y0, z, bar);
                         tma_load_3d(smem_u32(slot + K::C_BYTES + K::H_PAD), &Lt.tm_xh[bin], xr * K::EU, y0, z, bar);
                     }
-                    if (with_pih) tma_load_3d(smem_u32(slot + K::P_OFF), &Lt.tm_pih, x0 * K::EU, y0, z, bar);
+                    if (with_pih) tma_load_3d(smem_u32(slot + K::P_OFF), &Lt.tm_pih[bin], x0 * K::EU, y0, z, bar);
                 }
             }
             if (!ok) {
@@ -591,7 +592,7 @@ __global__ void __launch_bounds__(Z2Cfg<T, TY, TXMAX, S>::NT)
             const int T_steps = zb - za;
             const int bin = Lt.a_index ^ parity;
             C *psi_out = reinterpret_cast<C *>(Lt.psi[bin ^ 1]);
-            C *pih = reinterpret_cast<C *>(Lt.pih);
+            C *pih = reinterpret_cast<C *>(Lt.pih[bin ^ 1]);   // output; the input arrives by TMA
             const double tau = Lt.clock[bin];
             const StepCoefs<T> cf = make_coefs<T>(tau, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs);
             if (local == 0 && cid == 0) Lt.clock[bin ^ 1] = tau + Lt.dt;   // tau += dt, s_integrate.cpp:317
@@ -678,6 +679,437 @@ __global__ void __launch_bounds__(Z2Cfg<T, TY, TXMAX, S>::NT)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Two steps per pass (temporal blocking with halo depth 2), complex float.
+//
+// One pass reads psi_n and pih_{n-1} and writes psi_{n+2} and pih_{n+1}: 32
+// bytes per site for two site-updates instead of 64. A work item is an x-y
+// tile of tx * TY sites marched through a z-chunk, as in k_zmarch2:
+//  * the producer warp loads, per plane, psi_n over the tile plus a two-site
+//    periodic halo (rows y0-2 .. y0+TY+1 as three row bands, two-site x strips
+//    on both sides) and pih_{n-1} over the tile plus a one-site halo (rows
+//    y0-1 .. y0+TY, and the x strips): up to 14 TMA boxes, none of which wraps;
+//  * stage 1 (consumer warps) takes step n on plane m over the tile and its
+//    one-site ring without the corners (the sites that the 7-point stencil of
+//    stage 2 reads) and puts psi_{n+1} of the plane into a two-plane ring;
+//  * stage 2 takes step n+1 on plane m-1 over the tile, from psi_{n+1} of
+//    planes m-2, m-1, m and pih_n of plane m-1 (registers) and the in-plane
+//    neighbours (shared memory), and stores psi_{n+2} and pih_{n+1}.
+// Each consumer thread owns fixed 2-site vectors of the tile (and of the
+// ring), so the z-neighbours of both stages stay in registers. Both stages call
+// site_update / lap7 with the coefficients of a one-step launch at tau and
+// tau + dt, so one pass of two steps and two passes of one step give the same
+// bits. pih is read from pih[bin] and written to pih[bin ^ 1], which must be
+// different buffers: a neighbouring tile may already have stored pih_{n+1}
+// where this tile still reads pih_{n-1} in its halo.
+
+template <int TY, int TXMAX, int S, int NCW>
+struct Z3Cfg {
+    static constexpr int CS = 8;                                  // bytes per complex float site
+    static constexpr int NC = NCW * 32;                           // consumer threads
+    static constexpr int NT = NC + 32;
+    static constexpr int NVX = TXMAX / 2;                         // 2-site vectors per row
+    static constexpr int MAXV = (TY * NVX + NC - 1) / NC;         // tile vectors per thread
+    static constexpr int MAXR = (2 * NVX + NC - 1) / NC;          // ring-row vectors per thread
+    static constexpr int ST_M = (TY * 16 + 127) / 128 * 128;
+    static constexpr int STRIP = 128 + ST_M + 128;                // psi x strip: rows 0-1 | 2..TY+1 | TY+2..TY+3
+    static constexpr int PB = (TY + 4) * TXMAX * CS;              // psi_n band, rows y0-2 .. y0+TY+1
+    static constexpr int SL_OFF = PB, SR_OFF = PB + STRIP;
+    static constexpr int QB_OFF = PB + 2 * STRIP;                 // pih band, rows y0-1 .. y0+TY
+    static constexpr int QL_OFF = QB_OFF + (TY + 2) * TXMAX * CS; // pih x strips, rows y0 .. y0+TY-1
+    static constexpr int QR_OFF = QL_OFF + ST_M;
+    static constexpr int SLOT = QR_OFF + ST_M;
+    static constexpr int MB = (TY + 2) * TXMAX * CS;              // psi_{n+1} band, rows y0-1 .. y0+TY
+    static constexpr int MID = (MB + 2 * TY * CS + 127) / 128 * 128;   // + columns x0-1 and x0+tx
+    static constexpr int MID_OFF = S * SLOT;
+    static constexpr int BAR_OFF = MID_OFF + 2 * MID;
+    static constexpr int SMEM = BAR_OFF + 256;
+};
+
+// Byte offset of row r (0 .. TY+3 for y0-2 .. y0+TY+1) within a psi x strip
+// (two sites per row; rows 0-1, 2..TY+1 and TY+2..TY+3 are separate boxes).
+template <int TY, int ST_M>
+__device__ __forceinline__ int strip_off(int r) {
+    return r < 2 ? r * 16 : (r < TY + 2 ? 128 + (r - 2) * 16 : 128 + ST_M + (r - TY - 2) * 16);
+}
+
+__device__ __forceinline__ float4 ldb4(const unsigned char *base, int off) {
+    return *reinterpret_cast<const float4 *>(base + off);
+}
+__device__ __forceinline__ float2 ldb2(const unsigned char *base, int off) {
+    return *reinterpret_cast<const float2 *>(base + off);
+}
+__device__ __forceinline__ void st4(float2 *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+
+// One step of the two sites (c.xy, c.zw); same operations as k_zmarch2.
+__device__ __forceinline__ float4 update_vec2(float4 c, float4 zm, float4 zp, float4 up, float4 dn, float2 left,
+                                              float2 right, float4 &p, const StepCoefs<float> &cf) {
+    float4 o;
+    float L1 = lap7<float>(c.x, left.x, c.z, up.x, dn.x, zm.x, zp.x);
+    float L2 = lap7<float>(c.y, left.y, c.w, up.y, dn.y, zm.y, zp.y);
+    site_update<float>(c.x, c.y, L1, L2, p.x, p.y, o.x, o.y, cf);
+    L1 = lap7<float>(c.z, c.x, right.x, up.z, dn.z, zm.z, zp.z);
+    L2 = lap7<float>(c.w, c.y, right.y, up.w, dn.w, zm.w, zp.w);
+    site_update<float>(c.z, c.w, L1, L2, p.z, p.w, o.z, o.w, cf);
+    return o;
+}
+__device__ __forceinline__ float2 update_site(float2 c, float2 xm, float2 xp, float2 ym, float2 yp, float2 zm,
+                                              float2 zp, float2 &p, const StepCoefs<float> &cf) {
+    float2 o;
+    const float L1 = lap7<float>(c.x, xm.x, xp.x, ym.x, yp.x, zm.x, zp.x);
+    const float L2 = lap7<float>(c.y, xm.y, xp.y, ym.y, yp.y, zm.y, zp.y);
+    site_update<float>(c.x, c.y, L1, L2, p.x, p.y, o.x, o.y, cf);
+    return o;
+}
+
+template <int TY, int TXMAX, int S, int NCW>
+__global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
+    k_zmarch_2step(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity, int *derr) {
+    typedef Z3Cfg<TY, TXMAX, S, NCW> K;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + K::BAR_OFF);
+    uint64_t *empty = full + S;
+    uint64_t *ifull = empty + S;                                 // [2]
+    uint64_t *iempty = ifull + 2;                                // [2]
+    uint64_t *midbar = iempty + 2;                               // consumer barrier of the psi_{n+1} ring
+    volatile int64_t *items = reinterpret_cast<volatile int64_t *>(midbar + 1);   // [2]
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(items + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), NCW);
+        }
+        for (int k = 0; k < 2; ++k) {
+            mbar_init(smem_u32(&ifull[k]), 1);
+            mbar_init(smem_u32(&iempty[k]), NCW);
+        }
+        mbar_init(smem_u32(midbar), NCW);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp == NCW) {
+        // ------------------------------------------------------------ producer
+        if (lane == 0) {
+            int64_t q = 0;
+            bool ok = true;
+            for (int64_t k = 0; ok; ++k) {
+                if (k >= 2) ok = mbar_wait_bounded(smem_u32(&iempty[k & 1]), (uint32_t)(((k >> 1) - 1) & 1));
+                if (!ok || *abort_flag) break;
+                const int64_t item = (int64_t)atomicAdd(&counters[0], 1);
+                items[k & 1] = item;
+                mbar_arrive(smem_u32(&ifull[k & 1]));
+                if (item >= total_items) break;
+                int li = 0;
+                while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+                const ZLat &Lt = lats[li];
+                const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
+                const int64_t local = item - Lt.item_base;
+                const int ncols = ntx * nty;
+                const int zq = (int)(local / ncols), col = (int)(local % ncols);
+                const int x0 = (col % ntx) * tx, y0 = (col / ntx) * TY;
+                const int za = (int)((int64_t)zq * N / nzc), zb = (int)((int64_t)(zq + 1) * N / nzc);
+                const int nload = zb - za + 4;
+                const int bin = Lt.a_index ^ parity;
+                const bool xhalo = tx < N;
+                const uint32_t psi_bytes = (uint32_t)((TY + 4) * tx * K::CS + (xhalo ? 2 * (TY + 4) * 16 : 0));
+                const uint32_t pih_bytes = (uint32_t)((TY + 2) * tx * K::CS + (xhalo ? 2 * TY * 16 : 0));
+                const int ym2 = y0 >= 2 ? y0 - 2 : y0 - 2 + N;
+                const int ym1 = y0 >= 1 ? y0 - 1 : N - 1;
+                const int yp = (y0 + TY == N) ? 0 : y0 + TY;
+                const int xl = x0 >= 2 ? x0 - 2 : x0 - 2 + N;
+                const int xr = (x0 + tx == N) ? 0 : x0 + tx;
+                for (int i = 0; i < nload; ++i, ++q) {
+                    const int s = (int)(q % S);
+                    if (q >= S) {
+                        ok = mbar_wait_bounded(smem_u32(&empty[s]), (uint32_t)(((q / S) - 1) & 1));
+                        if (!ok || *abort_flag) break;
+                    }
+                    int z = za - 2 + i;
+                    z = z < 0 ? z + N : (z >= N ? z - N : z);
+                    unsigned char *slot = smem + s * K::SLOT;
+                    const uint32_t bar = smem_u32(&full[s]);
+                    const bool with_pih = i >= 1 && i <= nload - 2;
+                    mbar_expect_tx(bar, psi_bytes + (with_pih ? pih_bytes : 0u) +
+                                            (i == 0 ? (uint32_t)Lt.debug_tx_excess : 0u));
+                    tma_load_3d(smem_u32(slot), &Lt.t2_row2[bin], x0, ym2, z, bar);
+                    tma_load_3d(smem_u32(slot + 2 * tx * K::CS), &Lt.tm_main[bin], x0, y0, z, bar);
+                    tma_load_3d(smem_u32(slot + (TY + 2) * tx * K::CS), &Lt.t2_row2[bin], x0, yp, z, bar);
+                    if (xhalo) {
+                        tma_load_3d(smem_u32(slot + K::SL_OFF), &Lt.t2_str2[bin], xl, ym2, z, bar);
+                        tma_load_3d(smem_u32(slot + K::SL_OFF + 128), &Lt.tm_xh[bin], xl, y0, z, bar);
+                        tma_load_3d(smem_u32(slot + K::SL_OFF + 128 + K::ST_M), &Lt.t2_str2[bin], xl, yp, z, bar);
+                        tma_load_3d(smem_u32(slot + K::SR_OFF), &Lt.t2_str2[bin], xr, ym2, z, bar);
+                        tma_load_3d(smem_u32(slot + K::SR_OFF + 128), &Lt.tm_xh[bin], xr, y0, z, bar);
+                        tma_load_3d(smem_u32(slot + K::SR_OFF + 128 + K::ST_M), &Lt.t2_str2[bin], xr, yp, z, bar);
+                    }
+                    if (with_pih) {
+                        tma_load_3d(smem_u32(slot + K::QB_OFF), &Lt.t2_prow[bin], x0, ym1, z, bar);
+                        tma_load_3d(smem_u32(slot + K::QB_OFF + tx * K::CS), &Lt.tm_pih[bin], x0, y0, z, bar);
+                        tma_load_3d(smem_u32(slot + K::QB_OFF + (TY + 1) * tx * K::CS), &Lt.t2_prow[bin], x0, yp, z,
+                                    bar);
+                        if (xhalo) {
+                            tma_load_3d(smem_u32(slot + K::QL_OFF), &Lt.t2_pstr[bin], xl, y0, z, bar);
+                            tma_load_3d(smem_u32(slot + K::QR_OFF), &Lt.t2_pstr[bin], xr, y0, z, bar);
+                        }
+                    }
+                }
+            }
+            if (!ok) {
+                atomicOr(derr, DEVERR_TIMEOUT);
+                *abort_flag = 1;
+            }
+            // Drain: wait (bounded) for this CTA's last loads still in flight.
+            for (int64_t d = q > S ? q - S : 0; d < q; ++d)
+                mbar_wait_bounded(smem_u32(&full[d % S]), (uint32_t)((d / S) & 1));
+        }
+    } else {
+        // ------------------------------------------------------------ consumers
+        // Every shared-memory and global offset a thread touches depends only
+        // on the item's tile, so it is computed once per item; the plane loop
+        // holds loads, arithmetic and stores.
+        const int cid = tid;   // 0 .. NC-1
+        int64_t q0 = 0;        // loads of the items before the current one
+        int64_t g = 0;         // iterations done (completed phases of midbar)
+        for (int64_t k = 0;; ++k) {
+            int w = warp_wait(smem_u32(&ifull[k & 1]), (uint32_t)((k >> 1) & 1), abort_flag);
+            if (w) {
+                if (w == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
+                break;
+            }
+            const int64_t item = items[k & 1];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&iempty[k & 1]));
+            if (item >= total_items) break;
+            int li = 0;
+            while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+            const ZLat &Lt = lats[li];
+            const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
+            const int64_t local = item - Lt.item_base;
+            const int ncols = ntx * nty;
+            const int zq = (int)(local / ncols), col = (int)(local % ncols);
+            const int x0 = (col % ntx) * tx, y0 = (col / ntx) * TY;
+            const int za = (int)((int64_t)zq * N / nzc), zb = (int)((int64_t)(zq + 1) * N / nzc);
+            const int T_steps = zb - za;
+            const int bin = Lt.a_index ^ parity;
+            float2 *psi_out = reinterpret_cast<float2 *>(Lt.psi[bin ^ 1]);
+            float2 *pih_out = reinterpret_cast<float2 *>(Lt.pih[bin ^ 1]);
+            const double tau = Lt.clock[bin];
+            const double tau1 = tau + Lt.dt;
+            const StepCoefs<float> cf1 = make_coefs<float>(tau, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs);
+            const StepCoefs<float> cf2 = make_coefs<float>(tau1, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs);
+            if (local == 0 && cid == 0) Lt.clock[bin ^ 1] = tau1 + Lt.dt;   // tau += dt twice, s_integrate.cpp:317
+            const bool xhalo = tx < N;
+            const int nvx = tx / 2;
+            const int nvec = nvx * TY, nring = 2 * nvx;
+            const int txb = tx * K::CS;   // bytes per band row
+            const int64_t NN = (int64_t)N * N;
+
+            // Tile vectors: byte offsets of the centre, left and right neighbours
+            // in an input slot (psi_n band rows y0-2 .. : centre row 2+yy; the
+            // pih band starts one row later) and in a psi_{n+1} plane (row 1+yy),
+            // and the global site offset at plane za.
+            int t_c[K::MAXV], t_l[K::MAXV], t_r[K::MAXV], m_l[K::MAXV], m_r[K::MAXV];
+            int64_t g_off[K::MAXV];
+#pragma unroll
+            for (int j = 0; j < K::MAXV; ++j) {
+                const int v = cid + j * K::NC;
+                const int yy = v < nvec ? v / nvx : 0, xx = v < nvec ? (v % nvx) * 2 : 0;
+                const int rowb = (2 + yy) * txb, mrow = (1 + yy) * txb;
+                t_c[j] = rowb + xx * K::CS;
+                t_l[j] = xx > 0 ? t_c[j] - K::CS
+                                : (xhalo ? K::SL_OFF + strip_off<TY, K::ST_M>(2 + yy) + K::CS : rowb + (tx - 1) * K::CS);
+                t_r[j] = xx + 2 < tx ? t_c[j] + 2 * K::CS : (xhalo ? K::SR_OFF + strip_off<TY, K::ST_M>(2 + yy) : rowb);
+                m_l[j] = xx > 0 ? mrow + (xx - 1) * K::CS : (xhalo ? K::MB + yy * K::CS : mrow + (tx - 1) * K::CS);
+                m_r[j] = xx + 2 < tx ? mrow + (xx + 2) * K::CS : (xhalo ? K::MB + (TY + yy) * K::CS : mrow);
+                g_off[j] = (int64_t)za * NN + (int64_t)(y0 + yy) * N + (x0 + xx);
+            }
+            // Ring-row vectors (rows y0-1 and y0+TY: band rows 1 and TY+2).
+            int r_c[K::MAXR], r_l[K::MAXR], r_r[K::MAXR];
+#pragma unroll
+            for (int j = 0; j < K::MAXR; ++j) {
+                const int u = cid + j * K::NC;
+                const int br = (u < nring && u >= nvx) ? TY + 2 : 1;
+                const int xx = u < nring ? (u % nvx) * 2 : 0;
+                const int rowb = br * txb;
+                r_c[j] = rowb + xx * K::CS;
+                r_l[j] = xx > 0 ? r_c[j] - K::CS
+                                : (xhalo ? K::SL_OFF + strip_off<TY, K::ST_M>(br) + K::CS : rowb + (tx - 1) * K::CS);
+                r_r[j] = xx + 2 < tx ? r_c[j] + 2 * K::CS : (xhalo ? K::SR_OFF + strip_off<TY, K::ST_M>(br) : rowb);
+            }
+            // Ring-column site: x0-1 (column 1 of the left strips) or x0+tx
+            // (column 0 of the right strips), row y0+cyy; it goes to the
+            // threads after the ring-row vectors.
+            const int ccol = xhalo ? (cid + K::NC - nring % K::NC) % K::NC : K::NC;
+            const bool has_col = ccol < 2 * TY;
+            int c_z = 0, c_xm = 0, c_xp = 0, c_ym = 0, c_yp = 0, c_q = 0, c_m = 0;
+            if (has_col) {
+                const int cside = ccol / TY, cyy = ccol % TY, r = 2 + cyy;
+                const int so = cside ? K::SR_OFF : K::SL_OFF;
+                const int own = cside ? 0 : K::CS;   // the site's byte within a two-site strip row
+                c_z = so + strip_off<TY, K::ST_M>(r) + own;
+                c_ym = so + strip_off<TY, K::ST_M>(r - 1) + own;
+                c_yp = so + strip_off<TY, K::ST_M>(r + 1) + own;
+                c_xm = cside ? r * txb + (tx - 1) * K::CS : so + strip_off<TY, K::ST_M>(r);
+                c_xp = cside ? so + strip_off<TY, K::ST_M>(r) + K::CS : r * txb;
+                c_q = (cside ? K::QR_OFF : K::QL_OFF) + cyy * 16 + own;
+                c_m = K::MB + (cside * TY + cyy) * K::CS;
+            }
+
+            float4 a_zm[K::MAXV], a_c[K::MAXV];    // psi_n of planes m-1, m
+            float4 b_m2[K::MAXV], b_m1[K::MAXV];   // psi_{n+1} of planes m-2, m-1
+            float4 p_m1[K::MAXV];                  // pih_n of plane m-1
+            float4 r_zm[K::MAXR], r_cv[K::MAXR];   // ring rows: psi_n of planes m-1, m
+            float2 c_zm = make_float2(0.f, 0.f), c_cv = c_zm;   // ring column site
+            const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < K::MAXV; ++j) { a_zm[j] = a_c[j] = b_m2[j] = b_m1[j] = p_m1[j] = zero4; }
+#pragma unroll
+            for (int j = 0; j < K::MAXR; ++j) { r_zm[j] = r_cv[j] = zero4; }
+
+            // load q sits in slot q % S and completes phase (q / S) & 1 of full[slot]
+            int s0 = (int)(q0 % S);
+            uint32_t ph0 = (uint32_t)((q0 / S) & 1);
+            int s1 = s0 + 1;
+            uint32_t ph1 = ph0;
+            if (s1 == S) { s1 = 0; ph1 ^= 1u; }
+            // planes za-2 and za-1 (loads 0 and 1) prime the registers
+            w = warp_wait(smem_u32(&full[s0]), ph0, abort_flag);
+            if (!w) w = warp_wait(smem_u32(&full[s1]), ph1, abort_flag);
+            if (w) {
+                if (w == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
+                break;
+            }
+            {
+                const unsigned char *B0 = smem + s0 * K::SLOT, *B1 = smem + s1 * K::SLOT;
+#pragma unroll
+                for (int j = 0; j < K::MAXV; ++j)
+                    if (cid + j * K::NC < nvec) {
+                        a_zm[j] = ldb4(B0, t_c[j]);
+                        a_c[j] = ldb4(B1, t_c[j]);
+                    }
+#pragma unroll
+                for (int j = 0; j < K::MAXR; ++j)
+                    if (cid + j * K::NC < nring) {
+                        r_zm[j] = ldb4(B0, r_c[j]);
+                        r_cv[j] = ldb4(B1, r_c[j]);
+                    }
+                if (has_col) {
+                    c_zm = ldb2(B0, c_z);
+                    c_cv = ldb2(B1, c_z);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&empty[s0]));
+
+            // stage 1 of iteration i: in-plane from load i+1 (slot sc), zp from load i+2 (slot sn)
+            int sc = s1, sn = s1 + 1;
+            uint32_t phn = ph1;
+            if (sn == S) { sn = 0; phn ^= 1u; }
+            bool ok = true;
+            for (int i = 0; i <= T_steps + 1; ++i) {
+                w = warp_wait(smem_u32(&full[sn]), phn, abort_flag);
+                if (w) {
+                    if (w == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
+                    ok = false;
+                    break;
+                }
+                const unsigned char *Sc = smem + sc * K::SLOT, *Sn = smem + sn * K::SLOT;
+                unsigned char *Mw = smem + K::MID_OFF + (int)(g & 1) * K::MID;
+                float4 b_new[K::MAXV], p_new[K::MAXV];
+#pragma unroll
+                for (int j = 0; j < K::MAXV; ++j) {
+                    b_new[j] = p_new[j] = zero4;
+                    if (cid + j * K::NC >= nvec) continue;
+                    const float4 zp = ldb4(Sn, t_c[j]);
+                    const float4 up = ldb4(Sc, t_c[j] - txb), dn = ldb4(Sc, t_c[j] + txb);
+                    float4 p = ldb4(Sc, K::QB_OFF + t_c[j] - txb);
+                    const float4 o = update_vec2(a_c[j], a_zm[j], zp, up, dn, ldb2(Sc, t_l[j]), ldb2(Sc, t_r[j]), p, cf1);
+                    *reinterpret_cast<float4 *>(Mw + t_c[j] - txb) = o;
+                    b_new[j] = o;
+                    p_new[j] = p;
+                    a_zm[j] = a_c[j];
+                    a_c[j] = zp;
+                }
+#pragma unroll
+                for (int j = 0; j < K::MAXR; ++j) {
+                    if (cid + j * K::NC >= nring) continue;
+                    const float4 zp = ldb4(Sn, r_c[j]);
+                    const float4 up = ldb4(Sc, r_c[j] - txb), dn = ldb4(Sc, r_c[j] + txb);
+                    float4 p = ldb4(Sc, K::QB_OFF + r_c[j] - txb);
+                    const float4 o = update_vec2(r_cv[j], r_zm[j], zp, up, dn, ldb2(Sc, r_l[j]), ldb2(Sc, r_r[j]), p, cf1);
+                    *reinterpret_cast<float4 *>(Mw + r_c[j] - txb) = o;
+                    r_zm[j] = r_cv[j];
+                    r_cv[j] = zp;
+                }
+                if (has_col) {
+                    const float2 zp = ldb2(Sn, c_z);
+                    float2 p = ldb2(Sc, c_q);
+                    *reinterpret_cast<float2 *>(Mw + c_m) = update_site(c_cv, ldb2(Sc, c_xm), ldb2(Sc, c_xp), ldb2(Sc, c_ym),
+                                                                        ldb2(Sc, c_yp), c_zm, zp, p, cf1);
+                    c_zm = c_cv;
+                    c_cv = zp;
+                }
+                // this warp is done with load i+1; at the last plane also with load i+2
+                __syncwarp();
+                if (lane == 0) {
+                    mbar_arrive(smem_u32(&empty[sc]));
+                    if (i == T_steps + 1) mbar_arrive(smem_u32(&empty[sn]));
+                }
+                // stage 2 on plane m-1 = za-2+i (the planes za .. zb-1)
+                if (i >= 2) {
+                    const unsigned char *Mr = smem + K::MID_OFF + (int)((g - 1) & 1) * K::MID;
+#pragma unroll
+                    for (int j = 0; j < K::MAXV; ++j) {
+                        if (cid + j * K::NC >= nvec) continue;
+                        const int mc = t_c[j] - txb;
+                        const float4 up = ldb4(Mr, mc - txb), dn = ldb4(Mr, mc + txb);
+                        float4 p = p_m1[j];
+                        const float4 o = update_vec2(b_m1[j], b_m2[j], b_new[j], up, dn, ldb2(Mr, m_l[j]), ldb2(Mr, m_r[j]), p, cf2);
+                        st4(&pih_out[g_off[j]], p);
+                        st4(&psi_out[g_off[j]], o);
+                        g_off[j] += NN;
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < K::MAXV; ++j) {
+                    b_m2[j] = b_m1[j];
+                    b_m1[j] = b_new[j];
+                    p_m1[j] = p_new[j];
+                }
+                // plane m of the psi_{n+1} ring is complete before anyone reads it;
+                // plane m-1 is no longer read when the next stage 1 overwrites it
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(midbar));
+                w = warp_wait(smem_u32(midbar), (uint32_t)(g & 1), abort_flag);
+                ++g;
+                if (w) {
+                    if (w == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
+                    ok = false;
+                    break;
+                }
+                sc = sn;
+                if (++sn == S) { sn = 0; phn ^= 1u; }
+            }
+            if (!ok) break;
+            q0 += T_steps + 4;
+        }
+    }
+    __syncwarp();      // reconverge every warp (the producer's lane 0 ran alone) before the barrier
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&counters[1], 1) == (int)gridDim.x - 1) {
+            counters[0] = 0;
+            counters[1] = 0;
+            __threadfence();
+        }
+    }
+}
+
 // ============================================================== host side
 
 static int g_num_sms = 0;
@@ -696,22 +1128,32 @@ static int grid_for(int64_t len, int threads = 256) {
     return (int)std::max<int64_t>(1, std::min(want, cap));
 }
 
+// ---- z-march variants -------------------------------------------------------
+// gen 1: k_zmarch (CTA barriers); gen 2: k_zmarch2 (producer warp); gen 3:
+// k_zmarch_2step (two steps per pass, complex float), whose odd last step of an
+// interval runs on the gen-2 `partner` with the same tile and launch table.
+struct ZVariant {
+    int gen, ty, txmax, slots, ncw, partner;
+};
+static const ZVariant kZVariants[] = {
+    {1, 8, 128, 4, 0, -1}, {1, 8, 128, 5, 0, -1}, {1, 16, 128, 4, 0, -1}, {1, 4, 256, 4, 0, -1},
+    {1, 8, 256, 4, 0, -1}, {2, 8, 128, 4, 8, -1}, {2, 8, 128, 5, 8, -1}, {2, 4, 256, 5, 8, -1},
+    {2, 8, 256, 5, 8, -1}, {2, 4, 128, 6, 8, -1}, {3, 8, 128, 4, 8, 6},  {3, 8, 128, 5, 8, 6},
+    {3, 4, 256, 4, 8, 7},  {3, 4, 128, 5, 8, 9},  {3, 8, 128, 4, 16, 6},
+};
+static const int kNumZVariants = sizeof(kZVariants) / sizeof(kZVariants[0]);
+
+static bool two_step(int variant) { return variant >= 0 && variant < kNumZVariants && kZVariants[variant].gen == 3; }
+
 std::string StepConfig::describe() const {
-    char b[160];
+    char b[200];
     if (kind == 0) snprintf(b, sizeof b, "generic per-site kernel");
+    else if (two_step(variant))
+        snprintf(b, sizeof b, "TMA z-march variant %d (two steps per pass, halo depth 2; odd step on variant %d), tx=%d, zchunk=%d",
+                 variant, kZVariants[variant].partner, tx, zchunk);
     else snprintf(b, sizeof b, "TMA z-march variant %d, tx=%d, zchunk=%d", variant, tx, zchunk);
     return b;
 }
-
-// ---- z-march variants -------------------------------------------------------
-struct ZVariant {
-    int gen, ty, txmax, slots;   // gen 1: k_zmarch (CTA barriers), gen 2: k_zmarch2 (producer warp)
-};
-static const ZVariant kZVariants[] = {
-    {1, 8, 128, 4}, {1, 8, 128, 5}, {1, 16, 128, 4}, {1, 4, 256, 4}, {1, 8, 256, 4},
-    {2, 8, 128, 4}, {2, 8, 128, 5}, {2, 4, 256, 5}, {2, 8, 256, 5}, {2, 4, 128, 6},
-};
-static const int kNumZVariants = sizeof(kZVariants) / sizeof(kZVariants[0]);
 
 // Sets the kernel's shared-memory attribute and caches its occupancy. Called
 // when a launch table is built, never inside a graph capture.
@@ -767,6 +1209,33 @@ static void launch_zmarch2_t(const ZLat *d, int nlat, int64_t items, int *counte
     count_launches(1);
 }
 
+template <int TY, int TXMAX, int S, int NCW>
+static int prepare_zmarch3_t() {
+    typedef Z3Cfg<TY, TXMAX, S, NCW> K;
+    static int occ = -1;
+    if (occ < 0) {
+        AXS_CUDA(cudaFuncSetAttribute(k_zmarch_2step<TY, TXMAX, S, NCW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      K::SMEM));
+        int o = 0;
+        AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_zmarch_2step<TY, TXMAX, S, NCW>, K::NT, K::SMEM));
+        if (o < 1) fail(AXS_ERR_CUDA, "two-step z-march kernel does not fit on an SM");
+        occ = o;
+    }
+    return occ;
+}
+
+template <int TY, int TXMAX, int S, int NCW>
+static void launch_zmarch3_t(const ZLat *d, int nlat, int64_t items, int *counters, int parity, int *derr,
+                             cudaStream_t st, int ctas_per_sm) {
+    typedef Z3Cfg<TY, TXMAX, S, NCW> K;
+    int occ = prepare_zmarch3_t<TY, TXMAX, S, NCW>();
+    int per = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ) : occ;
+    int64_t grid = std::min<int64_t>((int64_t)per * num_sms(), items);
+    k_zmarch_2step<TY, TXMAX, S, NCW><<<(int)grid, K::NT, K::SMEM, st>>>(d, nlat, items, counters, parity, derr);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+
 static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t items, int *counters, int parity,
                           int *derr, cudaStream_t st, int ctas_per_sm) {
 #define AXS_ZV(I, TY, TX, S)                                                                                    \
@@ -779,6 +1248,11 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
         if (esz == 4) launch_zmarch2_t<float, TY, TX, S>(d, nlat, items, counters, parity, derr, st, ctas_per_sm); \
         else launch_zmarch2_t<double, TY, TX, S>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);         \
         break;
+#define AXS_ZV3(I, TY, TX, S, W)                                                                          \
+    case I:                                                                                               \
+        if (esz != 4) fail(AXS_ERR_ARG, "two-step z-march variant %d needs complex float fields", variant); \
+        launch_zmarch3_t<TY, TX, S, W>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);          \
+        break;
     switch (variant) {
         AXS_ZV(0, 8, 128, 4)
         AXS_ZV(1, 8, 128, 5)
@@ -790,10 +1264,16 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
         AXS_ZV2(7, 4, 256, 5)
         AXS_ZV2(8, 8, 256, 5)
         AXS_ZV2(9, 4, 128, 6)
+        AXS_ZV3(10, 8, 128, 4, 8)
+        AXS_ZV3(11, 8, 128, 5, 8)
+        AXS_ZV3(12, 4, 256, 4, 8)
+        AXS_ZV3(13, 4, 128, 5, 8)
+        AXS_ZV3(14, 8, 128, 4, 16)
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
 #undef AXS_ZV
 #undef AXS_ZV2
+#undef AXS_ZV3
 }
 
 static void prepare_zmarch(int esz, int variant) {
@@ -807,6 +1287,10 @@ static void prepare_zmarch(int esz, int variant) {
         if (esz == 4) prepare_zmarch2_t<float, TY, TX, S>();      \
         else prepare_zmarch2_t<double, TY, TX, S>();              \
         break;
+#define AXS_ZP3(I, TY, TX, S, W)                                  \
+    case I:                                                       \
+        if (esz == 4) prepare_zmarch3_t<TY, TX, S, W>();          \
+        break;
     switch (variant) {
         AXS_ZP(0, 8, 128, 4)
         AXS_ZP(1, 8, 128, 5)
@@ -818,15 +1302,28 @@ static void prepare_zmarch(int esz, int variant) {
         AXS_ZP2(7, 4, 256, 5)
         AXS_ZP2(8, 8, 256, 5)
         AXS_ZP2(9, 4, 128, 6)
+        AXS_ZP3(10, 8, 128, 4, 8)
+        AXS_ZP3(11, 8, 128, 5, 8)
+        AXS_ZP3(12, 4, 256, 4, 8)
+        AXS_ZP3(13, 4, 128, 5, 8)
+        AXS_ZP3(14, 8, 128, 4, 16)
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
+    if (kZVariants[variant].gen == 3) prepare_zmarch(esz, kZVariants[variant].partner);
 #undef AXS_ZP
 #undef AXS_ZP2
+#undef AXS_ZP3
 }
 
 // Dynamic shared memory of a variant (mirrors ZCfg / Z2Cfg).
 static int variant_smem(const ZVariant &v, int esz) {
     int cs = 2 * esz;
+    if (v.gen == 3) {
+        int st_m = (v.ty * 16 + 127) / 128 * 128;
+        int slot = (v.ty + 4) * v.txmax * cs + 2 * (256 + st_m) + (v.ty + 2) * v.txmax * cs + 2 * st_m;
+        int mid = ((v.ty + 2) * v.txmax * cs + 2 * v.ty * cs + 127) / 128 * 128;
+        return v.slots * slot + 2 * mid + 256;
+    }
     int c_bytes = (v.ty + 2) * v.txmax * cs;
     int h_pad = (v.ty * 16 + 127) / 128 * 128;
     if (v.gen == 1) return v.slots * ((c_bytes + 2 * h_pad + 127) / 128 * 128) + 128;
@@ -845,6 +1342,14 @@ static int max_smem_optin() {
 
 // The tx a variant would use for an N (largest admissible divisor), or 0.
 static int variant_tx(const ZVariant &v, int N, int esz) {
+    if (v.gen == 3) {
+        // complex float only; the partner must tile N the same way
+        if (esz != 4 || variant_smem(v, esz) > max_smem_optin()) return 0;
+        const ZVariant &pv = kZVariants[v.partner];
+        int tx = variant_tx(pv, N, esz);
+        if (!tx || pv.ty != v.ty || tx > v.txmax || N < 4) return 0;
+        return tx;
+    }
     int cs = 2 * esz;
     int vs = 16 / cs;
     int txmax = v.txmax;
@@ -897,29 +1402,45 @@ static void encode_map(CUtensorMap *m, void *base, int N, int esz, int box_x_sit
 }
 
 // Fill the z-march table entry of lattice L for a variant; returns items.
-static int64_t fill_zlat(ZLat &z, Lattice *L, int variant, int zchunk, int64_t item_base) {
+// a_index: the psi buffer that launch parity 0 treats as current. The entry's
+// pih[b] is the momentum buffer that goes with psi[b]: L->pih for the current
+// psi, and for a two-step variant L->scratch for the other one (the momentum
+// is then written out of place and the host exchanges pih and scratch after
+// every launch); one-step variants update the momentum in place.
+static int64_t fill_zlat(ZLat &z, Lattice *L, int variant, int zchunk, int64_t item_base, int a_index) {
     const ZVariant &v = kZVariants[variant];
     int N = L->p.N;
     int tx = variant_tx(v, N, L->esz);
     if (!tx) fail(AXS_ERR_ARG, "z-march variant %d cannot tile N=%d", variant, N);
     prepare_zmarch(L->esz, variant);
+    const bool oop = v.gen == 3;
+    if (oop && (!L->scratch || L->scratch == L->pih)) fail(AXS_ERR_STATE, "two-step variant without a second momentum buffer");
     memset(&z, 0, sizeof z);
     int vs = 16 / (2 * L->esz);
+    void *pb[2];
+    pb[L->cur] = L->pih;
+    pb[L->cur ^ 1] = oop ? L->scratch : L->pih;
     for (int b = 0; b < 2; ++b) {
         encode_map(&z.tm_row[b], L->psi[b], N, L->esz, tx, 1);
         encode_map(&z.tm_main[b], L->psi[b], N, L->esz, tx, v.ty);
         encode_map(&z.tm_xh[b], L->psi[b], N, L->esz, vs, v.ty);
+        encode_map(&z.tm_pih[b], pb[b], N, L->esz, tx, v.ty);
+        if (oop) {
+            encode_map(&z.t2_row2[b], L->psi[b], N, L->esz, tx, 2);
+            encode_map(&z.t2_str2[b], L->psi[b], N, L->esz, vs, 2);
+            encode_map(&z.t2_prow[b], pb[b], N, L->esz, tx, 1);
+            encode_map(&z.t2_pstr[b], pb[b], N, L->esz, vs, v.ty);
+        }
         z.psi[b] = L->psi[b];
+        z.pih[b] = pb[b];
     }
-    encode_map(&z.tm_pih, L->pih, N, L->esz, tx, v.ty);
-    z.pih = L->pih;
     z.clock = L->dclock;
     z.N = N;
     z.tx = tx;
     z.ntx = N / tx;
     z.nty = N / v.ty;
     z.nzc = std::max(1, N / std::max(1, zchunk));
-    z.a_index = L->cur;
+    z.a_index = a_index;
     z.item_base = item_base;
     z.dt = (double)L->p.time_step;
     double dx = (double)L->p.space_step;
@@ -932,17 +1453,29 @@ static int64_t fill_zlat(ZLat &z, Lattice *L, int variant, int zchunk, int64_t i
     return (int64_t)z.ntx * z.nty * z.nzc;
 }
 
+static thread_local bool t_capturing = false;
+static thread_local int64_t t_captured = 0;
+
+// The lattice's own table uses absolute parity: a launch passes L->cur.
 static void ensure_single_table(Lattice *L) {
+    if (t_capturing) fail(AXS_ERR_STATE, "internal: z-march table rebuilt inside a graph capture");
     ZLat z;
-    int64_t items = fill_zlat(z, L, L->cfg.variant, L->cfg.zchunk, 0);
+    int64_t items = fill_zlat(z, L, L->cfg.variant, L->cfg.zchunk, 0, 0);
     if (!L->dzlat) L->dzlat = (ZLat *)dalloc(sizeof(ZLat));
     AXS_CUDA(cudaMemcpyAsync(L->dzlat, &z, sizeof(ZLat), cudaMemcpyHostToDevice, L->stream));
     AXS_CUDA(cudaStreamSynchronize(L->stream));
     L->zlat_variant = L->cfg.variant;
     L->zlat_zchunk = L->cfg.zchunk;
-    L->zlat_a_index = L->cur;
+    L->zlat_pih[0] = z.pih[0];
+    L->zlat_pih[1] = z.pih[1];
     L->zitems = items;
     L->cfg.tx = z.tx;
+}
+
+static bool single_table_valid(const Lattice *L) {
+    if (!L->dzlat || L->zlat_variant != L->cfg.variant || L->zlat_zchunk != L->cfg.zchunk) return false;
+    if (L->zlat_pih[L->cur] != L->pih) return false;
+    return two_step(L->cfg.variant) ? L->zlat_pih[L->cur ^ 1] == L->scratch : L->zlat_pih[L->cur ^ 1] == L->pih;
 }
 
 void step_setup(Lattice *L) {
@@ -958,9 +1491,13 @@ void step_setup(Lattice *L) {
     AXS_CUDA(cudaMemsetAsync(L->dcounter, 0, 2 * sizeof(int), L->stream));
 }
 
+void clear_graphs(std::map<GraphKey, GraphEntry> &g) {
+    for (auto &e : g) cudaGraphExecDestroy(e.second.exec);
+    g.clear();
+}
+
 void step_release(Lattice *L) {
-    for (auto &g : L->graphs) cudaGraphExecDestroy(g.second);
-    L->graphs.clear();
+    clear_graphs(L->graphs);
     dfree(L->dzlat);
     L->dzlat = nullptr;
     dfree(L->dcounter);
@@ -1000,11 +1537,15 @@ static void launch_generic_dispatch(Lattice *L, const double *cin, double *cout)
     }
 }
 
-// One step of a lattice (the handle's bookkeeping advances here; the kernels
-// may be running later inside a graph).
-void lattice_step_once(Lattice *L) {
+// Advances a lattice by one launch of at most max_steps (>= 1) steps and
+// returns the steps taken: two for a two-step variant when allowed, else one.
+// The handle's bookkeeping advances here; the kernels may run later inside a
+// graph.
+int lattice_advance(Lattice *L, int max_steps) {
     const double *cin = L->dclock + L->cur;
     double *cout = L->dclock + (L->cur ^ 1);
+    int k = 1;
+    bool swap = false;
     if (L->fresh) {
         if (L->esz == 4)
             k_drift0<float><<<grid_for(L->length), 256, 0, L->stream>>>((const float2 *)L->psi[L->cur],
@@ -1020,12 +1561,15 @@ void lattice_step_once(Lattice *L) {
         count_launches(1);
         L->fresh = 0;
     } else if (L->cfg.kind == 1) {
-        if (!L->dzlat || L->zlat_variant != L->cfg.variant || L->zlat_zchunk != L->cfg.zchunk) ensure_single_table(L);
-        // the table is built with a_index = cur at build time; parity is relative to it
-        int parity = L->cur ^ L->zlat_a_index;
-        launch_zmarch(L->esz, L->cfg.variant, L->dzlat, 1, L->zitems, L->dcounter, parity, L->derr, L->stream,
-                      L->cfg.ctas_per_sm);
-        if (L->debug_tx_excess) {   // an injected stall lasts one step: rebuild the table before the next
+        if (!single_table_valid(L)) ensure_single_table(L);
+        int kv = L->cfg.variant;
+        if (two_step(kv)) {
+            swap = true;
+            if (max_steps >= 2) k = 2;
+            else kv = kZVariants[kv].partner;
+        }
+        launch_zmarch(L->esz, kv, L->dzlat, 1, L->zitems, L->dcounter, L->cur, L->derr, L->stream, L->cfg.ctas_per_sm);
+        if (L->debug_tx_excess) {   // an injected stall lasts one launch: rebuild the table before the next
             L->debug_tx_excess = 0;
             L->zlat_variant = -1;
         }
@@ -1034,8 +1578,10 @@ void lattice_step_once(Lattice *L) {
         else launch_generic_dispatch<double>(L, cin, cout);
     }
     L->cur ^= 1;
-    L->tau = L->tau + (double)L->p.time_step;
-    L->steps += 1;
+    if (swap) std::swap(L->pih, L->scratch);
+    for (int s = 0; s < k; ++s) L->tau = L->tau + (double)L->p.time_step;
+    L->steps += k;
+    return k;
 }
 
 }  // namespace axs
@@ -1043,10 +1589,10 @@ void lattice_step_once(Lattice *L) {
 namespace axs {
 
 // ---------------------------------------------------------------- graphs
-static thread_local bool t_capturing = false;
 static int64_t g_launches = 0;
 void count_launches(int64_t n) {
-    if (!t_capturing) __atomic_fetch_add(&g_launches, n, __ATOMIC_RELAXED);
+    if (t_capturing) t_captured += n;
+    else __atomic_fetch_add(&g_launches, n, __ATOMIC_RELAXED);
 }
 int64_t total_launches() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
@@ -1057,15 +1603,22 @@ static bool env_flag(const char *name, bool dflt) {
 }
 
 static void prepare_tables(Lattice *L) {
-    if (L->cfg.kind == 1 && (!L->dzlat || L->zlat_variant != L->cfg.variant || L->zlat_zchunk != L->cfg.zchunk))
-        ensure_single_table(L);
+    if (L->cfg.kind == 1 && !single_table_valid(L)) ensure_single_table(L);
 }
 
+static uint64_t mix_state(uint64_t h, const Lattice *m) {
+    h ^= (uint64_t)(uintptr_t)m->pih + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+    h ^= (uint64_t)m->cur + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+    return h;
+}
+
+// Captures fn into a graph; *launches receives the kernels it launched.
 template <typename StepFn>
-static cudaGraphExec_t capture(cudaStream_t st, StepFn fn) {
+static cudaGraphExec_t capture(cudaStream_t st, StepFn fn, int64_t *launches) {
     cudaGraph_t g = nullptr;
     AXS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     t_capturing = true;
+    t_captured = 0;
     try {
         fn();
     } catch (...) {
@@ -1075,6 +1628,7 @@ static cudaGraphExec_t capture(cudaStream_t st, StepFn fn) {
         throw;
     }
     t_capturing = false;
+    *launches = t_captured;
     AXS_CUDA(cudaStreamEndCapture(st, &g));
     cudaGraphExec_t ex = nullptr;
     AXS_CUDA(cudaGraphInstantiate(&ex, g, 0));
@@ -1083,44 +1637,48 @@ static cudaGraphExec_t capture(cudaStream_t st, StepFn fn) {
 }
 
 void lattice_evolve(Lattice *L, int nsteps) {
-    if (nsteps <= 0) return;
     if (!L->tuned) {
         if (env_flag("AXS_AUTOTUNE", true)) lattice_autotune(L);
         L->tuned = true;
     }
+    if (nsteps <= 0) return;
     if (L->fresh) {
-        lattice_step_once(L);
+        lattice_advance(L, 1);
         if (--nsteps == 0) return;
     }
     prepare_tables(L);
     if (nsteps < 2 || !env_flag("AXS_GRAPHS", true)) {
-        for (int s = 0; s < nsteps; ++s) lattice_step_once(L);
+        while (nsteps > 0) nsteps -= lattice_advance(L, nsteps);
         return;
     }
-    GraphKey key{nsteps, L->cur};
+    GraphKey key{nsteps, L->cur, mix_state(0, L)};
     auto it = L->graphs.find(key);
     if (it == L->graphs.end()) {
-        int cur0 = L->cur;
-        double tau0 = L->tau;
-        int64_t steps0 = L->steps;
-        cudaGraphExec_t ex = capture(L->stream, [&] {
-            for (int s = 0; s < nsteps; ++s) lattice_step_once(L);
-        });
+        const int cur0 = L->cur;
+        const double tau0 = L->tau;
+        const int64_t steps0 = L->steps;
+        void *pih0 = L->pih, *scratch0 = L->scratch;
+        GraphEntry e;
+        e.exec = capture(L->stream, [&] {
+            int n = nsteps;
+            while (n > 0) n -= lattice_advance(L, n);
+        }, &e.launches);
+        e.cur_after.push_back(L->cur);
+        e.swapped.push_back(L->pih != pih0);
         L->cur = cur0;
         L->tau = tau0;
         L->steps = steps0;
-        it = L->graphs.insert(std::make_pair(key, ex)).first;
+        L->pih = pih0;
+        L->scratch = scratch0;
+        it = L->graphs.insert(std::make_pair(key, e)).first;
     }
-    AXS_CUDA(cudaGraphLaunch(it->second, L->stream));
-    count_launches(nsteps);
+    const GraphEntry &e = it->second;
+    AXS_CUDA(cudaGraphLaunch(e.exec, L->stream));
+    count_launches(e.launches);
     for (int s = 0; s < nsteps; ++s) L->tau = L->tau + (double)L->p.time_step;
-    L->cur ^= (nsteps & 1);
+    L->cur = e.cur_after[0];
+    if (e.swapped[0]) std::swap(L->pih, L->scratch);
     L->steps += nsteps;
-}
-
-static void clear_graphs(std::map<GraphKey, cudaGraphExec_t> &g) {
-    for (auto &e : g) cudaGraphExecDestroy(e.second);
-    g.clear();
 }
 
 // ---------------------------------------------------------------- autotune
@@ -1153,7 +1711,10 @@ static double time_launches(cudaStream_t st, int reps, const std::function<void(
 }
 
 // Candidate steps run with dt = 0: psi_out = psi + 0*pih and pih + 0*K are
-// bit-identical copies, so the state (and tau) is unchanged.
+// bit-identical copies, so the state (and tau) is unchanged. Candidates are
+// the generic kernel and every z-march variant that tiles N (one-step
+// variants, and two-step variants with halo depth 2) at z-chunks of 32, 64
+// and 128 planes; the time per step decides.
 void lattice_autotune(Lattice *L) {
     L->tuned = true;
     // AXS_FORCE_CONFIG="kind,variant,zchunk" pins a configuration (tests use it
@@ -1179,6 +1740,7 @@ void lattice_autotune(Lattice *L) {
         if (hit->second.kind != L->cfg.kind || hit->second.variant != L->cfg.variant || hit->second.zchunk != L->cfg.zchunk)
             clear_graphs(L->graphs);
         L->cfg = hit->second;
+        L->zlat_variant = -1;
         return;
     }
     if (!zmarch_supported(L->p)) {
@@ -1210,6 +1772,7 @@ void lattice_autotune(Lattice *L) {
     const int zchunks[] = {32, 64, 128};
     for (int v = 0; v < kNumZVariants; ++v) {
         if (!variant_tx(kZVariants[v], L->p.N, L->esz)) continue;
+        const bool two = two_step(v);
         for (int zc : zchunks) {
             if (zc > L->p.N) continue;
             StepConfig c;
@@ -1219,18 +1782,19 @@ void lattice_autotune(Lattice *L) {
             L->cfg = c;
             ensure_single_table(L);   // built with dt = 0
             double ms = time_launches(L->stream, reps, [&] {
-                int parity = L->cur ^ L->zlat_a_index;
-                launch_zmarch(L->esz, v, L->dzlat, 1, L->zitems, L->dcounter, parity, L->derr, L->stream, 0);
+                launch_zmarch(L->esz, v, L->dzlat, 1, L->zitems, L->dcounter, L->cur, L->derr, L->stream, 0);
                 L->cur ^= 1;
+                if (two) std::swap(L->pih, L->scratch);
             });
+            if (two) ms *= 0.5;   // per step
             c.tx = L->cfg.tx;
             log.push_back({c, ms});
             if (ms < best_ms) { best_ms = ms; best = c; }
         }
     }
     L->p.time_step = dt_save;
-    // dt = 0 steps copied psi back and forth; values are identical, but keep the
-    // buffer the caller had as current.
+    // dt = 0 steps copied psi (and, out of place, pih) back and forth; values
+    // are identical, but keep the psi buffer the caller had as current.
     if (L->cur != cur_save) {
         AXS_CUDA(cudaMemcpyAsync(L->psi[cur_save], L->psi[L->cur], (size_t)L->length * 2 * L->esz,
                                  cudaMemcpyDeviceToDevice, L->stream));
@@ -1244,7 +1808,7 @@ void lattice_autotune(Lattice *L) {
     clear_graphs(L->graphs);
     g_tune_cache[key] = best;
     if (env_flag("AXS_TUNE_LOG", false)) {
-        for (auto &e : log) fprintf(stderr, "[axs autotune N=%d] %-60s %.4f ms\n", L->p.N, e.first.describe().c_str(), e.second);
+        for (auto &e : log) fprintf(stderr, "[axs autotune N=%d] %-60s %.4f ms/step\n", L->p.N, e.first.describe().c_str(), e.second);
         fprintf(stderr, "[axs autotune N=%d] chose %s\n", L->p.N, best.describe().c_str());
     }
 }
@@ -1256,22 +1820,31 @@ static bool ensemble_variant_ok(Ensemble *E, int v) {
     return true;
 }
 
+// One table over all members, largest first (their items are taken first).
+// Parity is relative: a member's entry treats its cur at build time as
+// current at launch parity 0.
 static void ensemble_table(Ensemble *E, float dt_override, bool use_override) {
-    std::vector<int> order(E->members.size());
-    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    const size_t nm = E->members.size();
+    std::vector<int> order(nm);
+    for (size_t i = 0; i < nm; ++i) order[i] = (int)i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return E->members[a]->length > E->members[b]->length; });
-    std::vector<ZLat> tab(order.size());
+    std::vector<ZLat> tab(nm);
+    E->tab_cur.assign(nm, 0);
+    E->tab_pih.assign(2 * nm, nullptr);
     int64_t base = 0;
-    for (size_t k = 0; k < order.size(); ++k) {
-        Lattice *m = E->members[order[k]];
+    for (size_t k = 0; k < nm; ++k) {
+        const int i = order[k];
+        Lattice *m = E->members[i];
         float dt = m->p.time_step;
         if (use_override) m->p.time_step = dt_override;
-        base += fill_zlat(tab[k], m, E->cfg.variant, E->cfg.zchunk, base);
+        base += fill_zlat(tab[k], m, E->cfg.variant, E->cfg.zchunk, base, m->cur);
         m->p.time_step = dt;
-        m->zlat_a_index = m->cur;
+        E->tab_cur[i] = m->cur;
+        E->tab_pih[2 * i] = tab[k].pih[0];
+        E->tab_pih[2 * i + 1] = tab[k].pih[1];
     }
-    if (!E->dzlat) E->dzlat = (ZLat *)dalloc(sizeof(ZLat) * std::max<size_t>(1, tab.size()));
-    AXS_CUDA(cudaMemcpyAsync(E->dzlat, tab.data(), sizeof(ZLat) * tab.size(), cudaMemcpyHostToDevice, E->stream));
+    if (!E->dzlat) E->dzlat = (ZLat *)dalloc(sizeof(ZLat) * std::max<size_t>(1, nm));
+    AXS_CUDA(cudaMemcpyAsync(E->dzlat, tab.data(), sizeof(ZLat) * nm, cudaMemcpyHostToDevice, E->stream));
     AXS_CUDA(cudaStreamSynchronize(E->stream));
     E->zitems = base;
 }
@@ -1288,33 +1861,68 @@ void ensemble_setup(Ensemble *E) {
     if (E->cfg.kind == 1) ensemble_table(E, 0.f, false);
 }
 
+static int ensemble_parity(const Ensemble *E) { return E->members[0]->cur ^ E->tab_cur[0]; }
+
 static bool ensemble_table_valid(Ensemble *E) {
-    if (!E->dzlat) return false;
-    // every member must still sit at the same parity relative to its table entry
-    int d = E->members[0]->cur ^ E->members[0]->zlat_a_index;
-    for (Lattice *m : E->members)
-        if ((m->cur ^ m->zlat_a_index) != d) return false;
+    if (!E->dzlat || E->tab_cur.size() != E->members.size()) return false;
+    // every member must sit at the same parity relative to its entry, with the
+    // momentum buffer the entry expects
+    const int d = ensemble_parity(E);
+    const bool two = two_step(E->cfg.variant);
+    for (size_t i = 0; i < E->members.size(); ++i) {
+        const Lattice *m = E->members[i];
+        if ((m->cur ^ E->tab_cur[i]) != d) return false;
+        if (E->tab_pih[2 * i + m->cur] != m->pih) return false;
+        if (E->tab_pih[2 * i + (m->cur ^ 1)] != (two ? m->scratch : m->pih)) return false;
+    }
     return true;
 }
 
-static void ensemble_step_once(Ensemble *E) {
-    if (E->cfg.kind == 1) {
-        int parity = E->members[0]->cur ^ E->members[0]->zlat_a_index;
-        launch_zmarch(E->members[0]->esz, E->cfg.variant, E->dzlat, (int)E->members.size(), E->zitems, E->dcounter,
-                      parity, E->derr, E->stream, E->cfg.ctas_per_sm);
-        for (Lattice *m : E->members) {
-            m->cur ^= 1;
-            m->tau = m->tau + (double)m->p.time_step;
-            m->steps += 1;
-        }
-    } else {
-        for (Lattice *m : E->members) lattice_step_once(m);
+// One launch over every member; returns the steps taken (see lattice_advance).
+static int ensemble_advance(Ensemble *E, int max_steps) {
+    if (E->cfg.kind != 1) {
+        for (Lattice *m : E->members) lattice_advance(m, 1);
+        return 1;
     }
+    if (!ensemble_table_valid(E)) {
+        if (t_capturing) fail(AXS_ERR_STATE, "internal: ensemble table rebuilt inside a graph capture");
+        ensemble_table(E, 0.f, false);
+    }
+    int kv = E->cfg.variant, k = 1;
+    const bool two = two_step(kv);
+    if (two) {
+        if (max_steps >= 2) k = 2;
+        else kv = kZVariants[kv].partner;
+    }
+    launch_zmarch(E->members[0]->esz, kv, E->dzlat, (int)E->members.size(), E->zitems, E->dcounter, ensemble_parity(E),
+                  E->derr, E->stream, E->cfg.ctas_per_sm);
+    for (Lattice *m : E->members) {
+        m->cur ^= 1;
+        if (two) std::swap(m->pih, m->scratch);
+        for (int s = 0; s < k; ++s) m->tau = m->tau + (double)m->p.time_step;
+        m->steps += k;
+    }
+    return k;
 }
 
 void ensemble_autotune(Ensemble *E) {
     E->tuned = true;
     if (E->cfg.kind != 1) return;
+    // AXS_FORCE_CONFIG="1,variant,zchunk" pins the ensemble's z-march
+    // configuration too (when the variant tiles every member)
+    const char *force = getenv("AXS_FORCE_CONFIG");
+    if (force && *force) {
+        int k = 0, v = 0, zc = 64;
+        if (sscanf(force, "%d,%d,%d", &k, &v, &zc) >= 2 && k == 1 && v >= 0 && v < kNumZVariants &&
+            ensemble_variant_ok(E, v)) {
+            E->cfg.kind = 1;
+            E->cfg.variant = v;
+            E->cfg.zchunk = zc > 0 ? zc : 64;
+            ensemble_table(E, 0.f, false);
+            clear_graphs(E->graphs);
+            return;
+        }
+    }
     std::vector<int> cur_save;
     for (Lattice *m : E->members) cur_save.push_back(m->cur);
     int reps = 6;
@@ -1323,6 +1931,7 @@ void ensemble_autotune(Ensemble *E) {
     const int zchunks[] = {32, 64, 128};
     for (int v = 0; v < kNumZVariants; ++v) {
         if (!ensemble_variant_ok(E, v)) continue;
+        const bool two = two_step(v);
         for (int zc : zchunks) {
             StepConfig c;
             c.kind = 1;
@@ -1331,14 +1940,17 @@ void ensemble_autotune(Ensemble *E) {
             E->cfg = c;
             ensemble_table(E, 0.f, true);
             double ms = time_launches(E->stream, reps, [&] {
-                int parity = E->members[0]->cur ^ E->members[0]->zlat_a_index;
-                launch_zmarch(E->members[0]->esz, v, E->dzlat, (int)E->members.size(), E->zitems, E->dcounter, parity,
-                              E->derr, E->stream, 0);
-                for (Lattice *m : E->members) m->cur ^= 1;
+                launch_zmarch(E->members[0]->esz, v, E->dzlat, (int)E->members.size(), E->zitems, E->dcounter,
+                              ensemble_parity(E), E->derr, E->stream, 0);
+                for (Lattice *m : E->members) {
+                    m->cur ^= 1;
+                    if (two) std::swap(m->pih, m->scratch);
+                }
             });
+            if (two) ms *= 0.5;   // per step
             if (ms < best_ms) { best_ms = ms; best = c; }
             if (env_flag("AXS_TUNE_LOG", false))
-                fprintf(stderr, "[axs autotune ensemble] %-60s %.4f ms\n", c.describe().c_str(), ms);
+                fprintf(stderr, "[axs autotune ensemble] %-60s %.4f ms/step\n", c.describe().c_str(), ms);
         }
     }
     for (size_t i = 0; i < E->members.size(); ++i) {
@@ -1357,55 +1969,76 @@ void ensemble_autotune(Ensemble *E) {
     clear_graphs(E->graphs);
 }
 
+std::string ensemble_describe(const Ensemble *E) {
+    StepConfig c = E->cfg;
+    if (c.kind == 1 && !E->members.empty()) c.tx = variant_tx(kZVariants[c.variant], E->members[0]->p.N, E->members[0]->esz);
+    return c.describe();
+}
+
 void ensemble_evolve(Ensemble *E, int nsteps) {
-    if (nsteps <= 0) return;
-    for (Lattice *m : E->members)
-        if (m->fresh != E->members[0]->fresh || m->steps != E->members[0]->steps)
-            fail(AXS_ERR_STATE, "ensemble members are not at the same step");
     if (!E->tuned) {
         if (env_flag("AXS_AUTOTUNE", true)) ensemble_autotune(E);
         E->tuned = true;
     }
+    if (nsteps <= 0) return;
+    for (Lattice *m : E->members)
+        if (m->fresh != E->members[0]->fresh || m->steps != E->members[0]->steps)
+            fail(AXS_ERR_STATE, "ensemble members are not at the same step");
     if (E->members[0]->fresh) {
-        for (Lattice *m : E->members) lattice_step_once(m);   // pure drift per member
+        for (Lattice *m : E->members) lattice_advance(m, 1);   // pure drift per member
         if (--nsteps == 0) return;
     }
-    if (E->cfg.kind == 1 && !ensemble_table_valid(E)) {
-        ensemble_table(E, 0.f, false);
-        clear_graphs(E->graphs);
-    }
+    if (E->cfg.kind == 1 && !ensemble_table_valid(E)) ensemble_table(E, 0.f, false);
     if (E->cfg.kind != 1)
         for (Lattice *m : E->members) prepare_tables(m);
     if (nsteps < 2 || !env_flag("AXS_GRAPHS", true)) {
-        for (int s = 0; s < nsteps; ++s) ensemble_step_once(E);
+        while (nsteps > 0) nsteps -= ensemble_advance(E, nsteps);
         return;
     }
-    GraphKey key{nsteps, E->members[0]->cur ^ E->members[0]->zlat_a_index};
+    uint64_t h = 0;
+    for (Lattice *m : E->members) h = mix_state(h, m);
+    GraphKey key{nsteps, E->cfg.kind == 1 ? ensemble_parity(E) : E->members[0]->cur, h};
     auto it = E->graphs.find(key);
     if (it == E->graphs.end()) {
         std::vector<int> cur0;
         std::vector<double> tau0;
         std::vector<int64_t> st0;
-        for (Lattice *m : E->members) { cur0.push_back(m->cur); tau0.push_back(m->tau); st0.push_back(m->steps); }
-        cudaGraphExec_t ex = capture(E->stream, [&] {
-            for (int s = 0; s < nsteps; ++s) ensemble_step_once(E);
-        });
-        for (size_t i = 0; i < E->members.size(); ++i) {
-            E->members[i]->cur = cur0[i];
-            E->members[i]->tau = tau0[i];
-            E->members[i]->steps = st0[i];
+        std::vector<void *> pih0, scr0;
+        for (Lattice *m : E->members) {
+            cur0.push_back(m->cur);
+            tau0.push_back(m->tau);
+            st0.push_back(m->steps);
+            pih0.push_back(m->pih);
+            scr0.push_back(m->scratch);
         }
-        it = E->graphs.insert(std::make_pair(key, ex)).first;
+        GraphEntry e;
+        e.exec = capture(E->stream, [&] {
+            int n = nsteps;
+            while (n > 0) n -= ensemble_advance(E, n);
+        }, &e.launches);
+        for (size_t i = 0; i < E->members.size(); ++i) {
+            Lattice *m = E->members[i];
+            e.cur_after.push_back(m->cur);
+            e.swapped.push_back(m->pih != pih0[i]);
+            m->cur = cur0[i];
+            m->tau = tau0[i];
+            m->steps = st0[i];
+            m->pih = pih0[i];
+            m->scratch = scr0[i];
+        }
+        it = E->graphs.insert(std::make_pair(key, e)).first;
     }
-    AXS_CUDA(cudaGraphLaunch(it->second, E->stream));
-    count_launches(E->cfg.kind == 1 ? nsteps : (int64_t)nsteps * (int64_t)E->members.size());
-    for (Lattice *m : E->members) {
+    const GraphEntry &e = it->second;
+    AXS_CUDA(cudaGraphLaunch(e.exec, E->stream));
+    count_launches(e.launches);
+    for (size_t i = 0; i < E->members.size(); ++i) {
+        Lattice *m = E->members[i];
         for (int s = 0; s < nsteps; ++s) m->tau = m->tau + (double)m->p.time_step;
-        m->cur ^= (nsteps & 1);
+        m->cur = e.cur_after[i];
+        if (e.swapped[i]) std::swap(m->pih, m->scratch);
         m->steps += nsteps;
     }
 }
-
 // ---------------------------------------------------------------- helpers
 template <typename T, int ND, int R>
 static void sync_pi_t(Lattice *L) {

@@ -256,6 +256,8 @@ int axs_autotune(axs_lattice *h);
 int axs_inject_wait_timeout(axs_lattice *h);
 /* Describe the step kernel configuration in use (for logs and benches). */
 int axs_describe(axs_lattice *h, char *buf, size_t len);
+/* The same for an ensemble's one launch per step (no reference counterpart). */
+int axs_ensemble_describe(axs_ensemble *e, char *buf, size_t len);
 /* Number of kernels this library launched since load (graph replays count
  * every kernel node they run). */
 int64_t axs_kernel_launches(void);

@@ -39,6 +39,32 @@ def test_members_bit_identical_to_alone(axs, precision):
             assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("force", ["1,10,32", "1,13,64", "1,12,128"])
+def test_two_step_members_bit_identical_to_one_step_alone(axs, force, monkeypatch):
+    """An ensemble on a two-step variant (halo depth 2, momentum out of place)
+    matches each member run alone with the one-step kernel, over even and odd
+    intervals."""
+    specs = [(160, 1.0, 31), (64, 0.7, 32), (96, 2.5, 33), (32, 0.5, 34)]
+    plist = [params(axs, 3, N, 32, lambda_=lam, T_initial=0.0, prs=1) for N, lam, _ in specs]
+    monkeypatch.setenv("AXS_FORCE_CONFIG", force)
+    with axs.Ensemble(plist) as E:
+        for m, (_, _, seed) in zip(E.members, specs):
+            m.init_flat(seed, 1.0)
+        for n in (1, 4, 3, 1, 6):
+            E.evolve(n)
+        assert "two steps per pass" in E.describe(), E.describe()
+        res_e = [(m.download(dtype=np.float32), m.time) for m in E.members]
+    monkeypatch.setenv("AXS_FORCE_CONFIG", "0,0,64")
+    for (N, lam, seed), p, (fe, te) in zip(specs, plist, res_e):
+        with axs.Lattice(p) as L:
+            L.init_flat(seed, 1.0)
+            L.evolve(15)
+            f = L.download(dtype=np.float32)
+            assert L.time == te
+        for q in range(4):
+            assert np.array_equal(f[q], fe[q]), (N, q)
+
+
 def test_ensemble_rejects_mixed_precision(axs):
     with pytest.raises(axs.AxsError):
         axs.Ensemble([params(axs, 3, 32, 32), params(axs, 3, 32, 64)])

@@ -76,6 +76,71 @@ def test_kernel_variants_bit_identical(axs, oracle, precision):
             assert np.array_equal(g[q], g0[q]), (d0, d, q)
 
 
+TWO_STEP = ["1,10,32", "1,11,64", "1,12,128", "1,13,16", "1,14,64"]
+
+
+@pytest.mark.parametrize("N", [64, 160])
+def test_two_step_variants_bit_identical(axs, N):
+    """Two steps per pass (halo depth 2) give the bits of two one-step passes:
+    even and odd intervals (the odd step runs on the one-step partner), eager
+    launches and graph replays, one x tile (N=64) and two (N=160, tx=80)."""
+    p = params(axs, 3, N, 32)
+    outs = []
+    for force in ["0,0,64", "1,6,64"] + TWO_STEP:
+        os.environ["AXS_FORCE_CONFIG"] = force
+        try:
+            with axs.Lattice(p) as L:
+                L.init_thermal(21)
+                for n in (1, 3, 1, 6, 2, 5):
+                    L.evolve(n)
+                d = L.describe()
+                outs.append((force, d, L.download(dtype=np.float32), L.time))
+        finally:
+            del os.environ["AXS_FORCE_CONFIG"]
+    f0, d0, g0, t0 = outs[0]
+    assert "generic" in d0
+    for force, d, g, t in outs[1:]:
+        if force in TWO_STEP:
+            assert "two steps per pass" in d, d
+        assert t == t0, (d, t, t0)
+        for q in range(4):
+            assert np.array_equal(g[q], g0[q]), (d0, d, q)
+
+
+def test_two_step_after_analysis_and_checkpoint(axs):
+    """The momentum moves between two buffers in two-step mode; analysis
+    (which uses the spare buffer), checkpoints and uploads in between keep
+    the run identical to the one-step run."""
+    p = params(axs, 3, 160, 32)
+    res = []
+    for force in ["1,6,64", "1,10,64"]:
+        os.environ["AXS_FORCE_CONFIG"] = force
+        try:
+            with axs.Lattice(p) as L:
+                L.init_thermal(8)
+                L.evolve(5)
+                a = L.download(dtype=np.float32)
+                n1, _, _ = L.find_strings()
+                e1 = L.energies()
+                ck = L.checkpoint()
+                L.evolve(4)
+                L.restore(ck)
+                L.evolve(3)
+                pk = L.axion_spectrum(16)
+                L.evolve(2)
+                res.append((a, n1, e1, pk, L.download(dtype=np.float32), L.time))
+        finally:
+            del os.environ["AXS_FORCE_CONFIG"]
+    (a0, n0, e0, pk0, g0, t0), (a1, n1, e1, pk1, g1, t1) = res
+    assert n0 == n1 and t0 == t1
+    assert np.array_equal(np.asarray(e0), np.asarray(e1))
+    for x, y in zip(pk0, pk1):
+        assert np.array_equal(x, y)
+    for q in range(4):
+        assert np.array_equal(a0[q], a1[q])
+        assert np.array_equal(g0[q], g1[q])
+
+
 def test_fp32_error_against_fp64(axs, oracle):
     """FP32 fields after 10 steps from the identical (rounded) start stay
     within 1e-5 relative of the FP64 run."""
