@@ -762,7 +762,7 @@ __device__ __forceinline__ float2 update_site(float2 c, float2 xm, float2 xp, fl
     return o;
 }
 
-template <int TY, int TXMAX, int S, int NCW>
+template <int TY, int TXMAX, int S, int NCW, int UNR>
 __global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
     k_zmarch_2step(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity, int *derr) {
     typedef Z3Cfg<TY, TXMAX, S, NCW> K;
@@ -1010,6 +1010,8 @@ __global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
             uint32_t phn = ph1;
             if (sn == S) { sn = 0; phn ^= 1u; }
             bool ok = true;
+            // unrolling lets the compiler rename the rotating register planes
+#pragma unroll UNR
             for (int i = 0; i <= T_steps + 1; ++i) {
                 w = warp_wait(smem_u32(&full[sn]), phn, abort_flag);
                 if (w) {
@@ -1139,7 +1141,8 @@ static const ZVariant kZVariants[] = {
     {1, 8, 128, 4, 0, -1}, {1, 8, 128, 5, 0, -1}, {1, 16, 128, 4, 0, -1}, {1, 4, 256, 4, 0, -1},
     {1, 8, 256, 4, 0, -1}, {2, 8, 128, 4, 8, -1}, {2, 8, 128, 5, 8, -1}, {2, 4, 256, 5, 8, -1},
     {2, 8, 256, 5, 8, -1}, {2, 4, 128, 6, 8, -1}, {3, 8, 128, 4, 8, 6},  {3, 8, 128, 5, 8, 6},
-    {3, 4, 256, 4, 8, 7},  {3, 4, 128, 5, 8, 9},  {3, 8, 128, 4, 16, 6},
+    {3, 4, 256, 4, 8, 7},  {3, 8, 128, 4, 8, 6},  {3, 8, 128, 4, 8, 6},  {3, 8, 128, 5, 8, 6},
+    {2, 8, 64, 5, 8, -1},  {3, 8, 64, 4, 4, 16},  {3, 8, 64, 5, 4, 16},  {3, 4, 128, 5, 4, 9},
 };
 static const int kNumZVariants = sizeof(kZVariants) / sizeof(kZVariants[0]);
 
@@ -1209,29 +1212,30 @@ static void launch_zmarch2_t(const ZLat *d, int nlat, int64_t items, int *counte
     count_launches(1);
 }
 
-template <int TY, int TXMAX, int S, int NCW>
+template <int TY, int TXMAX, int S, int NCW, int UNR>
 static int prepare_zmarch3_t() {
     typedef Z3Cfg<TY, TXMAX, S, NCW> K;
     static int occ = -1;
     if (occ < 0) {
-        AXS_CUDA(cudaFuncSetAttribute(k_zmarch_2step<TY, TXMAX, S, NCW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      K::SMEM));
+        AXS_CUDA(cudaFuncSetAttribute(k_zmarch_2step<TY, TXMAX, S, NCW, UNR>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
         int o = 0;
-        AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_zmarch_2step<TY, TXMAX, S, NCW>, K::NT, K::SMEM));
+        AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_zmarch_2step<TY, TXMAX, S, NCW, UNR>, K::NT,
+                                                               K::SMEM));
         if (o < 1) fail(AXS_ERR_CUDA, "two-step z-march kernel does not fit on an SM");
         occ = o;
     }
     return occ;
 }
 
-template <int TY, int TXMAX, int S, int NCW>
+template <int TY, int TXMAX, int S, int NCW, int UNR>
 static void launch_zmarch3_t(const ZLat *d, int nlat, int64_t items, int *counters, int parity, int *derr,
                              cudaStream_t st, int ctas_per_sm) {
     typedef Z3Cfg<TY, TXMAX, S, NCW> K;
-    int occ = prepare_zmarch3_t<TY, TXMAX, S, NCW>();
+    int occ = prepare_zmarch3_t<TY, TXMAX, S, NCW, UNR>();
     int per = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ) : occ;
     int64_t grid = std::min<int64_t>((int64_t)per * num_sms(), items);
-    k_zmarch_2step<TY, TXMAX, S, NCW><<<(int)grid, K::NT, K::SMEM, st>>>(d, nlat, items, counters, parity, derr);
+    k_zmarch_2step<TY, TXMAX, S, NCW, UNR><<<(int)grid, K::NT, K::SMEM, st>>>(d, nlat, items, counters, parity, derr);
     AXS_CUDA(cudaGetLastError());
     count_launches(1);
 }
@@ -1248,10 +1252,10 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
         if (esz == 4) launch_zmarch2_t<float, TY, TX, S>(d, nlat, items, counters, parity, derr, st, ctas_per_sm); \
         else launch_zmarch2_t<double, TY, TX, S>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);         \
         break;
-#define AXS_ZV3(I, TY, TX, S, W)                                                                          \
+#define AXS_ZV3(I, TY, TX, S, W, U)                                                                       \
     case I:                                                                                               \
         if (esz != 4) fail(AXS_ERR_ARG, "two-step z-march variant %d needs complex float fields", variant); \
-        launch_zmarch3_t<TY, TX, S, W>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);          \
+        launch_zmarch3_t<TY, TX, S, W, U>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);       \
         break;
     switch (variant) {
         AXS_ZV(0, 8, 128, 4)
@@ -1264,11 +1268,16 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
         AXS_ZV2(7, 4, 256, 5)
         AXS_ZV2(8, 8, 256, 5)
         AXS_ZV2(9, 4, 128, 6)
-        AXS_ZV3(10, 8, 128, 4, 8)
-        AXS_ZV3(11, 8, 128, 5, 8)
-        AXS_ZV3(12, 4, 256, 4, 8)
-        AXS_ZV3(13, 4, 128, 5, 8)
-        AXS_ZV3(14, 8, 128, 4, 16)
+        AXS_ZV3(10, 8, 128, 4, 8, 1)
+        AXS_ZV3(11, 8, 128, 5, 8, 1)
+        AXS_ZV3(12, 4, 256, 4, 8, 1)
+        AXS_ZV3(13, 8, 128, 4, 8, 2)
+        AXS_ZV3(14, 8, 128, 4, 8, 3)
+        AXS_ZV3(15, 8, 128, 5, 8, 6)
+        AXS_ZV2(16, 8, 64, 5)
+        AXS_ZV3(17, 8, 64, 4, 4, 1)
+        AXS_ZV3(18, 8, 64, 5, 4, 1)
+        AXS_ZV3(19, 4, 128, 5, 4, 1)
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
 #undef AXS_ZV
@@ -1287,9 +1296,9 @@ static void prepare_zmarch(int esz, int variant) {
         if (esz == 4) prepare_zmarch2_t<float, TY, TX, S>();      \
         else prepare_zmarch2_t<double, TY, TX, S>();              \
         break;
-#define AXS_ZP3(I, TY, TX, S, W)                                  \
+#define AXS_ZP3(I, TY, TX, S, W, U)                               \
     case I:                                                       \
-        if (esz == 4) prepare_zmarch3_t<TY, TX, S, W>();          \
+        if (esz == 4) prepare_zmarch3_t<TY, TX, S, W, U>();       \
         break;
     switch (variant) {
         AXS_ZP(0, 8, 128, 4)
@@ -1302,11 +1311,16 @@ static void prepare_zmarch(int esz, int variant) {
         AXS_ZP2(7, 4, 256, 5)
         AXS_ZP2(8, 8, 256, 5)
         AXS_ZP2(9, 4, 128, 6)
-        AXS_ZP3(10, 8, 128, 4, 8)
-        AXS_ZP3(11, 8, 128, 5, 8)
-        AXS_ZP3(12, 4, 256, 4, 8)
-        AXS_ZP3(13, 4, 128, 5, 8)
-        AXS_ZP3(14, 8, 128, 4, 16)
+        AXS_ZP3(10, 8, 128, 4, 8, 1)
+        AXS_ZP3(11, 8, 128, 5, 8, 1)
+        AXS_ZP3(12, 4, 256, 4, 8, 1)
+        AXS_ZP3(13, 8, 128, 4, 8, 2)
+        AXS_ZP3(14, 8, 128, 4, 8, 3)
+        AXS_ZP3(15, 8, 128, 5, 8, 6)
+        AXS_ZP2(16, 8, 64, 5)
+        AXS_ZP3(17, 8, 64, 4, 4, 1)
+        AXS_ZP3(18, 8, 64, 5, 4, 1)
+        AXS_ZP3(19, 4, 128, 5, 4, 1)
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
     if (kZVariants[variant].gen == 3) prepare_zmarch(esz, kZVariants[variant].partner);

@@ -35,7 +35,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "axion-strings_gb300")
 
 N_MAIN = 1024
-BYTES_PER_SITE = {32: 32, 64: 64}     # psi1, psi2, pi1, pi2: one read + one write each
+# per site and pass of the step kernel: psi1, psi2, pi1, pi2 read once and
+# written once; a two-step pass (halo depth 2) advances every site twice
+BYTES_PER_SITE = {32: 32, 64: 64}
 ENSEMBLE_SIZES = (64, 96, 128, 160, 192)
 
 
@@ -310,13 +312,17 @@ def gpu_arm(args, dist):
                        n=args.n)
     sites_all = dist.sum(main["sites"])
     value = sites_all * args.steps / (main["ms"] * 1e-3)
-    per_launch_ms = main["ms"] / args.steps
+    launches = max(1, main["launches"])
+    steps_per_launch = args.steps / launches              # 2 for the two-step kernel, else 1
+    per_launch_ms = main["ms"] / launches
     achieved = BYTES_PER_SITE[args.precision] * main["sites"] / (per_launch_ms * 1e-3) / 1e9
+    two_step = "two steps per pass" in main["desc"]
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "k_zmarch_traffic.txt")
+    tkey = "zmarch_2step_fp32_1024_per_launch_bytes:" if two_step else "zmarch_fp32_1024_per_launch_bytes:"
     if args.precision == 32 and args.n == N_MAIN and os.path.exists(tfile):
         for line in open(tfile):
-            if line.startswith("zmarch_fp32_1024_per_launch_bytes:"):
+            if line.startswith(tkey):
                 traffic = float(line.split(":", 1)[1]) / 1e9     # GB per launch, like `achieved`'s bytes
     fp64 = ens = None
     if not args.quick:
@@ -357,7 +363,8 @@ def gpu_arm(args, dist):
                      "traffic": traffic, "traffic_unit": "GB per launch (ncu dram read+write)",
                      "algorithmic_gb_per_launch": BYTES_PER_SITE[args.precision] * main["sites"] / 1e9,
                      "peak_source": peak_note,
-                     "algorithmic_bytes_per_site_update": BYTES_PER_SITE[args.precision]},
+                     "algorithmic_bytes_per_site_update": BYTES_PER_SITE[args.precision] / steps_per_launch,
+                     "steps_per_launch": steps_per_launch, "ms_per_launch": per_launch_ms},
         "cpu_baseline": cpu,
         "e2e": e2e_line,
         "gpu_launches": main["launches"],

@@ -76,7 +76,8 @@ def test_kernel_variants_bit_identical(axs, oracle, precision):
             assert np.array_equal(g[q], g0[q]), (d0, d, q)
 
 
-TWO_STEP = ["1,10,32", "1,11,64", "1,12,128", "1,13,16", "1,14,64"]
+TWO_STEP = ["1,10,32", "1,11,64", "1,12,128", "1,13,16", "1,14,64", "1,15,128", "1,17,32", "1,18,64",
+            "1,19,128"]
 
 
 @pytest.mark.parametrize("N", [64, 160])
