@@ -329,12 +329,14 @@ def gpu_arm(args, dist):
         f64 = run_lattice(axs, dist, 64, max(3, args.steps // 2), args.warmup, with_e2e=False, n=args.n)
         r64 = dist.sum(f64["sites"]) * max(3, args.steps // 2) / (f64["ms"] * 1e-3)
         fp64 = {"value": r64, "unit": "site-updates/s", "ms_per_step": f64["ms"] / max(3, args.steps // 2),
-                "hbm_frac": r64 / dist.world * 64 / 1e9 / hbm, "kernel": f64["desc"],
+                "hbm_frac": r64 / dist.world * 64 * f64["launches"] / max(3, args.steps // 2) / 1e9 / hbm,
+                "kernel": f64["desc"],
                 "fp32_over_fp64": value / r64}
         e = run_ensemble(axs, dist, args.steps, args.warmup)
         re = e["sites"] * args.steps / (e["ms"] * 1e-3)
         ens = {"value": re, "unit": "site-updates/s", "members": e["members"], "sites": e["sites"],
-               "ms_per_step": e["ms"] / args.steps, "hbm_frac": re / dist.world * 32 / 1e9 / hbm,
+               "ms_per_step": e["ms"] / args.steps,
+               "hbm_frac": re / dist.world * 32 * e["launches"] / args.steps / 1e9 / hbm,
                "master_seed": e["master_seed"], "launches_per_step": e["launches"] / args.steps}
     cpu = None
     if dist.rank == 0 and not args.no_cpu:
