@@ -568,6 +568,12 @@ struct RefBinsI {
         while ((int64_t)(s + 1) * (s + 1) <= n2) ++s;
         return s - 1;
     }
+    // bin of n2 >= the n2 that gave b (bins only grow along a row)
+    __device__ __forceinline__ int next(int b, int64_t n2) const {
+        if (b < 0 || n2 >= (int64_t)half * half) return bin(n2);
+        while ((int64_t)(b + 2) * (b + 2) <= n2) ++b;
+        return b;
+    }
 };
 struct LogBinsI {
     const int *thr;   // thr[b] for b = 1..nbins-1 (thr[0] = 0)
@@ -587,6 +593,12 @@ struct LogBinsI {
         }
         return lo;
     }
+    // bin of n2 >= the n2 that gave b (bins only grow along a row)
+    __device__ __forceinline__ int next(int b, int64_t n2) const {
+        if (b < 0) return bin(n2);
+        while (b + 1 < nbins && (int64_t)thr[b + 1] <= n2) ++b;
+        return b;
+    }
 };
 
 // Float-float values (hi + lo, about 48 significant bits): the warp-level sums
@@ -603,8 +615,8 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
     const float hi = __fadd_rn(s, err);
     return FF{hi, __fsub_rn(err, __fsub_rn(hi, s))};
 }
-__device__ __forceinline__ FF ff_shfl_xor(FF a, int o) {
-    return FF{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+__device__ __forceinline__ FF ff_shfl_up(FF a, int o) {
+    return FF{__shfl_up_sync(0xffffffffu, a.hi, o), __shfl_up_sync(0xffffffffu, a.lo, o)};
 }
 __device__ __forceinline__ double ff_to_double(FF a) { return (double)a.hi + (double)a.lo; }
 
@@ -616,26 +628,37 @@ template <> __device__ __forceinline__ FF mode_power<double>(const double2 &f) {
     return FF{hi, __double2float_rn(v - (double)hi)};
 }
 
-// Same deterministic per-warp histograms and block partial rows as k_bin
-// (three rows: power, |n|, count); warps walk whole rows of the half spectrum
-// (no per-mode division), |n| comes from a float-float table, lanes of one bin
-// are summed in float-float by a fixed shuffle tree and flushed by one lane in
-// FP64.
+// Run-length binner over the rows of the half spectrum. Along a row |n|^2 =
+// ix^2 + c only grows, so the bins do too: each lane takes a contiguous slice
+// of the (shared-memory staged) row and sums runs of one bin in registers
+// (float-float). A run strictly inside a lane's slice belongs to that lane
+// alone and goes straight into the warp's histogram; a lane's first run may
+// continue runs of the lanes before it (equal bins sit in consecutive lanes:
+// one segmented scan of 5 shuffle steps), and its last run has a bin no other
+// lane's last run has. Every bin thus receives its sums in an order fixed by
+// the data: results are the same run to run and for an ensemble member alone.
+// Per-warp histograms, block partial rows and k_bin_final3 as before (three
+// rows: power, |n|, count).
 template <typename T, typename B>
-__global__ void __launch_bounds__(128) k_bin_rows(const typename Cplx<T>::type *__restrict__ F, int N, int ndims,
+__global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *__restrict__ F, int N, int ndims,
                                                   B binner, int nbins, const float2 *__restrict__ sqrt_tab,
                                                   double *__restrict__ partials) {
-    extern __shared__ double hist[];   // [4 warps][3][nbins], then the bin table
+    typedef typename Cplx<T>::type C;
+    extern __shared__ double hist[];   // [4 warps][3][nbins], bin table, [4 warps][nh] staged rows
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nh = N / 2 + 1;
     for (int i = threadIdx.x; i < 4 * 3 * nbins; i += blockDim.x) hist[i] = 0.0;
     const B bins = binner.staged(hist + 4 * 3 * nbins);
+    // staged rows start 16-byte aligned (complex double rows are read as double2)
+    C *stage = reinterpret_cast<C *>(hist + (((4 * 3 + B::kSmemTable) * nbins + 1) & ~1)) + (size_t)w * nh;
     __syncthreads();
     double *hp = hist + (size_t)w * 3 * nbins;
     double *hk = hp + nbins;
     double *hc = hk + nbins;
-    const int nh = N / 2 + 1;
     const int64_t rows = ndims == 2 ? (int64_t)N : (int64_t)N * N;
     const int64_t nwarps = (int64_t)gridDim.x * 4;
+    const int chunk = (nh + 31) / 32;
+    const int lo = min(nh, lane * chunk), hi = min(nh, lo + chunk);
     for (int64_t r = (int64_t)blockIdx.x * 4 + w; r < rows; r += nwarps) {
         int64_t c2;
         if (ndims == 2) {
@@ -646,45 +669,70 @@ __global__ void __launch_bounds__(128) k_bin_rows(const typename Cplx<T>::type *
             const int64_t fz = iz < N / 2 ? iz : iz - N, fy = iy < N / 2 ? iy : iy - N;
             c2 = fy * fy + fz * fz;
         }
-        const typename Cplx<T>::type *row = F + r * nh;
-        for (int ix0 = 0; ix0 < nh; ix0 += 32) {
-            const int ix = ix0 + lane;
-            int b = -1, wt = 0;
-            FF v{0.f, 0.f}, kk{0.f, 0.f};
-            if (ix < nh) {
-                const int64_t n2 = (int64_t)ix * ix + c2;
-                b = bins.bin(n2);
+        const C *row = F + r * nh;
+        for (int ix = lane; ix < nh; ix += 32) stage[ix] = row[ix];
+        __syncwarp();
+        int b = -1, fb = -1, lb = -1;
+        FF v{0.f, 0.f}, kk{0.f, 0.f}, fv{0.f, 0.f}, fk{0.f, 0.f};
+        int c = 0, fc = 0;
+        for (int ix = lo; ix < hi; ++ix) {
+            const int64_t n2 = (int64_t)ix * ix + c2;
+            const int nb = bins.next(b, n2);
+            if (nb != b) {
                 if (b >= 0) {
-                    wt = (ix == 0 || 2 * ix == N) ? 1 : 2;
-                    const float fw = (float)wt;   // x1 or x2: exact in float-float
-                    const FF p = mode_power<T>(row[ix]);
-                    const float2 sq = sqrt_tab[n2];
-                    v = FF{fw * p.hi, fw * p.lo};
-                    kk = FF{fw * sq.x, fw * sq.y};
+                    if (fb < 0) { fb = b; fv = v; fk = kk; fc = c; }
+                    else {   // a run inside the slice: no other lane has this bin in this row
+                        hp[b] += ff_to_double(v);
+                        hk[b] += ff_to_double(kk);
+                        hc[b] += (double)c;
+                    }
                 }
+                b = nb;
+                v = kk = FF{0.f, 0.f};
+                c = 0;
             }
-            unsigned active = __ballot_sync(0xffffffffu, b >= 0);
-            while (active) {
-                const int leader = __ffs(active) - 1;
-                const int bl = __shfl_sync(0xffffffffu, b, leader);
-                const unsigned same = __ballot_sync(0xffffffffu, b == bl) & active;
-                const bool mine = (same >> lane) & 1u;
-                FF sv = mine ? v : FF{0.f, 0.f}, sk = mine ? kk : FF{0.f, 0.f};
-                int sc = mine ? wt : 0;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    sv = ff_add(sv, ff_shfl_xor(sv, o));
-                    sk = ff_add(sk, ff_shfl_xor(sk, o));
-                    sc += __shfl_xor_sync(0xffffffffu, sc, o);
-                }
-                if (lane == 0) {
-                    hp[bl] += ff_to_double(sv);
-                    hk[bl] += ff_to_double(sk);
-                    hc[bl] += (double)sc;
-                }
-                active &= ~same;
+            if (nb >= 0) {
+                const int wt = (ix == 0 || 2 * ix == N) ? 1 : 2;
+                const float fw = (float)wt;   // x1 or x2: exact in float-float
+                const FF p = mode_power<T>(stage[ix]);
+                const float2 sq = sqrt_tab[n2];
+                v = ff_add(v, FF{fw * p.hi, fw * p.lo});
+                kk = ff_add(kk, FF{fw * sq.x, fw * sq.y});
+                c += wt;
             }
         }
+        FF lv{0.f, 0.f}, lk{0.f, 0.f};
+        int lc = 0;
+        if (b >= 0) {   // the open run: the lane's first if it has none yet, else its last
+            if (fb < 0) { fb = b; fv = v; fk = kk; fc = c; }
+            else { lb = b; lv = v; lk = kk; lc = c; }
+        }
+        __syncwarp();   // inside runs are in; the staged row is no longer read
+        // first runs: inclusive segmented scan over lanes with equal bins
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int ob = __shfl_up_sync(0xffffffffu, fb, o);
+            const FF ov = ff_shfl_up(fv, o), ok = ff_shfl_up(fk, o);
+            const int oc = __shfl_up_sync(0xffffffffu, fc, o);
+            if (lane >= o && fb >= 0 && ob == fb) {
+                fv = ff_add(ov, fv);
+                fk = ff_add(ok, fk);
+                fc += oc;
+            }
+        }
+        const int nextb = __shfl_down_sync(0xffffffffu, fb, 1);
+        if (fb >= 0 && (lane == 31 || nextb != fb)) {
+            hp[fb] += ff_to_double(fv);
+            hk[fb] += ff_to_double(fk);
+            hc[fb] += (double)fc;
+        }
+        __syncwarp();
+        if (lb >= 0) {
+            hp[lb] += ff_to_double(lv);
+            hk[lb] += ff_to_double(lk);
+            hc[lb] += (double)lc;
+        }
+        __syncwarp();
     }
     __syncthreads();
     for (int bn = threadIdx.x; bn < nbins; bn += blockDim.x) {
@@ -723,8 +771,44 @@ __global__ void k_gather_axion(const typename Cplx<T>::type *__restrict__ psi, c
     for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
         auto a = psi[m];
         auto p = pi[m];
-        T r = sqrt(a.x * a.x + a.y * a.y);
-        dst[m] = r > (T)0 ? (a.y * p.x - a.x * p.y) * itau / r : (T)0;
+        dst[m] = axion_f<T>(a.x, a.y, p.x, p.y, itau);
+    }
+}
+
+// The same f straight from psi and pih for 3D radius 1: pi_n is formed per
+// site with k_sync_pi's arithmetic and never stored. Each thread marches one
+// (x, y) column through z with psi's z-neighbours in registers, so every psi
+// plane comes from DRAM once (the x and y neighbours are the neighbouring
+// threads' loads of the same plane, in L1); 20 B per site (psi, pih in, f out)
+// instead of 48 B for the two-kernel path. Blocks are 32 x 8 columns.
+template <typename T>
+__global__ void __launch_bounds__(256) k_axion_zcol(const typename Cplx<T>::type *__restrict__ psi,
+                                                    const typename Cplx<T>::type *__restrict__ pih, T *__restrict__ dst,
+                                                    const double *clock, int N, double dt, double inv_dx2, double lambda,
+                                                    double T0sq3, int prs, int fresh, double tau) {
+    typedef typename Cplx<T>::type C;
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= N || y >= N) return;
+    const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs);
+    const T itau = (T)(1.0 / tau);
+    const int64_t NN = (int64_t)N * N;
+    const int64_t col = (int64_t)y * N + x;
+    const int64_t xm = (int64_t)y * N + (x == 0 ? N - 1 : x - 1), xp = (int64_t)y * N + (x == N - 1 ? 0 : x + 1);
+    const int64_t ym = (int64_t)(y == 0 ? N - 1 : y - 1) * N + x, yp = (int64_t)(y == N - 1 ? 0 : y + 1) * N + x;
+    C zm = psi[(int64_t)(N - 1) * NN + col], zc = psi[col];
+    for (int z = 0; z < N; ++z) {
+        const int64_t base = (int64_t)z * NN;
+        const C zp = psi[(z + 1 == N ? 0 : base + NN) + col];
+        C p = pih[base + col];
+        if (!fresh) {   // a fresh state holds pi_0 itself (the reference's ker is zero)
+            const C a = psi[base + xm], b = psi[base + xp], d = psi[base + ym], e = psi[base + yp];
+            const T L1 = lap7<T>(zc.x, a.x, b.x, d.x, e.x, zm.x, zp.x);
+            const T L2 = lap7<T>(zc.y, a.y, b.y, d.y, e.y, zm.y, zp.y);
+            sync_pi_site<T>(zc.x, zc.y, L1, L2, p.x, p.y, c);
+        }
+        dst[base + col] = axion_f<T>(zc.x, zc.y, p.x, p.y, itau);
+        zm = zc;
+        zc = zp;
     }
 }
 
@@ -752,7 +836,8 @@ static void bin_spectrum(Lattice *L, const B &binner, int nbins, std::vector<dou
                          std::vector<unsigned long long> &cnt) {
     int N = L->p.N;
     int64_t half = (L->p.NDIMS == 2 ? (int64_t)N : (int64_t)N * N) * (N / 2 + 1);
-    size_t sm = (size_t)(4 * 3 + B::kSmemTable) * nbins * sizeof(double);
+    const int nh = N / 2 + 1;
+    size_t sm = (size_t)(((4 * 3 + B::kSmemTable) * nbins + 1) & ~1) * sizeof(double) + (size_t)4 * nh * 2 * L->esz;
     // as many 4-warp blocks as fit on the SMs (up to 16 per SM): the per-warp
     // histograms leave this kernel latency-bound at low occupancy
     int per_sm = (int)std::max<size_t>(1, std::min<size_t>(16, (size_t)(200 * 1024) / std::max<size_t>(sm, 1)));
@@ -773,13 +858,13 @@ static void bin_spectrum(Lattice *L, const B &binner, int nbins, std::vector<dou
             count_launches(1);
         }
         if (sm > 48 * 1024) {
-            if (L->esz == 4) AXS_CUDA(cudaFuncSetAttribute(k_bin_rows<float, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            else AXS_CUDA(cudaFuncSetAttribute(k_bin_rows<double, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            if (L->esz == 4) AXS_CUDA(cudaFuncSetAttribute(k_bin_runs<float, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            else AXS_CUDA(cudaFuncSetAttribute(k_bin_runs<double, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         }
         if (L->esz == 4)
-            k_bin_rows<float, B><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, (const float2 *)L->dsqrt, part);
+            k_bin_runs<float, B><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, (const float2 *)L->dsqrt, part);
         else
-            k_bin_rows<double, B><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, (const float2 *)L->dsqrt, part);
+            k_bin_runs<double, B><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, (const float2 *)L->dsqrt, part);
         AXS_CUDA(cudaGetLastError());
         k_bin_final3<<<nbins, 256, 0, L->stream>>>(part, nblk, nbins, out);
         AXS_CUDA(cudaGetLastError());
@@ -831,14 +916,30 @@ void powerspec(Lattice *L, int field, double *pk, double *ks, int *count) {
 void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *count) {
     if (nbins < 1) fail(AXS_ERR_ARG, "nbins must be >= 1");
     ensure_fft(L);
-    launch_sync_pi(L);
-    int g = grid_cap(L->length, 256, 16);
-    if (L->esz == 4)
-        k_gather_axion<float><<<g, 256, 0, L->stream>>>((const float2 *)L->psi[L->cur], (const float2 *)L->scratch,
-                                                        (float *)L->fft_in, L->length, L->tau);
-    else
-        k_gather_axion<double><<<g, 256, 0, L->stream>>>((const double2 *)L->psi[L->cur], (const double2 *)L->scratch,
-                                                         (double *)L->fft_in, L->length, L->tau);
+    if (L->p.NDIMS == 3 && L->p.stencil_setting == 0) {
+        const axs_params &p = L->p;
+        const int N = p.N;
+        const double dx = p.space_step, T0 = p.T_initial;
+        dim3 grid((N + 31) / 32, (N + 7) / 8), block(32, 8);
+        if (L->esz == 4)
+            k_axion_zcol<float><<<grid, block, 0, L->stream>>>(
+                (const float2 *)L->psi[L->cur], (const float2 *)L->pih, (float *)L->fft_in, L->dclock + L->cur, N,
+                (double)p.time_step, 1.0 / (dx * dx), (double)p.lambda, (T0 * T0) / 3.0, p.prs, L->fresh, L->tau);
+        else
+            k_axion_zcol<double><<<grid, block, 0, L->stream>>>(
+                (const double2 *)L->psi[L->cur], (const double2 *)L->pih, (double *)L->fft_in, L->dclock + L->cur, N,
+                (double)p.time_step, 1.0 / (dx * dx), (double)p.lambda, (T0 * T0) / 3.0, p.prs, L->fresh, L->tau);
+    } else {
+        launch_sync_pi(L);
+        int g = grid_cap(L->length, 256, 16);
+        if (L->esz == 4)
+            k_gather_axion<float><<<g, 256, 0, L->stream>>>((const float2 *)L->psi[L->cur], (const float2 *)L->scratch,
+                                                            (float *)L->fft_in, L->length, L->tau);
+        else
+            k_gather_axion<double><<<g, 256, 0, L->stream>>>((const double2 *)L->psi[L->cur],
+                                                             (const double2 *)L->scratch, (double *)L->fft_in, L->length,
+                                                             L->tau);
+    }
     AXS_CUDA(cudaGetLastError());
     count_launches(1);
     exec_r2c(L);

@@ -275,6 +275,24 @@ __device__ __forceinline__ void site_update(T a, T b, T L1, T L2, T &p1, T &p2, 
     bn = fma(c.dt, p2, b);
 }
 
+// Synchronised momentum of one site: pi_n = pih_{n-1} + dt/2 K(psi_n) with
+// c = make_coefs(tau_n, dt, dt/2, ...); (L1, L2) the stencil sums.
+template <typename T>
+__device__ __forceinline__ void sync_pi_site(T a, T b, T L1, T L2, T &p1, T &p2, const StepCoefs<T> &c) {
+    T r = fma(a, a, fma(b, b, c.c0));
+    T g = c.kdt_coef * r;
+    p1 = fma(c.kdt_idx2, L1, fma(g, a, p1));
+    p2 = fma(c.kdt_idx2, L2, fma(g, b, p2));
+}
+
+// The axion field of the kinetic spectrum, f = |phi| dtheta/dtau =
+// (psi2 pi1 - psi1 pi2) / (tau |psi|), with itau = 1/tau.
+template <typename T>
+__device__ __forceinline__ T axion_f(T a, T b, T p1, T p2, T itau) {
+    T r = sqrt(a * a + b * b);
+    return r > (T)0 ? (b * p1 - a * p2) * itau / r : (T)0;
+}
+
 // Philox-4x32-10 (Salmon et al., SC'11) and Box-Muller; the deviate for
 // array a at offset m. Must agree with the oracle's definition.
 // Both deviates of arrays 2*pair and 2*pair+1 at offset m from one Philox block

@@ -130,10 +130,7 @@ __global__ void k_sync_pi(const typename Cplx<T>::type *__restrict__ psi, const 
         typename Cplx<T>::type ctr;
         stencil_at<T, ND, R>(psi, m, N, setting, L1, L2, ctr);
         auto p = pih[m];
-        T r = fma(ctr.x, ctr.x, fma(ctr.y, ctr.y, c.c0));
-        T g = c.kdt_coef * r;
-        p.x = fma(c.kdt_idx2, L1, fma(g, ctr.x, p.x));
-        p.y = fma(c.kdt_idx2, L2, fma(g, ctr.y, p.y));
+        sync_pi_site<T>(ctr.x, ctr.y, L1, L2, p.x, p.y, c);
         dst[m] = p;
     }
 }

@@ -58,3 +58,38 @@ def test_axion_spectrum_matches_oracle(axs, oracle, nd, N, nbins):
     ok = cnto > 0
     assert rel(pk[ok], pko[ok]) <= 1e-10
     assert rel(k[ok], ko[ok]) <= 1e-12
+
+
+@pytest.mark.parametrize("N,nbins", [(40, 24), (32, 16)])
+def test_axion_spectrum_fresh_state(axs, oracle, N, nbins):
+    """Right after an upload the momentum is pi_0 itself (no stencil term)."""
+    p = params(axs, 3, N, 64, T_initial=0.0)
+    op = orc(p)
+    f = oracle.init_flat(op, 5, 2.0)
+    with axs.Lattice(p) as L:
+        L.upload(*f)
+        tau, _ = L.time
+        k, pk, cnt = L.axion_spectrum(nbins)
+    ko, pko, cnto = oracle.axion_spectrum(op, *f, tau, nbins)
+    assert np.array_equal(cnt, cnto)
+    ok = cnto > 0
+    assert rel(pk[ok], pko[ok]) <= 1e-10
+    assert rel(k[ok], ko[ok]) <= 1e-12
+
+
+def test_axion_spectrum_fp32(axs, oracle):
+    """FP32 fields: the spectrum of the downloaded (FP32) state within 1e-4."""
+    p = params(axs, 3, 48, 32, T_initial=0.0)
+    op = orc(p)
+    f = oracle.init_flat(op, 6, 2.0)
+    with axs.Lattice(p) as L:
+        L.upload(*f)
+        L.evolve(9)
+        g = L.download()
+        tau, _ = L.time
+        k, pk, cnt = L.axion_spectrum(32)
+    ko, pko, cnto = oracle.axion_spectrum(op, *g, tau, 32)
+    assert np.array_equal(cnt, cnto)
+    ok = cnto > 0
+    assert rel(pk[ok], pko[ok]) <= 1e-4
+    assert rel(k[ok], ko[ok]) <= 1e-6
