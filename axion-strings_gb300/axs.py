@@ -42,6 +42,7 @@ class Params(ctypes.Structure):
         ("precision", ctypes.c_int),
         ("prs", ctypes.c_int),
         ("tau_initial", ctypes.c_double),
+        ("form", ctypes.c_int),
     ]
 
     def as_dict(self):

@@ -60,6 +60,23 @@ __device__ __forceinline__ double circd(double a, double b) {
 }
 __device__ __forceinline__ double sum3(double a, double b, double c) { return __dadd_rn(__dadd_rn(a, b), c); }
 
+// The reference's double decision for the 3D cell whose (i,j,k) corner is
+// site (x, y, z) (reference (i,j,k) = (z,y,x)). Out of line: it runs only for
+// cells within the float margin, and inlined its double registers would
+// lower the occupancy of the float path.
+template <typename T, bool FROM_THETA>
+__device__ __noinline__ int cell3_exact(Corner<T, FROM_THETA> cn, int64_t x, int64_t y, int64_t z, int N,
+                                        double accept) {
+    const int64_t NN = (int64_t)N * N;
+    const int64_t xp = x + 1 == N ? 0 : x + 1, yp = y + 1 == N ? 0 : y + 1, zp = z + 1 == N ? 0 : z + 1;
+    const double d000 = cn.nd(z * NN + y * N + x), d100 = cn.nd(zp * NN + y * N + x), d110 = cn.nd(zp * NN + yp * N + x),
+                 d010 = cn.nd(z * NN + yp * N + x), d011 = cn.nd(z * NN + yp * N + xp), d001 = cn.nd(z * NN + y * N + xp);
+    const double ta = sum3(circd(d000, d100), circd(d100, d110), circd(d110, d010));
+    const double tb = sum3(circd(d000, d100), circd(d100, d011), circd(d011, d001));
+    const double tc = sum3(circd(d000, d010), circd(d010, d011), circd(d011, d001));
+    return (ta > accept || tb > accept || tc > accept) ? 1 : 0;
+}
+
 template <typename T, int ND, bool FROM_THETA>
 __global__ void __launch_bounds__(256) k_cores(const typename Cplx<T>::type *__restrict__ psi,
                                                const double *__restrict__ theta, uint8_t *__restrict__ mask, int N,
@@ -102,14 +119,7 @@ __global__ void __launch_bounds__(256) k_cores(const typename Cplx<T>::type *__r
             float mx = fmaxf(sa, fmaxf(sb, sc));
             if (mx > acc_f + kMargin) flag = 1;
             else if (mx < acc_f - kMargin) flag = 0;
-            else {
-                double d000 = cn.nd(o000), d100 = cn.nd(o100), d110 = cn.nd(o110), d010 = cn.nd(o010),
-                       d011 = cn.nd(o011), d001 = cn.nd(o001);
-                double ta = sum3(circd(d000, d100), circd(d100, d110), circd(d110, d010));
-                double tb = sum3(circd(d000, d100), circd(d100, d011), circd(d011, d001));
-                double tc = sum3(circd(d000, d010), circd(d010, d011), circd(d011, d001));
-                flag = (ta > accept || tb > accept || tc > accept);
-            }
+            else flag = cell3_exact<T, FROM_THETA>(cn, x, y, z, N, accept);
         }
         mask[m] = (uint8_t)flag;
         local += flag;
@@ -126,7 +136,7 @@ __global__ void __launch_bounds__(256) k_cores(const typename Cplx<T>::type *__r
 static constexpr int kCX = 64, kCY = 8, kCZ = 32;   // cells per block tile; 256 threads x 2 cells
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_cores3_tiled(const typename Cplx<T>::type *__restrict__ psi,
+__global__ void __launch_bounds__(256, 4) k_cores3_tiled(const typename Cplx<T>::type *__restrict__ psi,
                                                       uint8_t *__restrict__ mask, int N, double accept,
                                                       unsigned long long *count) {
     typedef typename Cplx<T>::type C;
@@ -189,16 +199,7 @@ __global__ void __launch_bounds__(256) k_cores3_tiled(const typename Cplx<T>::ty
             const int64_t m = (int64_t)z * NN + (int64_t)y * N + x;
             if (mx > acc_f + kMargin) flag = 1;
             else if (mx < acc_f - kMargin) flag = 0;
-            else {
-                const int64_t xp = x + 1 == N ? 0 : x + 1, yp = y + 1 == N ? 0 : y + 1, zp = z + 1 == N ? 0 : z + 1;
-                const double d000 = cn.nd(m), d100 = cn.nd(zp * NN + (int64_t)y * N + x),
-                             d110 = cn.nd(zp * NN + yp * N + x), d010 = cn.nd((int64_t)z * NN + yp * N + x),
-                             d011 = cn.nd((int64_t)z * NN + yp * N + xp), d001 = cn.nd((int64_t)z * NN + (int64_t)y * N + xp);
-                const double ta = sum3(circd(d000, d100), circd(d100, d110), circd(d110, d010));
-                const double tb = sum3(circd(d000, d100), circd(d100, d011), circd(d011, d001));
-                const double tc = sum3(circd(d000, d010), circd(d010, d011), circd(d011, d001));
-                flag = (ta > accept || tb > accept || tc > accept);
-            }
+            else flag = cell3_exact<T, false>(cn, x, y, z, N, accept);
             mask[m] = (uint8_t)flag;
             local += flag;
         }
@@ -789,7 +790,7 @@ __global__ void __launch_bounds__(256) k_axion_zcol(const typename Cplx<T>::type
     typedef typename Cplx<T>::type C;
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
     if (x >= N || y >= N) return;
-    const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs);
+    const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs, 0);
     const T itau = (T)(1.0 / tau);
     const int64_t NN = (int64_t)N * N;
     const int64_t col = (int64_t)y * N + x;
@@ -915,6 +916,7 @@ void powerspec(Lattice *L, int field, double *pk, double *ks, int *count) {
 
 void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *count) {
     if (nbins < 1) fail(AXS_ERR_ARG, "nbins must be >= 1");
+    if (L->p.form != 0) fail(AXS_ERR_STATE, "the axion kinetic spectrum is defined on the field-rescaled variables (form 0)");
     ensure_fft(L);
     if (L->p.NDIMS == 3 && L->p.stencil_setting == 0) {
         const axs_params &p = L->p;
@@ -1091,6 +1093,7 @@ void background(Lattice *L, double out[6]) {
 }
 
 void energies(Lattice *L, double out[3]) {
+    if (L->p.form != 0) fail(AXS_ERR_STATE, "the energies are defined on the field-rescaled variables (form 0)");
     launch_sync_pi(L);
     int g = reduce_grid(L->length);
     double *part = ensure_partials(L, g, 3);

@@ -84,6 +84,7 @@ static void validate(const axs_params &p) {
     if (!(p.space_step > 0.0f)) fail(AXS_ERR_ARG, "space_step must be positive");
     if (!std::isfinite(p.time_step)) fail(AXS_ERR_ARG, "time_step must be finite");
     if (p.N > 4096) fail(AXS_ERR_ARG, "N=%d exceeds the supported maximum 4096", p.N);
+    if (p.form != 0 && p.form != 1) fail(AXS_ERR_ARG, "form must be 0 (field-rescaled) or 1 (Hamiltonian)");
 }
 
 static void set_device_clock(Lattice *L) {
@@ -356,6 +357,7 @@ void axs_default_params(axs_params *p) {
     p->precision = AXS_F64;
     p->prs = 1;
     p->tau_initial = 1.0;      // physics.cpp:50
+    p->form = 0;               // vvsl_field_rescaled, the integrator s_run.cpp calls
 }
 
 int axs_last_error(char *buf, size_t len) {
@@ -653,8 +655,8 @@ int axs_ensemble_create(const axs_params *members, int n, axs_ensemble **out) {
     for (int i = 1; i < n; ++i) {
         const axs_params &a = members[0], &b = members[i];
         if (a.NDIMS != b.NDIMS || a.precision != b.precision || a.time_step != b.time_step ||
-            a.space_step != b.space_step || a.stencil_setting != b.stencil_setting)
-            fail(AXS_ERR_ARG, "ensemble members must share NDIMS, precision, dt, dx and stencil");
+            a.space_step != b.space_step || a.stencil_setting != b.stencil_setting || a.form != b.form)
+            fail(AXS_ERR_ARG, "ensemble members must share NDIMS, precision, dt, dx, stencil and form");
     }
     axs_ensemble *e = new axs_ensemble();
     try {

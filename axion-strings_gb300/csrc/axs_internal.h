@@ -74,7 +74,7 @@ struct ZLat {
     int a_index;             // which of psi[0]/psi[1] is "current" at launch parity 0
     int64_t item_base;
     double dt, inv_dx2, lambda, T0sq3;
-    int prs;
+    int prs, form;
     int debug_tx_excess;     // test-only: bytes the first load of each item expects but never gets
 };
 
@@ -237,10 +237,23 @@ template <typename T> struct StepCoefs {
     T c0;        // T0^2/3 - tau^2
 };
 
+// form 0, field-rescaled (s_integrate.cpp:305-348): K = L/dx^2 - lambda/tau^(2 prs)
+//   psi (|psi|^2 - tau^2 + T0^2/3), drift dt.
+// form 1, Hamiltonian-like (s_integrate.cpp:358-395): K = tau^2 L/dx^2 - lambda tau^2
+//   phi (|phi|^2 - 1 + T0^2/(3 tau^2)), drift dt / tau_{n+1}^2 (tau is advanced
+//   before the drift there).
 template <typename T>
 __device__ __forceinline__ StepCoefs<T> make_coefs(double tau, double dt, double kick, double inv_dx2,
-                                                    double lambda, double T0sq3, int prs) {
+                                                    double lambda, double T0sq3, int prs, int form) {
     StepCoefs<T> c;
+    if (form == 1) {
+        const double t1 = tau + dt, tsq = tau * tau;
+        c.dt = (T)(dt / (t1 * t1));
+        c.kdt_idx2 = (T)(kick * tsq * inv_dx2);
+        c.kdt_coef = (T)(kick * (-lambda * tsq));
+        c.c0 = (T)(T0sq3 / tsq - 1.0);
+        return c;
+    }
     double coef = prs ? -lambda / (tau * tau) : -lambda;
     c.dt = (T)dt;
     c.kdt_idx2 = (T)(kick * inv_dx2);

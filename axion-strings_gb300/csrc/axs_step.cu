@@ -31,8 +31,9 @@ namespace axs {
 template <typename T>
 __global__ void k_drift0(const typename Cplx<T>::type *__restrict__ psi, typename Cplx<T>::type *__restrict__ out,
                          const typename Cplx<T>::type *__restrict__ pih, const double *clock_in, double *clock_out,
-                         int64_t len, double dt) {
-    T d = (T)dt;
+                         int64_t len, double dt, int form) {
+    const double t1 = *clock_in + dt;
+    const T d = (T)(form == 1 ? dt / (t1 * t1) : dt);   // the drift of make_coefs
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
         auto a = psi[m];
@@ -101,9 +102,9 @@ __global__ void __launch_bounds__(256) k_step_generic(const typename Cplx<T>::ty
                                                       typename Cplx<T>::type *__restrict__ pih,
                                                       const double *clock_in, double *clock_out, int N, int64_t len,
                                                       double dt, double inv_dx2, double lambda, double T0sq3, int prs,
-                                                      int setting) {
+                                                      int setting, int form) {
     double tau = *clock_in;
-    StepCoefs<T> c = make_coefs<T>(tau, dt, dt, inv_dx2, lambda, T0sq3, prs);
+    StepCoefs<T> c = make_coefs<T>(tau, dt, dt, inv_dx2, lambda, T0sq3, prs, form);
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
         T L1, L2;
@@ -122,8 +123,8 @@ __global__ void __launch_bounds__(256) k_step_generic(const typename Cplx<T>::ty
 template <typename T, int ND, int R>
 __global__ void k_sync_pi(const typename Cplx<T>::type *__restrict__ psi, const typename Cplx<T>::type *__restrict__ pih,
                           typename Cplx<T>::type *__restrict__ dst, const double *clock, int N, int64_t len, double dt,
-                          double inv_dx2, double lambda, double T0sq3, int prs, int setting) {
-    StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs);
+                          double inv_dx2, double lambda, double T0sq3, int prs, int setting, int form) {
+    StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs, form);
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
         T L1, L2;
@@ -295,7 +296,7 @@ __global__ void __launch_bounds__(256) k_zmarch(const ZLat *__restrict__ lats, i
         const C *pih = reinterpret_cast<const C *>(Lt.pih[bin]);
         C *pih_out = reinterpret_cast<C *>(Lt.pih[bin ^ 1]);
         const double tau = Lt.clock[bin];
-        const StepCoefs<T> cf = make_coefs<T>(tau, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs);
+        const StepCoefs<T> cf = make_coefs<T>(tau, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs, Lt.form);
         if (local == 0 && tid == 0) Lt.clock[bin ^ 1] = tau + Lt.dt;   // tau += dt, s_integrate.cpp:317
         const bool xhalo = tx < N;
         const uint32_t slot_bytes_tx = (uint32_t)((TY + 2) * tx * K::CS + (xhalo ? 2 * K::H_BYTES : 0));
@@ -591,7 +592,7 @@ __global__ void __launch_bounds__(Z2Cfg<T, TY, TXMAX, S>::NT)
             C *psi_out = reinterpret_cast<C *>(Lt.psi[bin ^ 1]);
             C *pih = reinterpret_cast<C *>(Lt.pih[bin ^ 1]);   // output; the input arrives by TMA
             const double tau = Lt.clock[bin];
-            const StepCoefs<T> cf = make_coefs<T>(tau, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs);
+            const StepCoefs<T> cf = make_coefs<T>(tau, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs, Lt.form);
             if (local == 0 && cid == 0) Lt.clock[bin ^ 1] = tau + Lt.dt;   // tau += dt, s_integrate.cpp:317
             const bool xhalo = tx < N;
             const int nvx = tx / K::VS;
@@ -896,8 +897,8 @@ __global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
             float2 *pih_out = reinterpret_cast<float2 *>(Lt.pih[bin ^ 1]);
             const double tau = Lt.clock[bin];
             const double tau1 = tau + Lt.dt;
-            const StepCoefs<float> cf1 = make_coefs<float>(tau, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs);
-            const StepCoefs<float> cf2 = make_coefs<float>(tau1, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs);
+            const StepCoefs<float> cf1 = make_coefs<float>(tau, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs, Lt.form);
+            const StepCoefs<float> cf2 = make_coefs<float>(tau1, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs, Lt.form);
             if (local == 0 && cid == 0) Lt.clock[bin ^ 1] = tau1 + Lt.dt;   // tau += dt twice, s_integrate.cpp:317
             const bool xhalo = tx < N;
             const int nvx = tx / 2;
@@ -1460,6 +1461,7 @@ static int64_t fill_zlat(ZLat &z, Lattice *L, int variant, int zchunk, int64_t i
     double T0 = (double)L->p.T_initial;
     z.T0sq3 = (T0 * T0) / 3.0;
     z.prs = L->p.prs;
+    z.form = L->p.form;
     z.debug_tx_excess = L->debug_tx_excess;
     return (int64_t)z.ntx * z.nty * z.nzc;
 }
@@ -1523,7 +1525,7 @@ static void launch_generic_t(Lattice *L, const double *cin, double *cout) {
     double T0 = p.T_initial;
     k_step_generic<T, ND, R><<<grid_for(L->length), 256, 0, L->stream>>>(
         (const C *)L->psi[L->cur], (C *)L->psi[L->cur ^ 1], (C *)L->pih, cin, cout, p.N, L->length,
-        (double)p.time_step, 1.0 / (dx * dx), (double)p.lambda, (T0 * T0) / 3.0, p.prs, p.stencil_setting);
+        (double)p.time_step, 1.0 / (dx * dx), (double)p.lambda, (T0 * T0) / 3.0, p.prs, p.stencil_setting, p.form);
     AXS_CUDA(cudaGetLastError());
     count_launches(1);
 }
@@ -1562,12 +1564,12 @@ int lattice_advance(Lattice *L, int max_steps) {
             k_drift0<float><<<grid_for(L->length), 256, 0, L->stream>>>((const float2 *)L->psi[L->cur],
                                                                          (float2 *)L->psi[L->cur ^ 1],
                                                                          (const float2 *)L->pih, cin, cout, L->length,
-                                                                         (double)L->p.time_step);
+                                                                         (double)L->p.time_step, L->p.form);
         else
             k_drift0<double><<<grid_for(L->length), 256, 0, L->stream>>>((const double2 *)L->psi[L->cur],
                                                                           (double2 *)L->psi[L->cur ^ 1],
                                                                           (const double2 *)L->pih, cin, cout,
-                                                                          L->length, (double)L->p.time_step);
+                                                                          L->length, (double)L->p.time_step, L->p.form);
         AXS_CUDA(cudaGetLastError());
         count_launches(1);
         L->fresh = 0;
@@ -2057,7 +2059,8 @@ static void sync_pi_t(Lattice *L) {
     double dx = L->p.space_step, T0 = L->p.T_initial;
     k_sync_pi<T, ND, R><<<grid_for(L->length), 256, 0, L->stream>>>(
         (const C *)L->psi[L->cur], (const C *)L->pih, (C *)L->scratch, L->dclock + L->cur, L->p.N, L->length,
-        (double)L->p.time_step, 1.0 / (dx * dx), (double)L->p.lambda, (T0 * T0) / 3.0, L->p.prs, L->p.stencil_setting);
+        (double)L->p.time_step, 1.0 / (dx * dx), (double)L->p.lambda, (T0 * T0) / 3.0, L->p.prs, L->p.stencil_setting,
+        L->p.form);
     AXS_CUDA(cudaGetLastError());
     count_launches(1);
 }

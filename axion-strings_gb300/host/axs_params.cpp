@@ -53,6 +53,7 @@ int read_parameter_file(const char *fname, RunConfig &c, std::string &err) {
         {"refinement_threshold", FLOAT, &c.refinement_threshold, true, false},
         {"gpu_precision", INT, &c.gpu_precision, false, false},
         {"gpu_prs", INT, &c.gpu_prs, false, false},
+        {"gpu_form", INT, &c.gpu_form, false, false},
         {"init_mode", INT, &c.init_mode, false, false},
         {"k_cut", FLOAT, &c.k_cut, false, false},
         {"string_interval", INT, &c.string_interval, false, false},
@@ -117,6 +118,7 @@ axs_params to_params(const RunConfig &c) {
     p.thr = c.thr;
     p.precision = c.gpu_precision;
     p.prs = c.gpu_prs;
+    p.form = c.gpu_form;
     p.tau_initial = 1.0;   // set_physics_variables (src/common/physics.cpp:50)
     return p;
 }

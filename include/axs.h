@@ -72,13 +72,17 @@ typedef struct axs_params {
                                       1 = the reference's standard integrator,
                                       0 = the unrescaled-coupling (physical) equation */
     double       tau_initial;      /* starting conformal time (the reference uses 1)    */
+    int          form;             /* equation of motion: 0 = field-rescaled psi = tau phi
+                                      (vvsl_field_rescaled, s_integrate.cpp:305-348),
+                                      1 = Hamiltonian-like form in phi and pi = tau^2 phi'
+                                      (vvsl_hamiltonian_form, s_integrate.cpp:358-395) */
 } axs_params;
 
 typedef struct axs_lattice axs_lattice;     /* one lattice on the GPU            */
 typedef struct axs_ensemble axs_ensemble;   /* independent lattices, batched     */
 
 /* Fill p with the values of the reference's default.param plus
- * precision = AXS_F64, prs = 1, tau_initial = 1. */
+ * precision = AXS_F64, prs = 1, tau_initial = 1, form = 0. */
 void axs_default_params(axs_params *p);
 
 /* Copy the message of the last failure on this thread into buf. */

@@ -119,6 +119,52 @@ void orc_vvsl_step(const orc_params *p, double *phi1, double *phi2, double *pi1,
     memcpy(ker2, ker2n, sizeof(double) * len);
 }
 
+void orc_vvsl_hamiltonian_step(const orc_params *p, double *phi1, double *phi2, double *pi1, double *pi2,
+                               double *ker1, double *ker2, double *ker1n, double *ker2n, double *tau) {
+    long len = lattice_length(p);
+    float dt = p->time_step;
+    double ddt = dt;
+    *tau = *tau + ddt;                                    /* s_integrate.cpp:364 */
+    double t = *tau, tsq = t * t;
+    /* drift with the advanced tau, s_integrate.cpp:366-370 */
+    #pragma omp parallel for schedule(static)
+    for (long i = 0; i < len; ++i) {
+        phi1[i] += ddt / tsq * (pi1[i] + 0.5f * ddt * ker1[i]);
+        phi2[i] += ddt / tsq * (pi2[i] + 0.5f * ddt * ker2[i]);
+    }
+    /* (tau^2/dx^2) A phi, s_integrate.cpp:374-376 */
+    double c[5];
+    int nc = stencil_coefficients(p->stencil_setting, p->NDIMS, c);
+    double dx = (double)p->space_step;
+    double alpha = tsq / (dx * dx);
+    long N = p->N;
+    #pragma omp parallel for schedule(static)
+    for (long m = 0; m < len; ++m) {
+        ker1n[m] = alpha * stencil_row(phi1, m, p->NDIMS, N, c, nc);
+        ker2n[m] = alpha * stencil_row(phi2, m, p->NDIMS, N, c, nc);
+    }
+    double T0 = p->T_initial;
+    double shift = (T0 * T0) / (3.0f * tsq);
+    double lam = (double)p->lambda;
+    /* potential, s_integrate.cpp:378-382 */
+    #pragma omp parallel for schedule(static)
+    for (long i = 0; i < len; ++i) {
+        double a = phi1[i], b = phi2[i];
+        double br = a * a + b * b - 1.0f + shift;
+        ker1n[i] += -tsq * lam * a * br;
+        ker2n[i] += -tsq * lam * b * br;
+    }
+    /* kick, s_integrate.cpp:384-388 */
+    #pragma omp parallel for schedule(static)
+    for (long i = 0; i < len; ++i) {
+        pi1[i] += 0.5f * (ker1[i] + ker1n[i]) * ddt;
+        pi2[i] += 0.5f * (ker2[i] + ker2n[i]) * ddt;
+    }
+    /* rotate kernels, s_integrate.cpp:390-394 */
+    memcpy(ker1, ker1n, sizeof(double) * len);
+    memcpy(ker2, ker2n, sizeof(double) * len);
+}
+
 /* Float build of the same step (data_t = float, tau float). The SpMV runs in
  * float like mkl_sparse_s_mv; the potential term is evaluated in double as the
  * reference's pow_2(double) promotes it, then rounded into the float kernel. */

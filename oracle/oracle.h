@@ -56,6 +56,10 @@ void orc_laplacian(const orc_params *p, const double *phi, double *out);
 /* One velocity-Verlet step, vvsl_field_rescaled (s_integrate.cpp:305-348). */
 void orc_vvsl_step(const orc_params *p, double *phi1, double *phi2, double *pi1, double *pi2,
                    double *ker1, double *ker2, double *ker1n, double *ker2n, double *tau);
+/* One step of vvsl_hamiltonian_form (s_integrate.cpp:358-395): phi and
+ * pi = tau^2 phi', tau advanced before the drift. */
+void orc_vvsl_hamiltonian_step(const orc_params *p, double *phi1, double *phi2, double *pi1, double *pi2,
+                               double *ker1, double *ker2, double *ker1n, double *ker2n, double *tau);
 /* The same step with float fields and float tau, as the reference compiles
  * without USE_DOUBLE_PRECISION (src/common/common.hpp:19-23). */
 void orc_vvsl_step_f32(const orc_params *p, float *phi1, float *phi2, float *pi1, float *pi2,

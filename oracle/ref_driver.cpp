@@ -54,9 +54,10 @@ void ref_gaussian_thermal(data_t *phi1, data_t *phi2, data_t *phidot1, data_t *p
     gaussian_thermal(phi1, phi2, phidot1, phidot2);    /* init.cpp:33 */
 }
 
-/* n calls of vvsl_field_rescaled (s_integrate.cpp:305) on caller arrays. */
-void ref_steps(data_t *phi1, data_t *phi2, data_t *pd1, data_t *pd2,
-               data_t *k1c, data_t *k2c, data_t *k1n, data_t *k2n, int nsteps) {
+/* n calls of vvsl_field_rescaled (s_integrate.cpp:305), or with form = 1 of
+ * vvsl_hamiltonian_form (s_integrate.cpp:358), on caller arrays. */
+static void ref_steps_form(data_t *phi1, data_t *phi2, data_t *pd1, data_t *pd2,
+                           data_t *k1c, data_t *k2c, data_t *k1n, data_t *k2n, int nsteps, int form) {
     if (!g_have_matrix || g_matrix_dims != parameters.NDIMS || g_matrix_n != parameters.N ||
         g_matrix_stencil != parameters.stencil_setting) {
         if (g_have_matrix) mkl_sparse_destroy(g_data.coefficient_matrix);
@@ -67,7 +68,20 @@ void ref_steps(data_t *phi1, data_t *phi2, data_t *pd1, data_t *pd2,
     g_data.phi1 = phi1; g_data.phi2 = phi2; g_data.phidot1 = pd1; g_data.phidot2 = pd2;
     g_data.ker1_curr = k1c; g_data.ker2_curr = k2c; g_data.ker1_next = k1n; g_data.ker2_next = k2n;
     g_data.axion = 0; g_data.saxion = 0;
-    for (int s = 0; s < nsteps; ++s) vvsl_field_rescaled(g_data);
+    for (int s = 0; s < nsteps; ++s) {
+        if (form == 1) vvsl_hamiltonian_form(g_data);
+        else vvsl_field_rescaled(g_data);
+    }
+}
+
+void ref_steps(data_t *phi1, data_t *phi2, data_t *pd1, data_t *pd2,
+               data_t *k1c, data_t *k2c, data_t *k1n, data_t *k2n, int nsteps) {
+    ref_steps_form(phi1, phi2, pd1, pd2, k1c, k2c, k1n, k2n, nsteps, 0);
+}
+
+void ref_steps_hamiltonian(data_t *phi1, data_t *phi2, data_t *pd1, data_t *pd2,
+                           data_t *k1c, data_t *k2c, data_t *k1n, data_t *k2n, int nsteps) {
+    ref_steps_form(phi1, phi2, pd1, pd2, k1c, k2c, k1n, k2n, nsteps, 1);
 }
 
 /* cores2/cores3 (string_finding.cpp:3-86) on a caller theta array. Writes up

@@ -44,6 +44,7 @@ class Oracle:
             "orc_laplacian": ([P, _vp, _vp], None),
             "orc_vvsl_step": ([P, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _dp], None),
             "orc_vvsl_step_f32": ([P, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_float)], None),
+            "orc_vvsl_hamiltonian_step": ([P, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _dp], None),
             "orc_cores": ([P, _vp, _vp], ctypes.c_int64),
             "orc_num_cores2": ([ctypes.c_int, _vp], ctypes.c_int64),
             "orc_xi": ([P, ctypes.c_int64, ctypes.c_int64, ctypes.c_double], ctypes.c_float),
@@ -78,13 +79,15 @@ class Oracle:
         self.lib.orc_laplacian(ctypes.byref(p), _ptr(phi), _ptr(out))
         return out
 
-    def evolve(self, p, phi1, phi2, pi1, pi2, nsteps, tau=1.0, ker=None):
-        """Reference-structured velocity-Verlet steps; returns the new state."""
+    def evolve(self, p, phi1, phi2, pi1, pi2, nsteps, tau=1.0, ker=None, form=0):
+        """Reference-structured velocity-Verlet steps (form 0: vvsl_field_rescaled,
+        form 1: vvsl_hamiltonian_form); returns the new state."""
         f = [np.array(a, dtype=np.float64, copy=True, order="C") for a in (phi1, phi2, pi1, pi2)]
         k = [np.zeros_like(f[0]) for _ in range(4)] if ker is None else [np.array(a, copy=True) for a in ker] + [np.zeros_like(f[0]), np.zeros_like(f[0])]
         t = ctypes.c_double(tau)
+        step = self.lib.orc_vvsl_hamiltonian_step if form == 1 else self.lib.orc_vvsl_step
         for _ in range(nsteps):
-            self.lib.orc_vvsl_step(ctypes.byref(p), *[_ptr(a) for a in f], _ptr(k[0]), _ptr(k[1]), _ptr(k[2]), _ptr(k[3]), ctypes.byref(t))
+            step(ctypes.byref(p), *[_ptr(a) for a in f], _ptr(k[0]), _ptr(k[1]), _ptr(k[2]), _ptr(k[3]), ctypes.byref(t))
         return f[0], f[1], f[2], f[3], t.value
 
     def evolve_f32(self, p, phi1, phi2, pi1, pi2, nsteps, tau=1.0):
@@ -175,6 +178,7 @@ class RefLib:
         L.ref_set_tau.argtypes = [ctypes.c_double]
         L.ref_gaussian_thermal.argtypes = [_vp] * 4
         L.ref_steps.argtypes = [_vp] * 8 + [ctypes.c_int]
+        L.ref_steps_hamiltonian.argtypes = [_vp] * 8 + [ctypes.c_int]
         L.ref_cores.argtypes = [_vp, _vp, ctypes.c_int]
         L.ref_cores.restype = ctypes.c_int
         L.ref_powerspec.argtypes = [_vp, _vp, _vp, _vp]
@@ -192,11 +196,12 @@ class RefLib:
         self.lib.ref_gaussian_thermal(*[_ptr(a) for a in out])
         return tuple(out)
 
-    def evolve(self, p, phi1, phi2, pi1, pi2, nsteps):
+    def evolve(self, p, phi1, phi2, pi1, pi2, nsteps, form=0):
         self.set_params(p)
         f = [np.array(a, dtype=self.dtype, copy=True, order="C") for a in (phi1, phi2, pi1, pi2)]
         k = [np.zeros_like(f[0]) for _ in range(4)]
-        self.lib.ref_steps(*[_ptr(a) for a in f + k], int(nsteps))
+        step = self.lib.ref_steps_hamiltonian if form == 1 else self.lib.ref_steps
+        step(*[_ptr(a) for a in f + k], int(nsteps))
         return f[0], f[1], f[2], f[3], self.lib.ref_get_tau()
 
     def cores(self, p, theta):

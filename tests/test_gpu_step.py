@@ -186,3 +186,52 @@ def test_literal_equation_stays_finite_short(axs, oracle):
     o = oracle.evolve(op, *f, 10)
     for q in range(4):
         assert rel(g[q], o[q]) <= 1e-12
+
+
+@pytest.mark.parametrize("nd,N,stencil", [(2, 64, 0), (2, 48, 1), (3, 32, 0), (3, 24, 2), (3, 40, 0)])
+def test_hamiltonian_form_matches_oracle(axs, oracle, nd, N, stencil):
+    """form = 1: vvsl_hamiltonian_form (s_integrate.cpp:358-395), FP64 within
+    1e-12 of the oracle (itself pinned to the reference's compiled function)."""
+    p = params(axs, nd, N, 64, stencil_setting=stencil, form=1)
+    op = orc(p)
+    f = oracle.init_thermal(op, 13)
+    with axs.Lattice(p) as L:
+        L.upload(*f)
+        L.evolve(10)
+        g = L.download()
+        tau, steps = L.time
+    o = oracle.evolve(op, *f, 10, form=1)
+    for q in range(4):
+        assert rel(g[q], o[q]) <= 1e-12, (q, rel(g[q], o[q]))
+    assert tau == o[4] and steps == 10
+
+
+@pytest.mark.parametrize("N", [64, 160])
+def test_hamiltonian_form_kernels_bit_identical(axs, N):
+    """The generic, one-step and two-step kernels give the same bits in form 1."""
+    p = params(axs, 3, N, 32, form=1)
+    outs = []
+    for force in ["0,0,64", "1,6,64", "1,10,128", "1,17,32"]:
+        os.environ["AXS_FORCE_CONFIG"] = force
+        try:
+            with axs.Lattice(p) as L:
+                L.init_thermal(4)
+                for n in (1, 4, 3):
+                    L.evolve(n)
+                outs.append((L.describe(), L.download(dtype=np.float32)))
+        finally:
+            del os.environ["AXS_FORCE_CONFIG"]
+    d0, g0 = outs[0]
+    for d, g in outs[1:]:
+        for q in range(4):
+            assert np.array_equal(g[q], g0[q]), (d0, d, q)
+
+
+def test_hamiltonian_form_rejects_rescaled_analyses(axs):
+    p = params(axs, 3, 32, 64, form=1)
+    with axs.Lattice(p) as L:
+        L.init_thermal(1)
+        with pytest.raises(axs.AxsError):
+            L.energies()
+        with pytest.raises(axs.AxsError):
+            L.axion_spectrum(16)

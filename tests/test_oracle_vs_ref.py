@@ -25,6 +25,19 @@ def test_step(oracle, nd, N, stencil):
     assert a[4] == b[4]
 
 
+@pytest.mark.parametrize("nd,N,stencil", [(2, 64, 0), (2, 48, 2), (3, 24, 0), (3, 24, 1)])
+def test_hamiltonian_step(oracle, nd, N, stencil):
+    """vvsl_hamiltonian_form (s_integrate.cpp:358-395) against the oracle."""
+    rng = np.random.default_rng(nd * 1000 + stencil + 7)
+    p = oracle_lib.make_params(NDIMS=nd, N=N, T0=4.0, stencil=stencil)
+    f = [rng.standard_normal((N,) * nd) for _ in range(4)]
+    a = oracle.evolve(p, *f, 10, form=1)
+    b = REF.evolve(p, *f, 10, form=1)
+    for q in range(4):
+        assert np.abs(a[q] - b[q]).max() / np.abs(b[q]).max() <= 1e-13
+    assert a[4] == b[4]
+
+
 @pytest.mark.parametrize("nd,N,thr", [(2, 96, 1), (3, 20, 1), (3, 20, 50)])
 def test_cores(oracle, nd, N, thr):
     rng = np.random.default_rng(N + thr)
