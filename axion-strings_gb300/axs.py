@@ -43,6 +43,7 @@ class Params(ctypes.Structure):
         ("prs", ctypes.c_int),
         ("tau_initial", ctypes.c_double),
         ("form", ctypes.c_int),
+        ("laplacian", ctypes.c_int),
     ]
 
     def as_dict(self):

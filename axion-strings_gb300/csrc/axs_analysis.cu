@@ -918,7 +918,7 @@ void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *c
     if (nbins < 1) fail(AXS_ERR_ARG, "nbins must be >= 1");
     if (L->p.form != 0) fail(AXS_ERR_STATE, "the axion kinetic spectrum is defined on the field-rescaled variables (form 0)");
     ensure_fft(L);
-    if (L->p.NDIMS == 3 && L->p.stencil_setting == 0) {
+    if (L->p.NDIMS == 3 && L->p.stencil_setting == 0 && L->p.laplacian == 0) {
         const axs_params &p = L->p;
         const int N = p.N;
         const double dx = p.space_step, T0 = p.T_initial;

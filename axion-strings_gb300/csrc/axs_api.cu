@@ -85,6 +85,7 @@ static void validate(const axs_params &p) {
     if (!std::isfinite(p.time_step)) fail(AXS_ERR_ARG, "time_step must be finite");
     if (p.N > 4096) fail(AXS_ERR_ARG, "N=%d exceeds the supported maximum 4096", p.N);
     if (p.form != 0 && p.form != 1) fail(AXS_ERR_ARG, "form must be 0 (field-rescaled) or 1 (Hamiltonian)");
+    if (p.laplacian != 0 && p.laplacian != 1) fail(AXS_ERR_ARG, "laplacian must be 0 (stencil) or 1 (spectral)");
 }
 
 static void set_device_clock(Lattice *L) {
@@ -358,6 +359,7 @@ void axs_default_params(axs_params *p) {
     p->prs = 1;
     p->tau_initial = 1.0;      // physics.cpp:50
     p->form = 0;               // vvsl_field_rescaled, the integrator s_run.cpp calls
+    p->laplacian = 0;          // the sparse-matrix stencil branch, s_integrate.cpp:321-325
 }
 
 int axs_last_error(char *buf, size_t len) {
@@ -655,8 +657,9 @@ int axs_ensemble_create(const axs_params *members, int n, axs_ensemble **out) {
     for (int i = 1; i < n; ++i) {
         const axs_params &a = members[0], &b = members[i];
         if (a.NDIMS != b.NDIMS || a.precision != b.precision || a.time_step != b.time_step ||
-            a.space_step != b.space_step || a.stencil_setting != b.stencil_setting || a.form != b.form)
-            fail(AXS_ERR_ARG, "ensemble members must share NDIMS, precision, dt, dx, stencil and form");
+            a.space_step != b.space_step || a.stencil_setting != b.stencil_setting || a.form != b.form ||
+            a.laplacian != b.laplacian)
+            fail(AXS_ERR_ARG, "ensemble members must share NDIMS, precision, dt, dx, stencil, form and Laplacian");
     }
     axs_ensemble *e = new axs_ensemble();
     try {

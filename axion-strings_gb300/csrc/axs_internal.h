@@ -141,6 +141,11 @@ struct Lattice {
     int64_t sqrt_len = 0;
     size_t partials_cap = 0;
     void *dstage = nullptr;          // transfer staging (length reals)
+    // spectral Laplacian (axs_params.laplacian = 1): complex transform plan and
+    // the per-axis k^2 table (N doubles, then N floats)
+    cufftHandle plan_c2c = 0;
+    bool have_c2c = false;
+    void *dksq = nullptr;
     std::map<GraphKey, GraphEntry> graphs;
 };
 

@@ -136,6 +136,100 @@ __global__ void k_sync_pi(const typename Cplx<T>::type *__restrict__ psi, const 
     }
 }
 
+// ---- spectral Laplacian (compute_laplacian_fft, s_integrate.cpp:179-296)
+//
+// L phi = IFFT(-k^2 FFT(phi)) / N^d. psi is complex-interleaved (re = phi1,
+// im = phi2) and -k^2 is real and even in k, so one complex transform pair
+// gives both fields' Laplacians (re and im of the result). The reference's
+// (-1)^(i+j+k) factors before and after its transforms only relabel the
+// frequencies: in the unshifted layout index j holds frequency j (j < N/2) or
+// j - N, whose k is the reference's k of shifted index j + N/2 (mod N).
+// ksq[j] is that k^2 (host-computed as the reference computes k, in double;
+// N doubles then the same N rounded to float).
+
+// W *= -(k_z^2 + k_y^2 + k_x^2) (slowest axis first, as coordinate3 orders it;
+// 2D: k_x^2 + k_y^2 with x fastest, as coordinate2).
+template <typename T>
+__global__ void k_kspace_laplacian(typename Cplx<T>::type *__restrict__ W, const void *__restrict__ ksq_tab, int N,
+                                   int ndims, int64_t len) {
+    const double *kd = reinterpret_cast<const double *>(ksq_tab);
+    const float *kf = reinterpret_cast<const float *>(kd + N);
+    const int64_t NN = (int64_t)N * N;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        int a, b, c = -1;   // slowest .. fastest
+        if (ndims == 2) { a = (int)(m % N); b = (int)(m / N); }
+        else { a = (int)(m / NN); b = (int)((m / N) % N); c = (int)(m % N); }
+        auto w = W[m];
+        if (sizeof(T) == 8) {
+            double s = kd[a] + kd[b];
+            if (c >= 0) s = s + kd[c];
+            w.x = (T)((double)w.x * -s);
+            w.y = (T)((double)w.y * -s);
+        } else {
+            float s = kf[a] + kf[b];
+            if (c >= 0) s = s + kf[c];
+            w.x = (T)((float)w.x * -s);
+            w.y = (T)((float)w.y * -s);
+        }
+        W[m] = w;
+    }
+}
+
+// One step with the spectral Laplacian: W holds N^d L psi (both components).
+template <typename T>
+__global__ void __launch_bounds__(256) k_step_spectral(const typename Cplx<T>::type *__restrict__ psi,
+                                                       typename Cplx<T>::type *__restrict__ out,
+                                                       typename Cplx<T>::type *__restrict__ pih,
+                                                       const typename Cplx<T>::type *__restrict__ W,
+                                                       const double *clock_in, double *clock_out, int64_t len,
+                                                       double dt, double lambda, double T0sq3, int prs, int form) {
+    const double tau = *clock_in;
+    const StepCoefs<T> c = make_coefs<T>(tau, dt, dt, 1.0, lambda, T0sq3, prs, form);   // k already physical
+    const T ilen = (T)len;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        const auto a = psi[m];
+        const auto w = W[m];
+        auto p = pih[m];
+        typename Cplx<T>::type o;
+        site_update<T>(a.x, a.y, w.x / ilen, w.y / ilen, p.x, p.y, o.x, o.y, c);   // ret = data / length, :228-231
+        pih[m] = p;
+        out[m] = o;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *clock_out = tau + dt;
+}
+
+// pi_n = pih + dt/2 K(psi_n) with the spectral Laplacian in W; written over W.
+template <typename T>
+__global__ void k_sync_pi_spectral(const typename Cplx<T>::type *__restrict__ psi,
+                                   const typename Cplx<T>::type *__restrict__ pih, typename Cplx<T>::type *W,
+                                   const double *clock, int64_t len, double dt, double lambda, double T0sq3, int prs,
+                                   int form) {
+    const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, 1.0, lambda, T0sq3, prs, form);
+    const T ilen = (T)len;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        const auto a = psi[m];
+        const auto w = W[m];
+        auto p = pih[m];
+        sync_pi_site<T>(a.x, a.y, w.x / ilen, w.y / ilen, p.x, p.y, c);
+        W[m] = p;
+    }
+}
+
+// One component of the spectral Laplacian in W into a double array.
+template <typename T>
+__global__ void k_laplacian_spectral(const typename Cplx<T>::type *__restrict__ W, double *__restrict__ out, int comp,
+                                     int64_t len) {
+    const T ilen = (T)len;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        const auto w = W[m];
+        out[m] = (double)((comp ? w.y : w.x) / ilen);
+    }
+}
+
 // (1/dx^2) * stencil of one component, in double.
 template <typename T, int ND, int R>
 __global__ void k_laplacian(const typename Cplx<T>::type *__restrict__ psi, double *__restrict__ out, int comp, int N,
@@ -1378,7 +1472,7 @@ static int variant_tx(const ZVariant &v, int N, int esz) {
 }
 
 bool zmarch_supported(const axs_params &p) {
-    if (p.NDIMS != 3 || p.stencil_setting != 0) return false;
+    if (p.NDIMS != 3 || p.stencil_setting != 0 || p.laplacian != 0) return false;
     int esz = p.precision == AXS_F32 ? 4 : 8;
     for (int v = 0; v < kNumZVariants; ++v)
         if (variant_tx(kZVariants[v], p.N, esz)) return true;
@@ -1509,7 +1603,10 @@ void clear_graphs(std::map<GraphKey, GraphEntry> &g) {
     g.clear();
 }
 
+static void spectral_release(Lattice *L);
+
 void step_release(Lattice *L) {
+    spectral_release(L);
     clear_graphs(L->graphs);
     dfree(L->dzlat);
     L->dzlat = nullptr;
@@ -1550,6 +1647,72 @@ static void launch_generic_dispatch(Lattice *L, const double *cin, double *cout)
     }
 }
 
+// ---------------------------------------------------------------- spectral Laplacian
+// scratch <- N^d L psi (both components): forward transform of the current psi
+// into scratch, times -k^2, backward transform in place. The caller divides by
+// N^d (as compute_laplacian_fft does after its backward transform).
+static void spectral_laplacian(Lattice *L) {
+    const int N = L->p.N;
+    if (!L->have_c2c) {
+        if (t_capturing) fail(AXS_ERR_STATE, "internal: transform plan created inside a graph capture");
+        cufftType ty = L->esz == 4 ? CUFFT_C2C : CUFFT_Z2Z;
+        if (L->p.NDIMS == 2) AXS_CUFFT(cufftPlan2d(&L->plan_c2c, N, N, ty));
+        else AXS_CUFFT(cufftPlan3d(&L->plan_c2c, N, N, N, ty));
+        AXS_CUFFT(cufftSetStream(L->plan_c2c, L->stream));
+        // k of the reference (s_integrate.cpp:183, :193/:241): (-N/2.0f + i) * 2.0f * M_PI / L,
+        // for the frequency of unshifted index j
+        std::vector<unsigned char> tab((size_t)N * (sizeof(double) + sizeof(float)));
+        double *kd = reinterpret_cast<double *>(tab.data());
+        float *kf = reinterpret_cast<float *>(kd + N);
+        const float Lf = N * L->p.space_step;
+        for (int j = 0; j < N; ++j) {
+            const int i = (j + N / 2) % N;   // shifted index of the same frequency
+            const double k = (-N / 2.0f + i) * 2.0f * 3.14159265358979323846 / Lf;
+            kd[j] = k * k;
+            kf[j] = (float)kd[j];
+        }
+        L->dksq = dalloc(tab.size());
+        AXS_CUDA(cudaMemcpyAsync(L->dksq, tab.data(), tab.size(), cudaMemcpyHostToDevice, L->stream));
+        AXS_CUDA(cudaStreamSynchronize(L->stream));
+        L->have_c2c = true;
+    }
+    const int g = grid_for(L->length);
+    if (L->esz == 4) {
+        AXS_CUFFT(cufftExecC2C(L->plan_c2c, (cufftComplex *)L->psi[L->cur], (cufftComplex *)L->scratch, CUFFT_FORWARD));
+        k_kspace_laplacian<float><<<g, 256, 0, L->stream>>>((float2 *)L->scratch, L->dksq, N, L->p.NDIMS, L->length);
+        AXS_CUDA(cudaGetLastError());
+        AXS_CUFFT(cufftExecC2C(L->plan_c2c, (cufftComplex *)L->scratch, (cufftComplex *)L->scratch, CUFFT_INVERSE));
+    } else {
+        AXS_CUFFT(cufftExecZ2Z(L->plan_c2c, (cufftDoubleComplex *)L->psi[L->cur], (cufftDoubleComplex *)L->scratch,
+                               CUFFT_FORWARD));
+        k_kspace_laplacian<double><<<g, 256, 0, L->stream>>>((double2 *)L->scratch, L->dksq, N, L->p.NDIMS, L->length);
+        AXS_CUDA(cudaGetLastError());
+        AXS_CUFFT(cufftExecZ2Z(L->plan_c2c, (cufftDoubleComplex *)L->scratch, (cufftDoubleComplex *)L->scratch,
+                               CUFFT_INVERSE));
+    }
+    count_launches(1);
+}
+
+template <typename T>
+static void spectral_step_t(Lattice *L) {
+    typedef typename Cplx<T>::type C;
+    spectral_laplacian(L);
+    const double T0 = L->p.T_initial;
+    k_step_spectral<T><<<grid_for(L->length), 256, 0, L->stream>>>(
+        (const C *)L->psi[L->cur], (C *)L->psi[L->cur ^ 1], (C *)L->pih, (const C *)L->scratch, L->dclock + L->cur,
+        L->dclock + (L->cur ^ 1), L->length, (double)L->p.time_step, (double)L->p.lambda, (T0 * T0) / 3.0, L->p.prs,
+        L->p.form);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+
+static void spectral_release(Lattice *L) {
+    if (L->have_c2c) cufftDestroy(L->plan_c2c);
+    L->have_c2c = false;
+    dfree(L->dksq);
+    L->dksq = nullptr;
+}
+
 // Advances a lattice by one launch of at most max_steps (>= 1) steps and
 // returns the steps taken: two for a two-step variant when allowed, else one.
 // The handle's bookkeeping advances here; the kernels may run later inside a
@@ -1586,6 +1749,9 @@ int lattice_advance(Lattice *L, int max_steps) {
             L->debug_tx_excess = 0;
             L->zlat_variant = -1;
         }
+    } else if (L->p.laplacian == 1) {
+        if (L->esz == 4) spectral_step_t<float>(L);
+        else spectral_step_t<double>(L);
     } else {
         if (L->esz == 4) launch_generic_dispatch<float>(L, cin, cout);
         else launch_generic_dispatch<double>(L, cin, cout);
@@ -1660,7 +1826,7 @@ void lattice_evolve(Lattice *L, int nsteps) {
         if (--nsteps == 0) return;
     }
     prepare_tables(L);
-    if (nsteps < 2 || !env_flag("AXS_GRAPHS", true)) {
+    if (nsteps < 2 || !env_flag("AXS_GRAPHS", true) || L->p.laplacian == 1) {   // spectral: transforms run eagerly
         while (nsteps > 0) nsteps -= lattice_advance(L, nsteps);
         return;
     }
@@ -2004,7 +2170,7 @@ void ensemble_evolve(Ensemble *E, int nsteps) {
     if (E->cfg.kind == 1 && !ensemble_table_valid(E)) ensemble_table(E, 0.f, false);
     if (E->cfg.kind != 1)
         for (Lattice *m : E->members) prepare_tables(m);
-    if (nsteps < 2 || !env_flag("AXS_GRAPHS", true)) {
+    if (nsteps < 2 || !env_flag("AXS_GRAPHS", true) || E->members[0]->p.laplacian == 1) {
         while (nsteps > 0) nsteps -= ensemble_advance(E, nsteps);
         return;
     }
@@ -2078,6 +2244,22 @@ void launch_sync_pi(Lattice *L) {
         AXS_CUDA(cudaMemcpyAsync(L->scratch, L->pih, (size_t)L->length * 2 * L->esz, cudaMemcpyDeviceToDevice, L->stream));
         return;
     }
+    if (L->p.laplacian == 1) {
+        spectral_laplacian(L);
+        const double T0 = L->p.T_initial;
+        const int g = grid_for(L->length);
+        if (L->esz == 4)
+            k_sync_pi_spectral<float><<<g, 256, 0, L->stream>>>(
+                (const float2 *)L->psi[L->cur], (const float2 *)L->pih, (float2 *)L->scratch, L->dclock + L->cur,
+                L->length, (double)L->p.time_step, (double)L->p.lambda, (T0 * T0) / 3.0, L->p.prs, L->p.form);
+        else
+            k_sync_pi_spectral<double><<<g, 256, 0, L->stream>>>(
+                (const double2 *)L->psi[L->cur], (const double2 *)L->pih, (double2 *)L->scratch, L->dclock + L->cur,
+                L->length, (double)L->p.time_step, (double)L->p.lambda, (T0 * T0) / 3.0, L->p.prs, L->p.form);
+        AXS_CUDA(cudaGetLastError());
+        count_launches(1);
+        return;
+    }
     if (L->esz == 4) sync_pi_dispatch<float>(L);
     else sync_pi_dispatch<double>(L);
 }
@@ -2101,6 +2283,15 @@ static void lap_dispatch(Lattice *L, int comp, double *dout) {
     }
 }
 void launch_laplacian(Lattice *L, int comp, double *dout) {
+    if (L->p.laplacian == 1) {   // the spectral Laplacian itself (already in physical units)
+        spectral_laplacian(L);
+        const int g = grid_for(L->length);
+        if (L->esz == 4) k_laplacian_spectral<float><<<g, 256, 0, L->stream>>>((const float2 *)L->scratch, dout, comp, L->length);
+        else k_laplacian_spectral<double><<<g, 256, 0, L->stream>>>((const double2 *)L->scratch, dout, comp, L->length);
+        AXS_CUDA(cudaGetLastError());
+        count_launches(1);
+        return;
+    }
     if (L->esz == 4) lap_dispatch<float>(L, comp, dout);
     else lap_dispatch<double>(L, comp, dout);
 }

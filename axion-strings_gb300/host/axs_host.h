@@ -48,6 +48,7 @@ struct RunConfig {
     int gpu_precision = 64;        // 32 or 64
     int gpu_prs = 1;               // potential coefficient lambda / tau^(2 prs); 1 = reference
     int gpu_form = 0;              // 0 = vvsl_field_rescaled (reference), 1 = vvsl_hamiltonian_form
+    int gpu_laplacian = 0;         // 0 = stencil (reference default), 1 = compute_laplacian_fft
     int init_mode = 0;             // 0 = gaussian_thermal (reference), 1 = flat k_cut
     float k_cut = 1.0f;            // flat init cut-off (physical k)
     int string_interval = 0;       // > 0: also find strings every this many steps

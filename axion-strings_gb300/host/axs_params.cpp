@@ -54,6 +54,7 @@ int read_parameter_file(const char *fname, RunConfig &c, std::string &err) {
         {"gpu_precision", INT, &c.gpu_precision, false, false},
         {"gpu_prs", INT, &c.gpu_prs, false, false},
         {"gpu_form", INT, &c.gpu_form, false, false},
+        {"gpu_laplacian", INT, &c.gpu_laplacian, false, false},
         {"init_mode", INT, &c.init_mode, false, false},
         {"k_cut", FLOAT, &c.k_cut, false, false},
         {"string_interval", INT, &c.string_interval, false, false},
@@ -119,6 +120,7 @@ axs_params to_params(const RunConfig &c) {
     p.precision = c.gpu_precision;
     p.prs = c.gpu_prs;
     p.form = c.gpu_form;
+    p.laplacian = c.gpu_laplacian;
     p.tau_initial = 1.0;   // set_physics_variables (src/common/physics.cpp:50)
     return p;
 }

@@ -76,13 +76,17 @@ typedef struct axs_params {
                                       (vvsl_field_rescaled, s_integrate.cpp:305-348),
                                       1 = Hamiltonian-like form in phi and pi = tau^2 phi'
                                       (vvsl_hamiltonian_form, s_integrate.cpp:358-395) */
+    int          laplacian;        /* 0 = finite-difference stencil (stencil_setting,
+                                      build_coefficient_matrix, s_integrate.cpp:5-149),
+                                      1 = spectral (compute_laplacian_fft, s_integrate.cpp:179-296,
+                                      the reference's compile-time alternative at :327-329) */
 } axs_params;
 
 typedef struct axs_lattice axs_lattice;     /* one lattice on the GPU            */
 typedef struct axs_ensemble axs_ensemble;   /* independent lattices, batched     */
 
 /* Fill p with the values of the reference's default.param plus
- * precision = AXS_F64, prs = 1, tau_initial = 1, form = 0. */
+ * precision = AXS_F64, prs = 1, tau_initial = 1, form = 0, laplacian = 0. */
 void axs_default_params(axs_params *p);
 
 /* Copy the message of the last failure on this thread into buf. */

@@ -65,7 +65,48 @@ static double stencil_row(const double *phi, long m, int ndims, long N, const do
     return acc;
 }
 
+void orc_laplacian_spectral(const orc_params *p, const double *field, double *ret) {
+    int N = p->N, nd = p->NDIMS;
+    long len = lattice_length(p);
+    float L = N * p->space_step;                                   /* s_integrate.cpp:183 */
+    double *k = (double *)malloc(sizeof(double) * N);
+    double *data = (double *)malloc(sizeof(double) * 2 * len);
+    for (int i = 0; i < N; ++i) k[i] = (-N / 2.0f + i) * 2.0f * M_PI / L;   /* :193 / :241 */
+    for (long m = 0; m < len; ++m) {                               /* :205-208, shift :210 */
+        long s = nd == 2 ? (m % N) + (m / N) : (m / ((long)N * N)) + ((m / N) % N) + (m % N);
+        double sg = (s & 1) ? -1.0 : 1.0;
+        data[2 * m] = field[m] * sg;
+        data[2 * m + 1] = 0.0 * sg;
+    }
+    int dims[3] = {N, N, N};
+    orc_fft_nd(data, nd, dims, -1);                                /* FFTW_FORWARD */
+    for (long m = 0; m < len; ++m) {                               /* :214-220 / :262-268 */
+        double ksq;
+        if (nd == 2) {
+            long i = m % N, j = m / N;                             /* coordinate2 */
+            ksq = k[i] * k[i] + k[j] * k[j];
+        } else {
+            long i = m / ((long)N * N), j = (m / N) % N, kk = m % N;   /* coordinate3 */
+            ksq = k[i] * k[i] + k[j] * k[j] + k[kk] * k[kk];
+        }
+        data[2 * m] *= -ksq;
+        data[2 * m + 1] *= -ksq;
+    }
+    orc_fft_nd(data, nd, dims, +1);                                /* FFTW_BACKWARD */
+    for (long m = 0; m < len; ++m) {                               /* shift :226, / length :228-231 */
+        long s = nd == 2 ? (m % N) + (m / N) : (m / ((long)N * N)) + ((m / N) % N) + (m % N);
+        double v = (s & 1) ? -data[2 * m] : data[2 * m];
+        ret[m] = v / len;
+    }
+    free(data);
+    free(k);
+}
+
 void orc_laplacian(const orc_params *p, const double *phi, double *out) {
+    if (p->laplacian == 1) {
+        orc_laplacian_spectral(p, phi, out);
+        return;
+    }
     double c[5];
     int nc = stencil_coefficients(p->stencil_setting, p->NDIMS, c);
     long len = lattice_length(p), N = p->N;
@@ -132,16 +173,26 @@ void orc_vvsl_hamiltonian_step(const orc_params *p, double *phi1, double *phi2, 
         phi1[i] += ddt / tsq * (pi1[i] + 0.5f * ddt * ker1[i]);
         phi2[i] += ddt / tsq * (pi2[i] + 0.5f * ddt * ker2[i]);
     }
-    /* (tau^2/dx^2) A phi, s_integrate.cpp:374-376 */
-    double c[5];
-    int nc = stencil_coefficients(p->stencil_setting, p->NDIMS, c);
-    double dx = (double)p->space_step;
-    double alpha = tsq / (dx * dx);
-    long N = p->N;
-    #pragma omp parallel for schedule(static)
-    for (long m = 0; m < len; ++m) {
-        ker1n[m] = alpha * stencil_row(phi1, m, p->NDIMS, N, c, nc);
-        ker2n[m] = alpha * stencil_row(phi2, m, p->NDIMS, N, c, nc);
+    /* (tau^2/dx^2) A phi, s_integrate.cpp:374-376; with the spectral
+       Laplacian (no counterpart in the reference's Hamiltonian form) tau^2 L phi */
+    if (p->laplacian == 1) {
+        orc_laplacian_spectral(p, phi1, ker1n);
+        orc_laplacian_spectral(p, phi2, ker2n);
+        for (long m = 0; m < len; ++m) {
+            ker1n[m] *= tsq;
+            ker2n[m] *= tsq;
+        }
+    } else {
+        double c[5];
+        int nc = stencil_coefficients(p->stencil_setting, p->NDIMS, c);
+        double dx = (double)p->space_step;
+        double alpha = tsq / (dx * dx);
+        long N = p->N;
+        #pragma omp parallel for schedule(static)
+        for (long m = 0; m < len; ++m) {
+            ker1n[m] = alpha * stencil_row(phi1, m, p->NDIMS, N, c, nc);
+            ker2n[m] = alpha * stencil_row(phi2, m, p->NDIMS, N, c, nc);
+        }
     }
     double T0 = p->T_initial;
     double shift = (T0 * T0) / (3.0f * tsq);

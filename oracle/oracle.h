@@ -39,6 +39,7 @@ typedef struct orc_params {
     int   stencil_setting;
     int   thr;
     int   prs;
+    int   laplacian;   /* 0: finite-difference stencil; 1: compute_laplacian_fft (s_integrate.cpp:179-296) */
 } orc_params;
 
 /* Unnormalised in-place complex FFT of a row-major array (interleaved re/im);
@@ -50,8 +51,13 @@ void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
 /* (1/dx^2) * A * phi, A the periodic finite-difference matrix of
  * build_coefficient_matrix (src/standard/s_integrate.cpp:5-149) applied as in
- * vvsl_field_rescaled (s_integrate.cpp:322). */
+ * vvsl_field_rescaled (s_integrate.cpp:322); with p->laplacian = 1 the
+ * spectral Laplacian below instead (the reference's `#else` branch, :327-329). */
 void orc_laplacian(const orc_params *p, const double *phi, double *out);
+/* compute_laplacian_fft (s_integrate.cpp:179-296): checkerboard shift, forward
+ * FFT, times -k^2 with k = (-N/2 + i) 2 pi / L evaluated as there, backward
+ * FFT, shift, / N^NDIMS. */
+void orc_laplacian_spectral(const orc_params *p, const double *field, double *ret);
 
 /* One velocity-Verlet step, vvsl_field_rescaled (s_integrate.cpp:305-348). */
 void orc_vvsl_step(const orc_params *p, double *phi1, double *phi2, double *pi1, double *pi2,

@@ -27,7 +27,12 @@ static all_data g_data;
 static bool g_have_matrix = false;
 static int g_matrix_dims = 0, g_matrix_n = 0, g_matrix_stencil = -1;
 
+void compute_laplacian_fft(data_t *ret, data_t *field);   // s_integrate.cpp:179 (no header declares it)
+
 extern "C" {
+
+/* compute_laplacian_fft on a caller array (parameters set by ref_set_params). */
+void ref_laplacian_fft(data_t *ret, data_t *field) { compute_laplacian_fft(ret, field); }
 
 int ref_sizeof_data_t(void) { return (int)sizeof(data_t); }
 

@@ -18,16 +18,18 @@ _dp = ctypes.POINTER(ctypes.c_double)
 class OrcParams(ctypes.Structure):
     _fields_ = [("NDIMS", ctypes.c_int), ("N", ctypes.c_int), ("lambda_", ctypes.c_float),
                 ("T_initial", ctypes.c_float), ("space_step", ctypes.c_float), ("time_step", ctypes.c_float),
-                ("stencil_setting", ctypes.c_int), ("thr", ctypes.c_int), ("prs", ctypes.c_int)]
+                ("stencil_setting", ctypes.c_int), ("thr", ctypes.c_int), ("prs", ctypes.c_int),
+                ("laplacian", ctypes.c_int)]
 
 
-def make_params(NDIMS=3, N=32, lam=1.0, T0=0.0, dx=0.5, dt=0.1, stencil=0, thr=1, prs=1):
-    return OrcParams(NDIMS, N, lam, T0, dx, dt, stencil, thr, prs)
+def make_params(NDIMS=3, N=32, lam=1.0, T0=0.0, dx=0.5, dt=0.1, stencil=0, thr=1, prs=1, laplacian=0):
+    return OrcParams(NDIMS, N, lam, T0, dx, dt, stencil, thr, prs, laplacian)
 
 
 def from_axs(p):
     """OrcParams from an axs.Params."""
-    return OrcParams(p.NDIMS, p.N, p.lambda_, p.T_initial, p.space_step, p.time_step, p.stencil_setting, p.thr, p.prs)
+    return OrcParams(p.NDIMS, p.N, p.lambda_, p.T_initial, p.space_step, p.time_step, p.stencil_setting, p.thr, p.prs,
+                     getattr(p, "laplacian", 0))
 
 
 def _ptr(a):
@@ -179,6 +181,7 @@ class RefLib:
         L.ref_gaussian_thermal.argtypes = [_vp] * 4
         L.ref_steps.argtypes = [_vp] * 8 + [ctypes.c_int]
         L.ref_steps_hamiltonian.argtypes = [_vp] * 8 + [ctypes.c_int]
+        L.ref_laplacian_fft.argtypes = [_vp, _vp]
         L.ref_cores.argtypes = [_vp, _vp, ctypes.c_int]
         L.ref_cores.restype = ctypes.c_int
         L.ref_powerspec.argtypes = [_vp, _vp, _vp, _vp]
@@ -195,6 +198,13 @@ class RefLib:
         out = [np.zeros(self.shape(p), dtype=self.dtype) for _ in range(4)]
         self.lib.ref_gaussian_thermal(*[_ptr(a) for a in out])
         return tuple(out)
+
+    def laplacian_fft(self, p, field):
+        self.set_params(p)
+        f = np.ascontiguousarray(field, dtype=self.dtype).copy()
+        out = np.zeros_like(f)
+        self.lib.ref_laplacian_fft(_ptr(out), _ptr(f))
+        return out
 
     def evolve(self, p, phi1, phi2, pi1, pi2, nsteps, form=0):
         self.set_params(p)

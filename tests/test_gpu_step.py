@@ -235,3 +235,37 @@ def test_hamiltonian_form_rejects_rescaled_analyses(axs):
             L.energies()
         with pytest.raises(axs.AxsError):
             L.axion_spectrum(16)
+
+
+@pytest.mark.parametrize("nd,N,form", [(2, 64, 0), (3, 32, 0), (3, 24, 1), (2, 48, 1)])
+def test_spectral_step_matches_oracle(axs, oracle, nd, N, form):
+    """laplacian = 1 (the reference's compute_laplacian_fft branch of
+    vvsl_field_rescaled, s_integrate.cpp:327-329), FP64 after 10 steps within
+    1e-11 of the oracle (the transforms differ from the oracle's by rounding)."""
+    p = params(axs, nd, N, 64, laplacian=1, form=form)
+    op = orc(p)
+    f = oracle.init_thermal(op, 17)
+    with axs.Lattice(p) as L:
+        L.upload(*f)
+        L.evolve(4)
+        L.evolve(6)
+        g = L.download()
+        tau, steps = L.time
+    o = oracle.evolve(op, *f, 10, form=form)
+    for q in range(4):
+        assert rel(g[q], o[q]) <= 1e-11, (q, rel(g[q], o[q]))
+    assert tau == o[4] and steps == 10
+
+
+def test_spectral_step_fp32_against_fp64(axs, oracle):
+    p64 = params(axs, 3, 48, 64, laplacian=1)
+    p32 = params(axs, 3, 48, 32, laplacian=1)
+    f = oracle.init_thermal(orc(p64), 19)
+    with axs.Lattice(p64) as A, axs.Lattice(p32) as B:
+        A.upload(*f)
+        B.upload(*f)
+        A.evolve(10)
+        B.evolve(10)
+        ga, gb = A.download(), B.download()
+    for q in range(4):
+        assert rel(gb[q], ga[q]) <= 1e-5, (q, rel(gb[q], ga[q]))

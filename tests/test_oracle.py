@@ -127,3 +127,18 @@ def test_strings_golden(oracle):
         if nd == 2:
             assert oracle.num_cores2(N, mask) == int(z["num_cores_serial"])
             assert num_cores2_ascending(N, np.flatnonzero(mask)) == int(z["num_cores_serial"])
+
+
+@pytest.mark.parametrize("nd,N", [(2, 32), (3, 16)])
+def test_spectral_laplacian_plane_wave(oracle, nd, N):
+    """The spectral Laplacian of a lattice plane wave is exactly -k^2 times it,
+    k = 2 pi n / (N dx), for every n below the Nyquist index."""
+    dx = 0.5
+    p = oracle_lib.make_params(NDIMS=nd, N=N, dx=dx, laplacian=1)
+    idx = np.indices((N,) * nd)
+    n = [3, 1, 2][:nd]
+    phase = sum(2 * np.pi * ni * ix / N for ni, ix in zip(n, idx))
+    f = np.cos(phase + 0.3)
+    k2 = sum((2 * np.pi * ni / (N * dx)) ** 2 for ni in n)
+    out = oracle.laplacian(p, f)
+    assert np.abs(out + k2 * f).max() <= 1e-11 * k2

@@ -38,6 +38,17 @@ def test_hamiltonian_step(oracle, nd, N, stencil):
     assert a[4] == b[4]
 
 
+@pytest.mark.parametrize("nd,N", [(2, 64), (2, 30), (3, 16), (3, 20)])
+def test_spectral_laplacian(oracle, nd, N):
+    """compute_laplacian_fft (s_integrate.cpp:179-296) against the oracle."""
+    rng = np.random.default_rng(nd * 10 + N)
+    p = oracle_lib.make_params(NDIMS=nd, N=N, dx=0.7, laplacian=1)
+    f = rng.standard_normal((N,) * nd)
+    a = oracle.laplacian(p, f)
+    b = REF.laplacian_fft(p, f)
+    assert np.abs(a - b).max() / np.abs(b).max() <= 1e-13
+
+
 @pytest.mark.parametrize("nd,N,thr", [(2, 96, 1), (3, 20, 1), (3, 20, 50)])
 def test_cores(oracle, nd, N, thr):
     rng = np.random.default_rng(N + thr)
