@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libaxs.so")
 DRIVER = os.path.join(HERE, "host", "axs_run")
 
-CUDA_SOURCES = ["axs_step.cu", "axs_init.cu", "axs_analysis.cu", "axs_api.cu"]
+CUDA_SOURCES = ["axs_step.cu", "axs_step_r.cu", "axs_init.cu", "axs_analysis.cu", "axs_api.cu"]
 HOST_SOURCES = ["axs_params.cpp", "axs_fileio.cpp", "axs_run.cpp"]
 
 NVCC = os.environ.get("NVCC", "nvcc")
@@ -43,7 +43,7 @@ def _stale(target, deps):
 
 def build(verbose=False, force=False):
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, "axs_internal.h"), os.path.join(ROOT, "include", "axs.h")]
+    headers = [os.path.join(CSRC, "axs_internal.h"), os.path.join(CSRC, "axs_tma.cuh"), os.path.join(ROOT, "include", "axs.h")]
     jobs = []
     objs = []
     for src in CUDA_SOURCES:

@@ -176,6 +176,10 @@ void lattice_autotune(Lattice *L);
 void ensemble_setup(Ensemble *E);
 void ensemble_evolve(Ensemble *E, int nsteps);
 void ensemble_autotune(Ensemble *E);
+// radius-R z-march kernels (axs_step_r.cu), by tile shape
+void launch_zmarch_r(int esz, int ty, int txmax, int slots, int r, const ZLat *d, int nlat, int64_t items,
+                     int *counters, int parity, int *derr, cudaStream_t st, int ctas_per_sm);
+void prepare_zmarch_r(int esz, int ty, int txmax, int slots, int r);
 std::string ensemble_describe(const Ensemble *E);
 void launch_sync_pi(Lattice *L);                      // scratch <- pi_n
 void launch_laplacian(Lattice *L, int comp, double *dout);

@@ -23,6 +23,7 @@
 #include <functional>
 
 #include "axs_internal.h"
+#include "axs_tma.cuh"
 
 namespace axs {
 
@@ -294,45 +295,6 @@ __global__ void k_unpack2(const typename Cplx<T>::type *__restrict__ src, S *__r
 // items from a global counter in z-chunk-major order, so tiles that share
 // halo rows run at the same time and meet their halos in L2.
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait: gives up after ~2^31 SM cycles (about a second).
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-    if (mbar_try_wait(bar, parity)) return true;
-    long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > (1ll << 31)) return false;
-    }
-    return true;
-}
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
-        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
-        : "memory");
-}
-
-template <typename T> struct Vec16;
-template <> struct Vec16<float> { typedef float4 type; };
-template <> struct Vec16<double> { typedef double2 type; };
-
 template <typename T, int TY, int TXMAX, int S>
 struct ZCfg {
     static constexpr int CS = 2 * (int)sizeof(T);             // bytes per complex site
@@ -537,19 +499,6 @@ __global__ void __launch_bounds__(256) k_zmarch(const ZLat *__restrict__ lats, i
 //    compute the plane, store psi_new and pih with 16-byte stores, and arrive
 //    on `empty` when they are done with a plane.
 // Items reach the consumers through a two-entry queue guarded by mbarriers.
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-// Warp-uniform bounded wait: 0 = completed, 1 = this warp timed out,
-// 2 = another warp or the producer aborted. Every lane gets the same answer,
-// so the warp never diverges around __syncwarp / the final barrier.
-__device__ __forceinline__ int warp_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag) {
-    const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(bar, parity));
-    if (!ok) return 1;
-    return __any_sync(0xffffffffu, *abort_flag != 0) ? 2 : 0;
-}
 
 template <typename T, int TY, int TXMAX, int S>
 struct Z2Cfg {
@@ -1226,8 +1175,9 @@ static int grid_for(int64_t len, int threads = 256) {
 // gen 1: k_zmarch (CTA barriers); gen 2: k_zmarch2 (producer warp); gen 3:
 // k_zmarch_2step (two steps per pass, complex float), whose odd last step of an
 // interval runs on the gen-2 `partner` with the same tile and launch table.
+// gen 4: k_zmarch2r (stencil radius r = 2..4, axs_step_r.cu).
 struct ZVariant {
-    int gen, ty, txmax, slots, ncw, partner;
+    int gen, ty, txmax, slots, ncw, partner, r;
 };
 static const ZVariant kZVariants[] = {
     {1, 8, 128, 4, 0, -1}, {1, 8, 128, 5, 0, -1}, {1, 16, 128, 4, 0, -1}, {1, 4, 256, 4, 0, -1},
@@ -1235,10 +1185,13 @@ static const ZVariant kZVariants[] = {
     {2, 8, 256, 5, 8, -1}, {2, 4, 128, 6, 8, -1}, {3, 8, 128, 4, 8, 6},  {3, 8, 128, 5, 8, 6},
     {3, 4, 256, 4, 8, 7},  {3, 8, 128, 4, 8, 6},  {3, 8, 128, 4, 8, 6},  {3, 8, 128, 5, 8, 6},
     {2, 8, 64, 5, 8, -1},  {3, 8, 64, 4, 4, 16},  {3, 8, 64, 5, 4, 16},  {3, 4, 128, 5, 4, 9},
+    {4, 8, 128, 6, 8, -1, 2},  {4, 4, 128, 6, 8, -1, 2},  {4, 8, 64, 8, 8, -1, 3},  {4, 4, 128, 8, 8, -1, 3},
+    {4, 4, 128, 10, 8, -1, 4}, {4, 8, 64, 10, 8, -1, 4},  {4, 4, 64, 10, 8, -1, 4},
 };
 static const int kNumZVariants = sizeof(kZVariants) / sizeof(kZVariants[0]);
 
 static bool two_step(int variant) { return variant >= 0 && variant < kNumZVariants && kZVariants[variant].gen == 3; }
+static int radius(const ZVariant &v) { return v.r > 0 ? v.r : 1; }
 
 std::string StepConfig::describe() const {
     char b[200];
@@ -1246,6 +1199,9 @@ std::string StepConfig::describe() const {
     else if (two_step(variant))
         snprintf(b, sizeof b, "TMA z-march variant %d (two steps per pass, halo depth 2; odd step on variant %d), tx=%d, zchunk=%d",
                  variant, kZVariants[variant].partner, tx, zchunk);
+    else if (variant >= 0 && variant < kNumZVariants && kZVariants[variant].gen == 4)
+        snprintf(b, sizeof b, "TMA z-march variant %d (stencil radius %d), tx=%d, zchunk=%d", variant,
+                 kZVariants[variant].r, tx, zchunk);
     else snprintf(b, sizeof b, "TMA z-march variant %d, tx=%d, zchunk=%d", variant, tx, zchunk);
     return b;
 }
@@ -1334,6 +1290,11 @@ static void launch_zmarch3_t(const ZLat *d, int nlat, int64_t items, int *counte
 
 static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t items, int *counters, int parity,
                           int *derr, cudaStream_t st, int ctas_per_sm) {
+    if (variant >= 0 && variant < kNumZVariants && kZVariants[variant].gen == 4) {
+        const ZVariant &v = kZVariants[variant];
+        launch_zmarch_r(esz, v.ty, v.txmax, v.slots, v.r, d, nlat, items, counters, parity, derr, st, ctas_per_sm);
+        return;
+    }
 #define AXS_ZV(I, TY, TX, S)                                                                                    \
     case I:                                                                                                     \
         if (esz == 4) launch_zmarch_t<float, TY, TX, S>(d, nlat, items, counters, parity, derr, st, ctas_per_sm); \
@@ -1378,6 +1339,11 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
 }
 
 static void prepare_zmarch(int esz, int variant) {
+    if (variant >= 0 && variant < kNumZVariants && kZVariants[variant].gen == 4) {
+        const ZVariant &v = kZVariants[variant];
+        prepare_zmarch_r(esz, v.ty, v.txmax, v.slots, v.r);
+        return;
+    }
 #define AXS_ZP(I, TY, TX, S)                                      \
     case I:                                                       \
         if (esz == 4) prepare_zmarch_t<float, TY, TX, S>();       \
@@ -1424,6 +1390,11 @@ static void prepare_zmarch(int esz, int variant) {
 // Dynamic shared memory of a variant (mirrors ZCfg / Z2Cfg).
 static int variant_smem(const ZVariant &v, int esz) {
     int cs = 2 * esz;
+    if (v.gen == 4) {   // mirrors ZRCfg
+        int vs = 16 / cs, rp = (v.r + vs - 1) / vs * vs;
+        int c = (v.ty + 2 * v.r) * v.txmax * cs, h = (v.ty * rp * cs + 127) / 128 * 128;
+        return v.slots * ((c + 2 * h + v.ty * v.txmax * cs + 127) / 128 * 128) + 256;
+    }
     if (v.gen == 3) {
         int st_m = (v.ty * 16 + 127) / 128 * 128;
         int slot = (v.ty + 4) * v.txmax * cs + 2 * (256 + st_m) + (v.ty + 2) * v.txmax * cs + 2 * st_m;
@@ -1461,7 +1432,7 @@ static int variant_tx(const ZVariant &v, int N, int esz) {
     int txmax = v.txmax;
     if (esz == 8) txmax = std::min(txmax, 128);   // box inner dim: 2*tx doubles <= 256
     if (variant_smem(v, esz) > max_smem_optin()) return 0;
-    if (N % v.ty != 0 || N < 4) return 0;
+    if (N % v.ty != 0 || N < 4 || v.ty < radius(v)) return 0;
     for (int tx = std::min(txmax, N); tx >= vs; --tx) {
         if (N % tx) continue;
         if (tx % vs) continue;
@@ -1471,11 +1442,16 @@ static int variant_tx(const ZVariant &v, int N, int esz) {
     return 0;
 }
 
+// A variant serves a lattice when its stencil radius is the lattice's and it tiles N.
+static bool variant_fits(const ZVariant &v, const axs_params &p, int esz) {
+    return radius(v) == p.stencil_setting + 1 && variant_tx(v, p.N, esz) > 0;
+}
+
 bool zmarch_supported(const axs_params &p) {
-    if (p.NDIMS != 3 || p.stencil_setting != 0 || p.laplacian != 0) return false;
+    if (p.NDIMS != 3 || p.laplacian != 0) return false;
     int esz = p.precision == AXS_F32 ? 4 : 8;
     for (int v = 0; v < kNumZVariants; ++v)
-        if (variant_tx(kZVariants[v], p.N, esz)) return true;
+        if (variant_fits(kZVariants[v], p, esz)) return true;
     return false;
 }
 
@@ -1523,13 +1499,15 @@ static int64_t fill_zlat(ZLat &z, Lattice *L, int variant, int zchunk, int64_t i
     if (oop && (!L->scratch || L->scratch == L->pih)) fail(AXS_ERR_STATE, "two-step variant without a second momentum buffer");
     memset(&z, 0, sizeof z);
     int vs = 16 / (2 * L->esz);
+    const int R = radius(v);
+    const int rp = (R + vs - 1) / vs * vs;   // x-halo sites per side (16-byte multiple)
     void *pb[2];
     pb[L->cur] = L->pih;
     pb[L->cur ^ 1] = oop ? L->scratch : L->pih;
     for (int b = 0; b < 2; ++b) {
-        encode_map(&z.tm_row[b], L->psi[b], N, L->esz, tx, 1);
+        encode_map(&z.tm_row[b], L->psi[b], N, L->esz, tx, R);     // R halo rows
         encode_map(&z.tm_main[b], L->psi[b], N, L->esz, tx, v.ty);
-        encode_map(&z.tm_xh[b], L->psi[b], N, L->esz, vs, v.ty);
+        encode_map(&z.tm_xh[b], L->psi[b], N, L->esz, rp, v.ty);   // x-halo strip
         encode_map(&z.tm_pih[b], pb[b], N, L->esz, tx, v.ty);
         if (oop) {
             encode_map(&z.t2_row2[b], L->psi[b], N, L->esz, tx, 2);
@@ -1591,7 +1569,7 @@ void step_setup(Lattice *L) {
     if (zmarch_supported(L->p)) {
         // default before tuning: first variant that tiles N
         for (int v = 0; v < kNumZVariants; ++v)
-            if (variant_tx(kZVariants[v], L->p.N, L->esz)) { L->cfg.kind = 1; L->cfg.variant = v; break; }
+            if (variant_fits(kZVariants[v], L->p, L->esz)) { L->cfg.kind = 1; L->cfg.variant = v; break; }
         L->cfg.zchunk = 64;
     }
     L->dcounter = (int *)dalloc(2 * sizeof(int));
@@ -1904,7 +1882,7 @@ void lattice_autotune(Lattice *L) {
         int k = 0, v = 0, zc = 64;
         if (sscanf(force, "%d,%d,%d", &k, &v, &zc) >= 1) {
             c.kind = (k == 1 && zmarch_supported(L->p) && v >= 0 && v < kNumZVariants &&
-                      variant_tx(kZVariants[v], L->p.N, L->esz)) ? 1 : 0;
+                      variant_fits(kZVariants[v], L->p, L->esz)) ? 1 : 0;
             c.variant = c.kind ? v : 0;
             c.zchunk = zc > 0 ? zc : 64;
             L->cfg = c;
@@ -1950,7 +1928,7 @@ void lattice_autotune(Lattice *L) {
     }
     const int zchunks[] = {32, 64, 128};
     for (int v = 0; v < kNumZVariants; ++v) {
-        if (!variant_tx(kZVariants[v], L->p.N, L->esz)) continue;
+        if (!variant_fits(kZVariants[v], L->p, L->esz)) continue;
         const bool two = two_step(v);
         for (int zc : zchunks) {
             if (zc > L->p.N) continue;
@@ -1995,7 +1973,7 @@ void lattice_autotune(Lattice *L) {
 // ---------------------------------------------------------------- ensemble
 static bool ensemble_variant_ok(Ensemble *E, int v) {
     for (Lattice *m : E->members)
-        if (m->p.NDIMS != 3 || m->p.stencil_setting != 0 || !variant_tx(kZVariants[v], m->p.N, m->esz)) return false;
+        if (m->p.NDIMS != 3 || m->p.laplacian != 0 || !variant_fits(kZVariants[v], m->p, m->esz)) return false;
     return true;
 }
 

@@ -1,0 +1,329 @@
+// TMA z-march step for the higher-order stencils: stencil_setting 1..3, i.e.
+// radius R = 2..4 of build_coefficient_matrix (src/standard/s_integrate.cpp:9-14,
+// 5-149). Same organisation as k_zmarch2 (one TMA producer warp, eight
+// consumer warps, full/empty mbarriers per ring slot, persistent CTAs taking
+// work items from a counter), with
+//  * per plane: the psi tile with an R-row periodic y halo (three boxes of R,
+//    TY and R rows that never wrap, TY >= R) and x strips of RP sites on both
+//    sides (R rounded up to 16 bytes, so strip coordinates stay 16-byte
+//    aligned; only the tile rows need them: the stencil is a cross), plus the
+//    pih tile;
+//  * a ring of S >= 2R + 2 slots holding the planes z-R .. z+R and one in flight;
+//  * the stencil sum formed exactly as stencil_at forms it for R > 1
+//    (c0 * psi, then per l: ((x- + x+) + (y- + y+)) + (z- + z+), fused into the
+//    sum with c_l), so every configuration is bit-identical to k_step_generic.
+// One pass per step: 32 B (FP32) / 64 B (FP64) per site-update, as for radius 1.
+#include <algorithm>
+
+#include "axs_internal.h"
+#include "axs_tma.cuh"
+
+namespace axs {
+
+template <typename T, int TY, int TXMAX, int S, int R>
+struct ZRCfg {
+    static constexpr int CS = 2 * (int)sizeof(T);
+    static constexpr int VS = 16 / CS;                         // sites per 16-byte vector
+    static constexpr int EU = CS / 8;                          // tensor-map elements per site
+    static constexpr int RP = (R + VS - 1) / VS * VS;          // x-halo sites per side
+    static constexpr int NCW = 8;
+    static constexpr int NT = (NCW + 1) * 32;
+    static constexpr int NC = NCW * 32;
+    static constexpr int MAXV = (TXMAX * TY / VS + NC - 1) / NC;
+    static constexpr int C_BYTES = (TY + 2 * R) * TXMAX * CS;  // psi rows y0-R .. y0+TY+R-1
+    static constexpr int H_PAD = (TY * RP * CS + 127) / 128 * 128;
+    static constexpr int P_OFF = C_BYTES + 2 * H_PAD;          // pih tile
+    static constexpr int SLOT = (P_OFF + TY * TXMAX * CS + 127) / 128 * 128;
+    static constexpr int BAR_OFF = S * SLOT;
+    static constexpr int SMEM = BAR_OFF + 256;
+    static_assert(S >= 2 * R + 2, "the ring holds 2R+1 planes and one in flight");
+    static_assert(TY >= R, "halo bands must not wrap inside a box");
+};
+
+template <typename T, int TY, int TXMAX, int S, int R>
+__global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R>::NT)
+    k_zmarch2r(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity, int *derr) {
+    typedef ZRCfg<T, TY, TXMAX, S, R> K;
+    typedef typename Cplx<T>::type C;
+    typedef typename Vec16<T>::type V;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + K::BAR_OFF);
+    uint64_t *empty = full + S;
+    uint64_t *ifull = empty + S;                                 // [2]
+    uint64_t *iempty = ifull + 2;                                // [2]
+    volatile int64_t *items = reinterpret_cast<volatile int64_t *>(iempty + 2);   // [2]
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(items + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), K::NCW);
+        }
+        for (int k = 0; k < 2; ++k) {
+            mbar_init(smem_u32(&ifull[k]), 1);
+            mbar_init(smem_u32(&iempty[k]), K::NCW);
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp == K::NCW) {
+        // ------------------------------------------------------------ producer
+        if (lane == 0) {
+            int64_t q = 0;
+            bool ok = true;
+            for (int64_t k = 0; ok; ++k) {
+                if (k >= 2) ok = mbar_wait_bounded(smem_u32(&iempty[k & 1]), (uint32_t)(((k >> 1) - 1) & 1));
+                if (!ok || *abort_flag) break;
+                const int64_t item = (int64_t)atomicAdd(&counters[0], 1);
+                items[k & 1] = item;
+                mbar_arrive(smem_u32(&ifull[k & 1]));
+                if (item >= total_items) break;
+                int li = 0;
+                while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+                const ZLat &Lt = lats[li];
+                const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
+                const int64_t local = item - Lt.item_base;
+                const int ncols = ntx * nty;
+                const int zq = (int)(local / ncols), col = (int)(local % ncols);
+                const int x0 = (col % ntx) * tx, y0 = (col / ntx) * TY;
+                const int za = (int)((int64_t)zq * N / nzc), zb = (int)((int64_t)(zq + 1) * N / nzc);
+                const int nload = zb - za + 2 * R;
+                const int bin = Lt.a_index ^ parity;
+                const bool xhalo = tx < N;
+                const uint32_t psi_bytes = (uint32_t)((TY + 2 * R) * tx * K::CS + (xhalo ? 2 * TY * K::RP * K::CS : 0));
+                const uint32_t pih_bytes = (uint32_t)(TY * tx * K::CS);
+                const int ym = y0 >= R ? y0 - R : y0 - R + N;
+                const int yp = (y0 + TY == N) ? 0 : y0 + TY;
+                const int xl = x0 >= K::RP ? x0 - K::RP : x0 - K::RP + N;
+                const int xr = (x0 + tx == N) ? 0 : x0 + tx;
+                for (int i = 0; i < nload; ++i, ++q) {
+                    const int s = (int)(q % S);
+                    if (q >= S) {
+                        ok = mbar_wait_bounded(smem_u32(&empty[s]), (uint32_t)(((q / S) - 1) & 1));
+                        if (!ok || *abort_flag) break;
+                    }
+                    int z = za - R + i;
+                    z = z < 0 ? z + N : (z >= N ? z - N : z);
+                    unsigned char *slot = smem + s * K::SLOT;
+                    const uint32_t bar = smem_u32(&full[s]);
+                    const bool with_pih = i >= R && i < nload - R;
+                    mbar_expect_tx(bar, psi_bytes + (with_pih ? pih_bytes : 0u) +
+                                            (i == 0 ? (uint32_t)Lt.debug_tx_excess : 0u));
+                    tma_load_3d(smem_u32(slot), &Lt.tm_row[bin], x0 * K::EU, ym, z, bar);
+                    tma_load_3d(smem_u32(slot + R * tx * K::CS), &Lt.tm_main[bin], x0 * K::EU, y0, z, bar);
+                    tma_load_3d(smem_u32(slot + (TY + R) * tx * K::CS), &Lt.tm_row[bin], x0 * K::EU, yp, z, bar);
+                    if (xhalo) {
+                        tma_load_3d(smem_u32(slot + K::C_BYTES), &Lt.tm_xh[bin], xl * K::EU, y0, z, bar);
+                        tma_load_3d(smem_u32(slot + K::C_BYTES + K::H_PAD), &Lt.tm_xh[bin], xr * K::EU, y0, z, bar);
+                    }
+                    if (with_pih) tma_load_3d(smem_u32(slot + K::P_OFF), &Lt.tm_pih[bin], x0 * K::EU, y0, z, bar);
+                }
+            }
+            if (!ok) {
+                atomicOr(derr, DEVERR_TIMEOUT);
+                *abort_flag = 1;
+            }
+            // Drain: wait (bounded) for this CTA's last loads still in flight.
+            for (int64_t d = q > S ? q - S : 0; d < q; ++d)
+                mbar_wait_bounded(smem_u32(&full[d % S]), (uint32_t)((d / S) & 1));
+        }
+    } else {
+        // ------------------------------------------------------------ consumers
+        const int cid = tid;
+        const int setting = R - 1;
+        T coef[R + 1];
+#pragma unroll
+        for (int l = 0; l <= R; ++l) coef[l] = (T)stencil_coef(setting, 3, l);
+        int64_t q0 = 0;
+        for (int64_t k = 0;; ++k) {
+            const int w0 = warp_wait(smem_u32(&ifull[k & 1]), (uint32_t)((k >> 1) & 1), abort_flag);
+            if (w0) {
+                if (w0 == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
+                break;
+            }
+            bool ok = true;
+            const int64_t item = items[k & 1];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&iempty[k & 1]));
+            if (item >= total_items) break;
+            int li = 0;
+            while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+            const ZLat &Lt = lats[li];
+            const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
+            const int64_t local = item - Lt.item_base;
+            const int ncols = ntx * nty;
+            const int zq = (int)(local / ncols), col = (int)(local % ncols);
+            const int x0 = (col % ntx) * tx, y0 = (col / ntx) * TY;
+            const int za = (int)((int64_t)zq * N / nzc), zb = (int)((int64_t)(zq + 1) * N / nzc);
+            const int T_steps = zb - za;
+            const int bin = Lt.a_index ^ parity;
+            C *psi_out = reinterpret_cast<C *>(Lt.psi[bin ^ 1]);
+            C *pih = reinterpret_cast<C *>(Lt.pih[bin ^ 1]);   // output; the input arrives by TMA
+            const double tau = Lt.clock[bin];
+            const StepCoefs<T> cf = make_coefs<T>(tau, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs, Lt.form);
+            if (local == 0 && cid == 0) Lt.clock[bin ^ 1] = tau + Lt.dt;   // tau += dt, s_integrate.cpp:317
+            const bool xhalo = tx < N;
+            const int nvx = tx / K::VS;
+            const int nvec = nvx * TY;
+            for (int t = 0; t < T_steps && ok; ++t) {
+                const int64_t qn = q0 + t + 2 * R;
+                int w = 0;
+                if (t == 0)
+                    for (int d = 0; d < 2 * R && !w; ++d)
+                        w = warp_wait(smem_u32(&full[(q0 + d) % S]), (uint32_t)(((q0 + d) / S) & 1), abort_flag);
+                if (!w) w = warp_wait(smem_u32(&full[qn % S]), (uint32_t)((qn / S) & 1), abort_flag);
+                if (w) {
+                    if (w == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
+                    ok = false;
+                    break;
+                }
+                const int z = za + t;
+                const C *Zp[2 * R + 1];   // planes z-R .. z+R
+#pragma unroll
+                for (int d = 0; d <= 2 * R; ++d) Zp[d] = reinterpret_cast<const C *>(smem + ((q0 + t + d) % S) * K::SLOT);
+                const C *Cz = Zp[R];
+                const C *Lh = reinterpret_cast<const C *>(reinterpret_cast<const unsigned char *>(Cz) + K::C_BYTES);
+                const C *Rh = reinterpret_cast<const C *>(reinterpret_cast<const unsigned char *>(Cz) + K::C_BYTES + K::H_PAD);
+                const C *Ph = reinterpret_cast<const C *>(reinterpret_cast<const unsigned char *>(Cz) + K::P_OFF);
+#pragma unroll
+                for (int jv = 0; jv < K::MAXV; ++jv) {
+                    const int v = cid + jv * K::NC;
+                    if (v >= nvec) continue;
+                    const int yy = v / nvx, xx = (v % nvx) * K::VS;
+                    const int rrow = (R + yy) * tx;   // the site's row in the band
+                    // an x neighbour at column pos of the site's row (periodic)
+                    auto getx = [&](int pos) -> C {
+                        if (pos >= 0 && pos < tx) return Cz[rrow + pos];
+                        if (xhalo) return pos < 0 ? Lh[yy * K::RP + pos + K::RP] : Rh[yy * K::RP + pos - tx];
+                        return Cz[rrow + (pos < 0 ? pos + tx : pos - tx)];
+                    };
+                    C ctr[K::VS];
+                    *reinterpret_cast<V *>(ctr) = *reinterpret_cast<const V *>(&Cz[rrow + xx]);
+                    T a1[K::VS], a2[K::VS];
+#pragma unroll
+                    for (int j = 0; j < K::VS; ++j) {
+                        a1[j] = coef[0] * ctr[j].x;
+                        a2[j] = coef[0] * ctr[j].y;
+                    }
+#pragma unroll
+                    for (int l = 1; l <= R; ++l) {
+                        C ym[K::VS], yp[K::VS], zm[K::VS], zp[K::VS];
+                        *reinterpret_cast<V *>(ym) = *reinterpret_cast<const V *>(&Cz[rrow - l * tx + xx]);
+                        *reinterpret_cast<V *>(yp) = *reinterpret_cast<const V *>(&Cz[rrow + l * tx + xx]);
+                        *reinterpret_cast<V *>(zm) = *reinterpret_cast<const V *>(&Zp[R - l][rrow + xx]);
+                        *reinterpret_cast<V *>(zp) = *reinterpret_cast<const V *>(&Zp[R + l][rrow + xx]);
+#pragma unroll
+                        for (int j = 0; j < K::VS; ++j) {
+                            const C xm = getx(xx + j - l), xp = getx(xx + j + l);
+                            T s1 = (xm.x + xp.x) + (ym[j].x + yp[j].x);
+                            T s2 = (xm.y + xp.y) + (ym[j].y + yp[j].y);
+                            s1 = s1 + (zm[j].x + zp[j].x);
+                            s2 = s2 + (zm[j].y + zp[j].y);
+                            a1[j] = fma(coef[l], s1, a1[j]);
+                            a2[j] = fma(coef[l], s2, a2[j]);
+                        }
+                    }
+                    T pv[2 * K::VS];
+                    *reinterpret_cast<V *>(pv) = *reinterpret_cast<const V *>(&Ph[yy * tx + xx]);
+                    C outv[K::VS];
+#pragma unroll
+                    for (int j = 0; j < K::VS; ++j)
+                        site_update<T>(ctr[j].x, ctr[j].y, a1[j], a2[j], pv[2 * j], pv[2 * j + 1], outv[j].x, outv[j].y, cf);
+                    const int64_t off = ((int64_t)z * N + (y0 + yy)) * N + (x0 + xx);
+                    *reinterpret_cast<V *>(&pih[off]) = *reinterpret_cast<V *>(pv);
+                    *reinterpret_cast<V *>(&psi_out[off]) = *reinterpret_cast<V *>(outv);
+                }
+                // this warp is done with plane z-R (load q0+t); at the last
+                // plane also with the item's last 2R loads
+                __syncwarp();
+                if (lane == 0) {
+                    mbar_arrive(smem_u32(&empty[(q0 + t) % S]));
+                    if (t == T_steps - 1)
+                        for (int d = 1; d <= 2 * R; ++d) mbar_arrive(smem_u32(&empty[(q0 + t + d) % S]));
+                }
+            }
+            if (!ok) break;
+            q0 += T_steps + 2 * R;
+        }
+    }
+    __syncwarp();      // reconverge every warp (the producer's lane 0 ran alone) before the barrier
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&counters[1], 1) == (int)gridDim.x - 1) {
+            counters[0] = 0;
+            counters[1] = 0;
+            __threadfence();
+        }
+    }
+}
+
+// ---------------------------------------------------------------- host side
+
+template <typename T, int TY, int TXMAX, int S, int R>
+static int prepare_r_t() {
+    typedef ZRCfg<T, TY, TXMAX, S, R> K;
+    static int occ = -1;
+    if (occ < 0) {
+        AXS_CUDA(cudaFuncSetAttribute(k_zmarch2r<T, TY, TXMAX, S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      K::SMEM));
+        int o = 0;
+        AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_zmarch2r<T, TY, TXMAX, S, R>, K::NT, K::SMEM));
+        if (o < 1) fail(AXS_ERR_CUDA, "radius-%d z-march kernel does not fit on an SM", R);
+        occ = o;
+    }
+    return occ;
+}
+
+template <typename T, int TY, int TXMAX, int S, int R>
+static void launch_r_t(const ZLat *d, int nlat, int64_t items, int *counters, int parity, int *derr, cudaStream_t st,
+                       int ctas_per_sm) {
+    typedef ZRCfg<T, TY, TXMAX, S, R> K;
+    const int occ = prepare_r_t<T, TY, TXMAX, S, R>();
+    const int per = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ) : occ;
+    const int64_t grid = std::min<int64_t>((int64_t)per * num_sms(), items);
+    k_zmarch2r<T, TY, TXMAX, S, R><<<(int)grid, K::NT, K::SMEM, st>>>(d, nlat, items, counters, parity, derr);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+
+// The instantiated shapes (ty, txmax, slots, radius); mirrored by the
+// radius-R entries of the variant table in axs_step.cu.
+#define AXS_ZR_SHAPES(X) \
+    X(8, 128, 6, 2)      \
+    X(4, 128, 6, 2)      \
+    X(8, 64, 8, 3)       \
+    X(4, 128, 8, 3)      \
+    X(4, 128, 10, 4)     \
+    X(8, 64, 10, 4)      \
+    X(4, 64, 10, 4)
+
+void launch_zmarch_r(int esz, int ty, int txmax, int slots, int r, const ZLat *d, int nlat, int64_t items,
+                     int *counters, int parity, int *derr, cudaStream_t st, int ctas_per_sm) {
+#define AXS_ZR_LAUNCH(TY, TX, S, R)                                                                         \
+    if (ty == TY && txmax == TX && slots == S && r == R) {                                                  \
+        if (esz == 4) launch_r_t<float, TY, TX, S, R>(d, nlat, items, counters, parity, derr, st, ctas_per_sm); \
+        else launch_r_t<double, TY, TX, S, R>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);         \
+        return;                                                                                             \
+    }
+    AXS_ZR_SHAPES(AXS_ZR_LAUNCH)
+#undef AXS_ZR_LAUNCH
+    fail(AXS_ERR_ARG, "no radius-%d z-march kernel for tile %dx%d, %d slots", r, txmax, ty, slots);
+}
+
+void prepare_zmarch_r(int esz, int ty, int txmax, int slots, int r) {
+#define AXS_ZR_PREP(TY, TX, S, R)                                \
+    if (ty == TY && txmax == TX && slots == S && r == R) {       \
+        if (esz == 4) prepare_r_t<float, TY, TX, S, R>();        \
+        else prepare_r_t<double, TY, TX, S, R>();                \
+        return;                                                  \
+    }
+    AXS_ZR_SHAPES(AXS_ZR_PREP)
+#undef AXS_ZR_PREP
+    fail(AXS_ERR_ARG, "no radius-%d z-march kernel for tile %dx%d, %d slots", r, txmax, ty, slots);
+}
+
+}  // namespace axs

@@ -269,3 +269,33 @@ def test_spectral_step_fp32_against_fp64(axs, oracle):
         ga, gb = A.download(), B.download()
     for q in range(4):
         assert rel(gb[q], ga[q]) <= 1e-5, (q, rel(gb[q], ga[q]))
+
+
+RADIUS_VARIANTS = {1: ["1,20,32", "1,21,64"], 2: ["1,22,64", "1,23,128"], 3: ["1,24,32", "1,25,64", "1,26,16"]}
+
+
+@pytest.mark.parametrize("stencil", [1, 2, 3])
+@pytest.mark.parametrize("N,precision", [(64, 32), (160, 32), (64, 64), (160, 64)])
+def test_higher_order_zmarch_bit_identical(axs, stencil, N, precision):
+    """The TMA z-march kernels for stencil radius 2..4 give the generic
+    kernel's bits (same stencil association order), with and without x tiling."""
+    p = params(axs, 3, N, precision, stencil_setting=stencil)
+    dt = np.float32 if precision == 32 else np.float64
+    outs = []
+    for force in ["0,0,64"] + RADIUS_VARIANTS[stencil]:
+        os.environ["AXS_FORCE_CONFIG"] = force
+        try:
+            with axs.Lattice(p) as L:
+                L.init_thermal(31)
+                for n in (1, 4, 3):
+                    L.evolve(n)
+                outs.append((L.describe(), L.download(dtype=dt)))
+        finally:
+            del os.environ["AXS_FORCE_CONFIG"]
+    d0, g0 = outs[0]
+    assert "generic" in d0
+    if precision == 32:
+        assert all("stencil radius %d" % (stencil + 1) in d for d, _ in outs[1:]), [d for d, _ in outs]
+    for d, g in outs[1:]:
+        for q in range(4):
+            assert np.array_equal(g[q], g0[q]), (d0, d, q)
