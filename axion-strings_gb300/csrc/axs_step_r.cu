@@ -194,14 +194,23 @@ __global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R>::NT)
                     if (v >= nvec) continue;
                     const int yy = v / nvx, xx = (v % nvx) * K::VS;
                     const int rrow = (R + yy) * tx;   // the site's row in the band
-                    // an x neighbour at column pos of the site's row (periodic)
-                    auto getx = [&](int pos) -> C {
-                        if (pos >= 0 && pos < tx) return Cz[rrow + pos];
-                        if (xhalo) return pos < 0 ? Lh[yy * K::RP + pos + K::RP] : Rh[yy * K::RP + pos - tx];
-                        return Cz[rrow + (pos < 0 ? pos + tx : pos - tx)];
-                    };
+                    // The x window [xx-RP, xx+VS+RP) of the site's row as 16-byte
+                    // vectors: RP is a multiple of VS, so each vector comes whole
+                    // from the band, a strip, or (one x tile) the periodic band.
+                    constexpr int NW = (2 * K::RP + K::VS) / K::VS;
+                    C win[NW * K::VS];
+#pragma unroll
+                    for (int kw = 0; kw < NW; ++kw) {
+                        const int pos = xx - K::RP + kw * K::VS;
+                        const C *src;
+                        if (pos >= 0 && pos < tx) src = &Cz[rrow + pos];
+                        else if (xhalo) src = pos < 0 ? &Lh[yy * K::RP + pos + K::RP] : &Rh[yy * K::RP + pos - tx];
+                        else src = &Cz[rrow + (pos < 0 ? pos + tx : pos - tx)];
+                        *reinterpret_cast<V *>(&win[kw * K::VS]) = *reinterpret_cast<const V *>(src);
+                    }
                     C ctr[K::VS];
-                    *reinterpret_cast<V *>(ctr) = *reinterpret_cast<const V *>(&Cz[rrow + xx]);
+#pragma unroll
+                    for (int j = 0; j < K::VS; ++j) ctr[j] = win[K::RP + j];
                     T a1[K::VS], a2[K::VS];
 #pragma unroll
                     for (int j = 0; j < K::VS; ++j) {
@@ -217,7 +226,7 @@ __global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R>::NT)
                         *reinterpret_cast<V *>(zp) = *reinterpret_cast<const V *>(&Zp[R + l][rrow + xx]);
 #pragma unroll
                         for (int j = 0; j < K::VS; ++j) {
-                            const C xm = getx(xx + j - l), xp = getx(xx + j + l);
+                            const C xm = win[K::RP + j - l], xp = win[K::RP + j + l];
                             T s1 = (xm.x + xp.x) + (ym[j].x + yp[j].x);
                             T s2 = (xm.y + xp.y) + (ym[j].y + yp[j].y);
                             s1 = s1 + (zm[j].x + zp[j].x);
