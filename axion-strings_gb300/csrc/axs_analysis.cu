@@ -21,14 +21,38 @@ static int grid_cap(int64_t work, int threads, int per_sm) {
 // of min(|dn|, 1-|dn|) over three edges of a plaquette exceeds
 // accept = (double)(0.5f*(1-thr/100.0f)), with n = (theta+pi)/(2 pi) and
 // theta = atan2(phi1, phi2). The decision is taken in two stages:
-//  1. FP32: n from atan2f, edges and sums in float. The error of each float
-//     sum against the exact double sum is below 2e-6 (|n| <= 1: atan2f within
-//     a few ulp of pi, n within 3e-7, each edge within 7e-7), so a float sum
-//     farther than kMargin = 1e-5 from accept decides the cell.
+//  1. FP32: n from fast_atan2 (below), edges and sums in float. The error of
+//     each float sum against the exact double sum is below 2e-6 (theta within
+//     5e-7 rad, n within 1.5e-7, each edge within 4e-7, plus the rounding of
+//     two additions), so a float sum farther than kMargin = 1e-5 from accept
+//     decides the cell.
 //  2. Otherwise the cell is recomputed with the reference's double
 //     expressions in the reference's order (no contraction, IEEE division),
 //     which makes the decision bit-exact to the reference on a given theta.
 static constexpr float kMargin = 1e-5f;
+
+// atan2(y, x) in float within 5e-7 rad, for the float stage above: octant
+// reduction to a = min(|x|,|y|) / max(|x|,|y|) in [0, 1], atan(a) = a P(a^2)
+// with P of degree 7 fitted to atan on [0, 1] (weighted least squares iterated
+// to equal ripple, Lawson's method; 1.4e-7 rad evaluated in float), then the
+// octant undone. Exact zeros take atan2f (the signed results on the axes).
+__device__ constexpr float kAtanC[8] = {0.9999993443489075f,  -0.33329859375953674f, 0.19946566224098206f,
+                                    -0.1390862911939621f, 0.0964219719171524f,   -0.0559123270213604f,
+                                    0.021862957626581192f, -0.004054567310959101f};
+__device__ __forceinline__ float fast_atan2(float y, float x) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+    if (mn == 0.0f) return atan2f(y, x);
+    const float a = __fdiv_rn(mn, mx);
+    const float s = a * a;
+    float p = kAtanC[7];
+#pragma unroll
+    for (int k = 6; k >= 0; --k) p = fmaf(p, s, kAtanC[k]);
+    float r = p * a;
+    if (ay > ax) r = 1.5707963267948966f - r;
+    if (x < 0.0f) r = 3.1415926535897932f - r;
+    return copysignf(r, y);
+}
 
 template <typename T, bool FROM_THETA>
 struct Corner {
@@ -37,7 +61,7 @@ struct Corner {
     __device__ __forceinline__ float nf(int64_t m) const {
         float th;
         if (FROM_THETA) th = (float)theta[m];
-        else { auto v = psi[m]; th = atan2f((float)v.x, (float)v.y); }
+        else { auto v = psi[m]; th = fast_atan2((float)v.x, (float)v.y); }
         return fmaf(th, 0.15915494309189535f, 0.5f);
     }
     __device__ __forceinline__ double nd(int64_t m) const {
@@ -133,10 +157,10 @@ __global__ void __launch_bounds__(256) k_cores(const typename Cplx<T>::type *__r
 // site of halo in +x and +y) are computed once per site into a two-plane
 // shared ring (k_cores evaluates them once per corner, six times per site).
 // Same float n, same margin test, same double replay: same decisions.
-static constexpr int kCX = 64, kCY = 8, kCZ = 32;   // cells per block tile; 256 threads x 2 cells
+static constexpr int kCX = 64, kCY = 16, kCZ = 32;   // cells per block tile; 256 threads x 4 cells
 
 template <typename T>
-__global__ void __launch_bounds__(256, 4) k_cores3_tiled(const typename Cplx<T>::type *__restrict__ psi,
+__global__ void __launch_bounds__(256, 3) k_cores3_tiled(const typename Cplx<T>::type *__restrict__ psi,
                                                       uint8_t *__restrict__ mask, int N, double accept,
                                                       unsigned long long *count) {
     typedef typename Cplx<T>::type C;
@@ -151,28 +175,43 @@ __global__ void __launch_bounds__(256, 4) k_cores3_tiled(const typename Cplx<T>:
     const int tid = threadIdx.x;
     const int cx = tid % 32, cy = tid / 32;
     unsigned long long local = 0;
+    // Per-thread offsets do not depend on z: the tile sites this thread loads
+    // (in-plane offset, shared index; -1 when outside) and its two cells.
+    int so[PER], si[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int s = tid + k * 256;
+        const int sx = s % (kCX + 1), sy = s / (kCX + 1);
+        int gx = x0 + sx, gy = y0 + sy;
+        si[k] = -1;
+        so[k] = 0;
+        if (s >= NS || gx > N || gy > N) continue;
+        gx = gx >= N ? gx - N : gx;
+        gy = gy >= N ? gy - N : gy;
+        so[k] = gy * N + gx;
+        si[k] = sy * (kCX + 1) + sx;
+    }
+    // cells (cx + 32 (c & 1), cy + 8 (c >> 1)) of the tile
+    int co[4];
+    bool cv[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const int x = x0 + cx + 32 * (c & 1), y = y0 + cy + 8 * (c >> 1);
+        cv[c] = x < N && y < N;
+        co[c] = cv[c] ? y * N + x : 0;
+    }
     C pre[PER];   // psi of the next plane's tile, loaded one plane ahead
     auto load = [&](int z) {
-        const int64_t zb = (int64_t)(z >= N ? z - N : z) * NN;
+        const C *pl = psi + (int64_t)(z >= N ? z - N : z) * NN;
 #pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            const int s = tid + k * 256;
-            const int sx = s % (kCX + 1), sy = s / (kCX + 1);
-            int gx = x0 + sx, gy = y0 + sy;
-            if (s >= NS || gx > N || gy > N) continue;
-            gx = gx >= N ? gx - N : gx;
-            gy = gy >= N ? gy - N : gy;
-            pre[k] = psi[zb + (int64_t)gy * N + gx];
-        }
+        for (int k = 0; k < PER; ++k)
+            if (si[k] >= 0) pre[k] = pl[so[k]];
     };
     auto store = [&](int buf) {
+        float *dst = &nsm[buf][0][0];
 #pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            const int s = tid + k * 256;
-            const int sx = s % (kCX + 1), sy = s / (kCX + 1);
-            if (s >= NS || x0 + sx > N || y0 + sy > N) continue;
-            nsm[buf][sy][sx] = fmaf(atan2f((float)pre[k].x, (float)pre[k].y), 0.15915494309189535f, 0.5f);
-        }
+        for (int k = 0; k < PER; ++k)
+            if (si[k] >= 0) dst[si[k]] = fmaf(fast_atan2((float)pre[k].x, (float)pre[k].y), 0.15915494309189535f, 0.5f);
     };
     load(z0);
     store(0);
@@ -182,13 +221,13 @@ __global__ void __launch_bounds__(256, 4) k_cores3_tiled(const typename Cplx<T>:
         store(cur ^ 1);                 // plane z+1
         if (z + 2 <= z1) load(z + 2);   // in flight while plane z is evaluated
         __syncthreads();
+        uint8_t *mz = mask + (int64_t)z * NN;
 #pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            const int lx = cx + 32 * c;
-            const int x = x0 + lx, y = y0 + cy;
-            if (x >= N || y >= N) continue;
-            const float f000 = nsm[cur][cy][lx], f100 = nsm[cur ^ 1][cy][lx], f110 = nsm[cur ^ 1][cy + 1][lx],
-                        f010 = nsm[cur][cy + 1][lx], f011 = nsm[cur][cy + 1][lx + 1], f001 = nsm[cur][cy][lx + 1];
+        for (int c = 0; c < 4; ++c) {
+            if (!cv[c]) continue;
+            const int lx = cx + 32 * (c & 1), ly = cy + 8 * (c >> 1);
+            const float f000 = nsm[cur][ly][lx], f100 = nsm[cur ^ 1][ly][lx], f110 = nsm[cur ^ 1][ly + 1][lx],
+                        f010 = nsm[cur][ly + 1][lx], f011 = nsm[cur][ly + 1][lx + 1], f001 = nsm[cur][ly][lx + 1];
             const float e_000_100 = circf(f000, f100);
             const float e_011_001 = circf(f011, f001);
             const float sa = e_000_100 + circf(f100, f110) + circf(f110, f010);
@@ -196,11 +235,10 @@ __global__ void __launch_bounds__(256, 4) k_cores3_tiled(const typename Cplx<T>:
             const float sc = circf(f000, f010) + circf(f010, f011) + e_011_001;
             const float mx = fmaxf(sa, fmaxf(sb, sc));
             int flag;
-            const int64_t m = (int64_t)z * NN + (int64_t)y * N + x;
             if (mx > acc_f + kMargin) flag = 1;
             else if (mx < acc_f - kMargin) flag = 0;
-            else flag = cell3_exact<T, false>(cn, x, y, z, N, accept);
-            mask[m] = (uint8_t)flag;
+            else flag = cell3_exact<T, false>(cn, x0 + lx, y0 + ly, z, N, accept);
+            mz[co[c]] = (uint8_t)flag;
             local += flag;
         }
         __syncthreads();   // plane z's buffer is refilled with plane z+2 next
