@@ -680,7 +680,7 @@ template <> __device__ __forceinline__ FF mode_power<double>(const double2 &f) {
 // rows: power, |n|, count).
 template <typename T, typename B>
 __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *__restrict__ F, int N, int ndims,
-                                                  B binner, int nbins, const float2 *__restrict__ sqrt_tab,
+                                                  B binner, int nbins,
                                                   double *__restrict__ partials) {
     typedef typename Cplx<T>::type C;
     extern __shared__ double hist[];   // [4 warps][3][nbins], bin table, [4 warps][nh] staged rows
@@ -734,7 +734,12 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
                 const int wt = (ix == 0 || 2 * ix == N) ? 1 : 2;
                 const float fw = (float)wt;   // x1 or x2: exact in float-float
                 const FF p = mode_power<T>(stage[ix]);
-                const float2 sq = sqrt_tab[n2];
+                // |n| = sqrt(n2) as float-float: hi = sqrtf (correctly rounded), the residual
+                // n2 - hi^2 is exact in float (that of a correctly rounded square
+                // root always is) and lo = residual / (2 hi); n2 < 2^24 is exact in float
+                const float n2f = (float)n2;
+                const float shi = sqrtf(n2f);
+                const float2 sq = make_float2(shi, shi > 0.0f ? __fdiv_rn(fmaf(-shi, shi, n2f), 2.0f * shi) : 0.0f);
                 v = ff_add(v, FF{fw * p.hi, fw * p.lo});
                 kk = ff_add(kk, FF{fw * sq.x, fw * sq.y});
                 c += wt;
@@ -784,16 +789,6 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
     }
 }
 
-// sqrt(i) as a float-float pair (IEEE double sqrt, split)
-__global__ void k_sqrt_table(float2 *tab, int64_t n) {
-    int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const double r = sqrt((double)i);
-        const float hi = __double2float_rn(r);
-        tab[i] = make_float2(hi, __double2float_rn(r - (double)hi));
-    }
-}
-
 // gather a real field into fft_in: src = complex array, component comp
 template <typename T>
 __global__ void k_gather_real(const T *__restrict__ src_cplx, int comp, T *__restrict__ dst, int64_t len) {
@@ -834,11 +829,16 @@ __global__ void __launch_bounds__(256) k_axion_zcol(const typename Cplx<T>::type
     const int64_t col = (int64_t)y * N + x;
     const int64_t xm = (int64_t)y * N + (x == 0 ? N - 1 : x - 1), xp = (int64_t)y * N + (x == N - 1 ? 0 : x + 1);
     const int64_t ym = (int64_t)(y == 0 ? N - 1 : y - 1) * N + x, yp = (int64_t)(y == N - 1 ? 0 : y + 1) * N + x;
-    C zm = psi[(int64_t)(N - 1) * NN + col], zc = psi[col];
+    // the next plane's psi and pih are loaded one iteration ahead, so two
+    // planes of loads are in flight per thread
+    C zm = psi[(int64_t)(N - 1) * NN + col], zc = psi[col], zp = psi[(N > 1 ? NN : 0) + col];
+    C pc = pih[col];
     for (int z = 0; z < N; ++z) {
         const int64_t base = (int64_t)z * NN;
-        const C zp = psi[(z + 1 == N ? 0 : base + NN) + col];
-        C p = pih[base + col];
+        const int z2 = z + 2 >= N ? z + 2 - N : z + 2;
+        const C zpn = psi[(int64_t)z2 * NN + col];
+        const C pn = pih[(z + 1 == N ? 0 : base + NN) + col];
+        C p = pc;
         if (!fresh) {   // a fresh state holds pi_0 itself (the reference's ker is zero)
             const C a = psi[base + xm], b = psi[base + xp], d = psi[base + ym], e = psi[base + yp];
             const T L1 = lap7<T>(zc.x, a.x, b.x, d.x, e.x, zm.x, zp.x);
@@ -848,6 +848,8 @@ __global__ void __launch_bounds__(256) k_axion_zcol(const typename Cplx<T>::type
         dst[base + col] = axion_f<T>(zc.x, zc.y, p.x, p.y, itau);
         zm = zc;
         zc = zp;
+        zp = zpn;
+        pc = pn;
     }
 }
 
@@ -886,24 +888,14 @@ static void bin_spectrum(Lattice *L, const B &binner, int nbins, std::vector<dou
     double *part = (double *)dalloc((size_t)nblk * 3 * nbins * sizeof(double) + (size_t)3 * nbins * sizeof(double));
     double *out = part + (size_t)nblk * 3 * nbins;
     try {
-        const int64_t nsq = (int64_t)L->p.NDIMS * (N / 2) * (N / 2) + 1;   // n2 <= NDIMS (N/2)^2
-        if (!L->dsqrt || L->sqrt_len < nsq) {
-            dfree(L->dsqrt);
-            L->dsqrt = nullptr;
-            L->dsqrt = (double *)dalloc((size_t)nsq * sizeof(double));
-            L->sqrt_len = nsq;
-            k_sqrt_table<<<grid_cap(nsq, 256, 4), 256, 0, L->stream>>>((float2 *)L->dsqrt, nsq);
-            AXS_CUDA(cudaGetLastError());
-            count_launches(1);
-        }
         if (sm > 48 * 1024) {
             if (L->esz == 4) AXS_CUDA(cudaFuncSetAttribute(k_bin_runs<float, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
             else AXS_CUDA(cudaFuncSetAttribute(k_bin_runs<double, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         }
         if (L->esz == 4)
-            k_bin_runs<float, B><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, (const float2 *)L->dsqrt, part);
+            k_bin_runs<float, B><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part);
         else
-            k_bin_runs<double, B><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, (const float2 *)L->dsqrt, part);
+            k_bin_runs<double, B><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part);
         AXS_CUDA(cudaGetLastError());
         k_bin_final3<<<nbins, 256, 0, L->stream>>>(part, nblk, nbins, out);
         AXS_CUDA(cudaGetLastError());
@@ -1181,8 +1173,6 @@ void analysis_release(Lattice *L) {
     if (L->have_plan) cufftDestroy(L->plan_r2c);
     L->have_plan = false;
     dfree(L->dpartials); L->dpartials = nullptr;
-    dfree(L->dsqrt); L->dsqrt = nullptr;
-    L->sqrt_len = 0;
 }
 
 }  // namespace axs

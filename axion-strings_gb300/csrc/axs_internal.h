@@ -137,8 +137,6 @@ struct Lattice {
     cufftHandle plan_r2c = 0;
     bool have_plan = false;
     double *dpartials = nullptr;     // reduction partials
-    double *dsqrt = nullptr;         // sqrt(n) for n = 0 .. NDIMS (N/2)^2 (spectrum binning)
-    int64_t sqrt_len = 0;
     size_t partials_cap = 0;
     void *dstage = nullptr;          // transfer staging (length reals)
     // spectral Laplacian (axs_params.laplacian = 1): complex transform plan and
