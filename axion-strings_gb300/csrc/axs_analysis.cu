@@ -335,12 +335,25 @@ static void ensure_mask(Lattice *L) {
     if (!L->dcount) L->dcount = (int64_t *)dalloc(4 * sizeof(int64_t));
 }
 
+// A work buffer of at least `bytes` in the lattice's slot (allocated once, grown
+// when a call needs more), so repeated analysis calls do not allocate.
+static void *lattice_tmp(Lattice *L, int slot, size_t bytes) {
+    if (L->tmp_cap[slot] < bytes) {
+        dfree(L->tmp[slot]);
+        L->tmp[slot] = nullptr;
+        L->tmp_cap[slot] = 0;
+        L->tmp[slot] = dalloc(bytes);
+        L->tmp_cap[slot] = bytes;
+    }
+    return L->tmp[slot];
+}
+
 // Build the ascending list of flagged offsets from the device mask.
 static int64_t compact(Lattice *L) {
     int64_t nch = (L->length + kChunk - 1) / kChunk;
-    int64_t *counts = (int64_t *)dalloc((size_t)nch * sizeof(int64_t));
+    int64_t *counts = (int64_t *)lattice_tmp(L, 0, (size_t)nch * sizeof(int64_t));
     int64_t total = 0;
-    try {
+    {
         k_chunk_counts<<<(unsigned)nch, 256, 0, L->stream>>>(L->dmask, L->length, counts);
         k_scan<<<1, 1024, 0, L->stream>>>(counts, nch, L->dcount + 2);
         count_launches(2);
@@ -357,11 +370,7 @@ static int64_t compact(Lattice *L) {
         count_launches(1);
         AXS_CUDA(cudaGetLastError());
         AXS_CUDA(cudaStreamSynchronize(L->stream));
-    } catch (...) {
-        dfree(counts);
-        throw;
     }
-    dfree(counts);
     L->list_valid = true;
     return total;
 }
@@ -885,9 +894,9 @@ static void bin_spectrum(Lattice *L, const B &binner, int nbins, std::vector<dou
     const int64_t rows = L->p.NDIMS == 2 ? (int64_t)N : (int64_t)N * N;
     int nblk = (int)std::min<int64_t>((int64_t)num_sms() * per_sm, (rows + 3) / 4);   // whole rows per warp
     (void)half;
-    double *part = (double *)dalloc((size_t)nblk * 3 * nbins * sizeof(double) + (size_t)3 * nbins * sizeof(double));
+    double *part = (double *)lattice_tmp(L, 1, (size_t)nblk * 3 * nbins * sizeof(double) + (size_t)3 * nbins * sizeof(double));
     double *out = part + (size_t)nblk * 3 * nbins;
-    try {
+    {
         if (sm > 48 * 1024) {
             if (L->esz == 4) AXS_CUDA(cudaFuncSetAttribute(k_bin_runs<float, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
             else AXS_CUDA(cudaFuncSetAttribute(k_bin_runs<double, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -907,11 +916,7 @@ static void bin_spectrum(Lattice *L, const B &binner, int nbins, std::vector<dou
         nsum.assign(h.begin() + nbins, h.begin() + 2 * nbins);
         cnt.resize(nbins);
         for (int b = 0; b < nbins; ++b) cnt[b] = (unsigned long long)h[2 * (size_t)nbins + b];
-    } catch (...) {
-        dfree(part);
-        throw;
     }
-    dfree(part);
 }
 
 void powerspec(Lattice *L, int field, double *pk, double *ks, int *count) {
@@ -981,17 +986,11 @@ void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *c
     // n2 >= t_b^2 is n2 >= ceil(t_b^2)
     std::vector<int> thr(nbins, 0);
     for (int b = 1; b < nbins; ++b) { double t = exp(log(ratio) * (double)b / (double)nbins); thr[b] = (int)ceil(t * t); }
-    int *de2 = (int *)dalloc(nbins * sizeof(int));
+    int *de2 = (int *)lattice_tmp(L, 2, nbins * sizeof(int));
     std::vector<double> ps, ns;
     std::vector<unsigned long long> c;
-    try {
-        AXS_CUDA(cudaMemcpyAsync(de2, thr.data(), nbins * sizeof(int), cudaMemcpyHostToDevice, L->stream));
-        bin_spectrum(L, LogBinsI{de2, nbins}, nbins, ps, ns, c);
-    } catch (...) {
-        dfree(de2);
-        throw;
-    }
-    dfree(de2);
+    AXS_CUDA(cudaMemcpyAsync(de2, thr.data(), nbins * sizeof(int), cudaMemcpyHostToDevice, L->stream));
+    bin_spectrum(L, LogBinsI{de2, nbins}, nbins, ps, ns, c);   // synchronises before thr goes out of scope
     double Ld = (double)N * (double)L->p.space_step;
     double norm = pow(Ld, d) / pow((double)L->length, 2.0);
     for (int b = 0; b < nbins; ++b) {
@@ -1173,6 +1172,11 @@ void analysis_release(Lattice *L) {
     if (L->have_plan) cufftDestroy(L->plan_r2c);
     L->have_plan = false;
     dfree(L->dpartials); L->dpartials = nullptr;
+    for (int i = 0; i < 3; ++i) {
+        dfree(L->tmp[i]);
+        L->tmp[i] = nullptr;
+        L->tmp_cap[i] = 0;
+    }
 }
 
 }  // namespace axs

@@ -139,6 +139,10 @@ struct Lattice {
     double *dpartials = nullptr;     // reduction partials
     size_t partials_cap = 0;
     void *dstage = nullptr;          // transfer staging (length reals)
+    // small per-call work buffers of the analysis, kept between calls (grow only):
+    // 0 = string-finder chunk counts, 1 = spectrum block partials, 2 = bin thresholds
+    void *tmp[3] = {nullptr, nullptr, nullptr};
+    size_t tmp_cap[3] = {0, 0, 0};
     // spectral Laplacian (axs_params.laplacian = 1): complex transform plan and
     // the per-axis k^2 table (N doubles, then N floats)
     cufftHandle plan_c2c = 0;
