@@ -822,43 +822,59 @@ __global__ void k_gather_axion(const typename Cplx<T>::type *__restrict__ psi, c
 // site with k_sync_pi's arithmetic and never stored. Each thread marches one
 // (x, y) column through z with psi's z-neighbours in registers, so every psi
 // plane comes from DRAM once (the x and y neighbours are the neighbouring
-// threads' loads of the same plane, in L1); 20 B per site (psi, pih in, f out)
-// instead of 48 B for the two-kernel path. Blocks are 32 x 8 columns.
+// threads' loads of the same plane, from L1 or L2); 20 B per site (psi, pih
+// in, f out) instead of 48 B for the two-kernel path. Blocks are 32 x 8
+// columns. The column's psi and pih are loaded two planes ahead and the x/y
+// neighbours one plane ahead, so several planes of loads are in flight per
+// thread; offsets within a plane are 32-bit (N^2 < 2^31) to keep the float
+// thread within 64 registers (4 blocks per SM). N >= 4, so z + 3 < 2N.
 template <typename T>
-__global__ void __launch_bounds__(256) k_axion_zcol(const typename Cplx<T>::type *__restrict__ psi,
-                                                    const typename Cplx<T>::type *__restrict__ pih, T *__restrict__ dst,
-                                                    const double *clock, int N, double dt, double inv_dx2, double lambda,
-                                                    double T0sq3, int prs, int fresh, double tau) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_axion_zcol(const typename Cplx<T>::type *__restrict__ psi,
+                                                       const typename Cplx<T>::type *__restrict__ pih,
+                                                       T *__restrict__ dst, const double *clock, int N, double dt,
+                                                       double inv_dx2, double lambda, double T0sq3, int prs, int fresh,
+                                                       double tau) {
     typedef typename Cplx<T>::type C;
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
     if (x >= N || y >= N) return;
     const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs, 0);
     const T itau = (T)(1.0 / tau);
     const int64_t NN = (int64_t)N * N;
-    const int64_t col = (int64_t)y * N + x;
-    const int64_t xm = (int64_t)y * N + (x == 0 ? N - 1 : x - 1), xp = (int64_t)y * N + (x == N - 1 ? 0 : x + 1);
-    const int64_t ym = (int64_t)(y == 0 ? N - 1 : y - 1) * N + x, yp = (int64_t)(y == N - 1 ? 0 : y + 1) * N + x;
-    // the next plane's psi and pih are loaded one iteration ahead, so two
-    // planes of loads are in flight per thread
-    C zm = psi[(int64_t)(N - 1) * NN + col], zc = psi[col], zp = psi[(N > 1 ? NN : 0) + col];
-    C pc = pih[col];
+    const int col = y * N + x;
+    const int xm = y * N + (x == 0 ? N - 1 : x - 1) - col, xp = y * N + (x == N - 1 ? 0 : x + 1) - col;
+    const int ym = (y == 0 ? N - 1 : y - 1) * N + x - col, yp = (y == N - 1 ? 0 : y + 1) * N + x - col;
+    auto plane = [N](int z) { return z >= N ? z - N : z; };   // for z < 2N
+    // column values: psi planes z-1, z, z+1 in use, z+2 and z+3 in flight;
+    // pih plane z in use, z+1 and z+2 in flight; neighbours of plane z in use
+    // (loaded last iteration), those of z+1 in flight
+    C zm = psi[(int64_t)(N - 1) * NN + col], zc = psi[col];
+    C zp = psi[NN + col], zq = psi[2 * NN + col];
+    C pc = pih[col], pq = pih[NN + col];
+    C a, b, d, e;
+    if (!fresh) { a = psi[col + xm]; b = psi[col + xp]; d = psi[col + ym]; e = psi[col + yp]; }
     for (int z = 0; z < N; ++z) {
         const int64_t base = (int64_t)z * NN;
-        const int z2 = z + 2 >= N ? z + 2 - N : z + 2;
-        const C zpn = psi[(int64_t)z2 * NN + col];
-        const C pn = pih[(z + 1 == N ? 0 : base + NN) + col];
+        const int64_t b1 = (int64_t)plane(z + 1) * NN;
+        const C zr = psi[(int64_t)plane(z + 3) * NN + col];
+        const C pr = pih[(int64_t)plane(z + 2) * NN + col];
         C p = pc;
         if (!fresh) {   // a fresh state holds pi_0 itself (the reference's ker is zero)
-            const C a = psi[base + xm], b = psi[base + xp], d = psi[base + ym], e = psi[base + yp];
+            const C na = psi[b1 + col + xm], nb = psi[b1 + col + xp], nd = psi[b1 + col + ym], ne = psi[b1 + col + yp];
             const T L1 = lap7<T>(zc.x, a.x, b.x, d.x, e.x, zm.x, zp.x);
             const T L2 = lap7<T>(zc.y, a.y, b.y, d.y, e.y, zm.y, zp.y);
             sync_pi_site<T>(zc.x, zc.y, L1, L2, p.x, p.y, c);
+            a = na;
+            b = nb;
+            d = nd;
+            e = ne;
         }
         dst[base + col] = axion_f<T>(zc.x, zc.y, p.x, p.y, itau);
         zm = zc;
         zc = zp;
-        zp = zpn;
-        pc = pn;
+        zp = zq;
+        zq = zr;
+        pc = pq;
+        pq = pr;
     }
 }
 

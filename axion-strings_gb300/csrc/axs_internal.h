@@ -316,6 +316,14 @@ __device__ __forceinline__ T axion_f(T a, T b, T p1, T p2, T itau) {
     T r = sqrt(a * a + b * b);
     return r > (T)0 ? (b * p1 - a * p2) * itau / r : (T)0;
 }
+// Float fields: one rsqrtf (2 ulp) in place of a correctly rounded square
+// root and division; float spectra are compared to the double ones within
+// 1e-4, far above this.
+template <>
+__device__ __forceinline__ float axion_f<float>(float a, float b, float p1, float p2, float itau) {
+    const float r2 = a * a + b * b;
+    return r2 > 0.f ? (b * p1 - a * p2) * itau * rsqrtf(r2) : 0.f;
+}
 
 // Philox-4x32-10 (Salmon et al., SC'11) and Box-Muller; the deviate for
 // array a at offset m. Must agree with the oracle's definition.
