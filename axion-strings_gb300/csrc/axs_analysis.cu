@@ -609,17 +609,17 @@ struct RefBinsI {
     int half;
     __device__ __forceinline__ RefBinsI staged(double *) const { return *this; }
     static constexpr int kSmemTable = 0;
-    __device__ __forceinline__ int bin(int64_t n2) const {
-        if (n2 == 0 || n2 >= (int64_t)half * half) return -1;
+    __device__ __forceinline__ int bin(int n2) const {
+        if (n2 == 0 || n2 >= half * half) return -1;
         int s = (int)sqrtf((float)n2);
-        while ((int64_t)s * s > n2) --s;
-        while ((int64_t)(s + 1) * (s + 1) <= n2) ++s;
+        while (s * s > n2) --s;
+        while ((s + 1) * (s + 1) <= n2) ++s;
         return s - 1;
     }
     // bin of n2 >= the n2 that gave b (bins only grow along a row)
-    __device__ __forceinline__ int next(int b, int64_t n2) const {
-        if (b < 0 || n2 >= (int64_t)half * half) return bin(n2);
-        while ((int64_t)(b + 2) * (b + 2) <= n2) ++b;
+    __device__ __forceinline__ int next(int b, int n2) const {
+        if (b < 0 || n2 >= half * half) return bin(n2);
+        while ((b + 2) * (b + 2) <= n2) ++b;
         return b;
     }
 };
@@ -632,19 +632,19 @@ struct LogBinsI {
         return LogBinsI{t, nbins};
     }
     static constexpr int kSmemTable = 1;   // nbins ints fit in nbins doubles
-    __device__ __forceinline__ int bin(int64_t n2) const {
+    __device__ __forceinline__ int bin(int n2) const {
         if (n2 == 0) return -1;
         int lo = 0, hi = nbins - 1;
         while (lo < hi) {
             int mid = (lo + hi + 1) >> 1;
-            if ((int64_t)thr[mid] <= n2) lo = mid; else hi = mid - 1;
+            if (thr[mid] <= n2) lo = mid; else hi = mid - 1;
         }
         return lo;
     }
     // bin of n2 >= the n2 that gave b (bins only grow along a row)
-    __device__ __forceinline__ int next(int b, int64_t n2) const {
+    __device__ __forceinline__ int next(int b, int n2) const {
         if (b < 0) return bin(n2);
-        while (b + 1 < nbins && (int64_t)thr[b + 1] <= n2) ++b;
+        while (b + 1 < nbins && thr[b + 1] <= n2) ++b;
         return b;
     }
 };
@@ -668,6 +668,16 @@ __device__ __forceinline__ FF ff_shfl_up(FF a, int o) {
 }
 __device__ __forceinline__ double ff_to_double(FF a) { return (double)a.hi + (double)a.lo; }
 
+// Add x to a float-float histogram slot (a double-sized slot holding hi, lo):
+// the per-warp histograms stay in FP32 arithmetic, off GB300's FP64 pipe, and
+// are widened to double once per block. All values added are non-negative.
+__device__ __forceinline__ void ff_acc(double *slot, FF x) {
+    float2 *s = reinterpret_cast<float2 *>(slot);
+    const float2 h = *s;
+    const FF r = ff_add(FF{h.x, h.y}, x);
+    *s = make_float2(r.hi, r.lo);
+}
+
 template <typename T> __device__ __forceinline__ FF mode_power(const typename Cplx<T>::type &f);
 template <> __device__ __forceinline__ FF mode_power<float>(const float2 &f) { return FF{fmaf(f.x, f.x, f.y * f.y), 0.0f}; }
 template <> __device__ __forceinline__ FF mode_power<double>(const double2 &f) {
@@ -685,9 +695,11 @@ template <> __device__ __forceinline__ FF mode_power<double>(const double2 &f) {
 // one segmented scan of 5 shuffle steps), and its last run has a bin no other
 // lane's last run has. Every bin thus receives its sums in an order fixed by
 // the data: results are the same run to run and for an ensemble member alone.
-// Per-warp histograms, block partial rows and k_bin_final3 as before (three
-// rows: power, |n|, count).
-template <typename T, typename B>
+// Per-warp histograms (float-float slots), block partial rows in double and
+// k_bin_final3 as before (three rows: power, |n|, count). With KS false only the power row is summed (the
+// |n| and count rows, which depend on N and the bin edges alone, stay zero;
+// the power sums are the same bits either way).
+template <typename T, typename B, bool KS>
 __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *__restrict__ F, int N, int ndims,
                                                   B binner, int nbins,
                                                   double *__restrict__ partials) {
@@ -708,13 +720,14 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
     const int chunk = (nh + 31) / 32;
     const int lo = min(nh, lane * chunk), hi = min(nh, lo + chunk);
     for (int64_t r = (int64_t)blockIdx.x * 4 + w; r < rows; r += nwarps) {
-        int64_t c2;
+        // |n|^2 = ix^2 + fy^2 + fz^2 <= 3 (N/2)^2 < 2^24 for N <= 4096: int
+        int c2;
         if (ndims == 2) {
-            const int64_t fy = r < N / 2 ? r : r - N;
+            const int fy = r < N / 2 ? (int)r : (int)r - N;
             c2 = fy * fy;
         } else {
-            const int64_t iz = r / N, iy = r - iz * N;
-            const int64_t fz = iz < N / 2 ? iz : iz - N, fy = iy < N / 2 ? iy : iy - N;
+            const int iz = (int)r / N, iy = (int)r - iz * N;   // r < N^2
+            const int fz = iz < N / 2 ? iz : iz - N, fy = iy < N / 2 ? iy : iy - N;
             c2 = fy * fy + fz * fz;
         }
         const C *row = F + r * nh;
@@ -724,15 +737,17 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
         FF v{0.f, 0.f}, kk{0.f, 0.f}, fv{0.f, 0.f}, fk{0.f, 0.f};
         int c = 0, fc = 0;
         for (int ix = lo; ix < hi; ++ix) {
-            const int64_t n2 = (int64_t)ix * ix + c2;
+            const int n2 = ix * ix + c2;
             const int nb = bins.next(b, n2);
             if (nb != b) {
                 if (b >= 0) {
                     if (fb < 0) { fb = b; fv = v; fk = kk; fc = c; }
                     else {   // a run inside the slice: no other lane has this bin in this row
-                        hp[b] += ff_to_double(v);
-                        hk[b] += ff_to_double(kk);
-                        hc[b] += (double)c;
+                        ff_acc(hp + b, v);
+                        if constexpr (KS) {
+                            ff_acc(hk + b, kk);
+                            ff_acc(hc + b, FF{(float)c, 0.f});
+                        }
                     }
                 }
                 b = nb;
@@ -743,15 +758,17 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
                 const int wt = (ix == 0 || 2 * ix == N) ? 1 : 2;
                 const float fw = (float)wt;   // x1 or x2: exact in float-float
                 const FF p = mode_power<T>(stage[ix]);
-                // |n| = sqrt(n2) as float-float: hi = sqrtf (correctly rounded), the residual
-                // n2 - hi^2 is exact in float (that of a correctly rounded square
-                // root always is) and lo = residual / (2 hi); n2 < 2^24 is exact in float
-                const float n2f = (float)n2;
-                const float shi = sqrtf(n2f);
-                const float2 sq = make_float2(shi, shi > 0.0f ? __fdiv_rn(fmaf(-shi, shi, n2f), 2.0f * shi) : 0.0f);
                 v = ff_add(v, FF{fw * p.hi, fw * p.lo});
-                kk = ff_add(kk, FF{fw * sq.x, fw * sq.y});
-                c += wt;
+                if constexpr (KS) {
+                    // |n| = sqrt(n2) as float-float: hi = sqrtf (correctly rounded), the residual
+                    // n2 - hi^2 is exact in float (that of a correctly rounded square
+                    // root always is) and lo = residual / (2 hi); n2 < 2^24 is exact in float
+                    const float n2f = (float)n2;
+                    const float shi = sqrtf(n2f);
+                    const float2 sq = make_float2(shi, shi > 0.0f ? __fdiv_rn(fmaf(-shi, shi, n2f), 2.0f * shi) : 0.0f);
+                    kk = ff_add(kk, FF{fw * sq.x, fw * sq.y});
+                    c += wt;
+                }
             }
         }
         FF lv{0.f, 0.f}, lk{0.f, 0.f};
@@ -765,25 +782,36 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int ob = __shfl_up_sync(0xffffffffu, fb, o);
-            const FF ov = ff_shfl_up(fv, o), ok = ff_shfl_up(fk, o);
-            const int oc = __shfl_up_sync(0xffffffffu, fc, o);
+            const FF ov = ff_shfl_up(fv, o);
+            FF ok{0.f, 0.f};
+            int oc = 0;
+            if constexpr (KS) {
+                ok = ff_shfl_up(fk, o);
+                oc = __shfl_up_sync(0xffffffffu, fc, o);
+            }
             if (lane >= o && fb >= 0 && ob == fb) {
                 fv = ff_add(ov, fv);
-                fk = ff_add(ok, fk);
-                fc += oc;
+                if constexpr (KS) {
+                    fk = ff_add(ok, fk);
+                    fc += oc;
+                }
             }
         }
         const int nextb = __shfl_down_sync(0xffffffffu, fb, 1);
         if (fb >= 0 && (lane == 31 || nextb != fb)) {
-            hp[fb] += ff_to_double(fv);
-            hk[fb] += ff_to_double(fk);
-            hc[fb] += (double)fc;
+            ff_acc(hp + fb, fv);
+            if constexpr (KS) {
+                ff_acc(hk + fb, fk);
+                ff_acc(hc + fb, FF{(float)fc, 0.f});
+            }
         }
         __syncwarp();
         if (lb >= 0) {
-            hp[lb] += ff_to_double(lv);
-            hk[lb] += ff_to_double(lk);
-            hc[lb] += (double)lc;
+            ff_acc(hp + lb, lv);
+            if constexpr (KS) {
+                ff_acc(hk + lb, lk);
+                ff_acc(hc + lb, FF{(float)lc, 0.f});
+            }
         }
         __syncwarp();
     }
@@ -792,7 +820,10 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             double acc = 0.0;
-            for (int ww = 0; ww < 4; ++ww) acc += hist[(size_t)ww * 3 * nbins + (size_t)q * nbins + bn];
+            for (int ww = 0; ww < 4; ++ww) {
+                const float2 h = reinterpret_cast<const float2 *>(hist)[(size_t)ww * 3 * nbins + (size_t)q * nbins + bn];
+                acc += (double)h.x + (double)h.y;
+            }
             partials[((int64_t)blockIdx.x * 3 + q) * nbins + bn] = acc;
         }
     }
@@ -897,9 +928,15 @@ static void exec_r2c(Lattice *L) {
 }
 
 // Bin the current fft_out; returns per-bin sums (pk, |n|) and weighted counts.
+// The |n| sums and counts of a binning (kind, edges) are computed by its first
+// call and reused afterwards, when the kernel sums the power alone.
 template <typename B>
-static void bin_spectrum(Lattice *L, const B &binner, int nbins, std::vector<double> &psum, std::vector<double> &nsum,
-                         std::vector<unsigned long long> &cnt) {
+static void bin_spectrum(Lattice *L, const B &binner, int kind, const std::vector<int> &edges, int nbins,
+                         std::vector<double> &psum, std::vector<double> &nsum, std::vector<unsigned long long> &cnt) {
+    const Lattice::BinGeom *geom = nullptr;
+    for (const Lattice::BinGeom &g : L->bin_geom)
+        if (g.kind == kind && g.edges == edges) geom = &g;
+    const bool ks = geom == nullptr;
     int N = L->p.N;
     int64_t half = (L->p.NDIMS == 2 ? (int64_t)N : (int64_t)N * N) * (N / 2 + 1);
     const int nh = N / 2 + 1;
@@ -913,14 +950,16 @@ static void bin_spectrum(Lattice *L, const B &binner, int nbins, std::vector<dou
     double *part = (double *)lattice_tmp(L, 1, (size_t)nblk * 3 * nbins * sizeof(double) + (size_t)3 * nbins * sizeof(double));
     double *out = part + (size_t)nblk * 3 * nbins;
     {
-        if (sm > 48 * 1024) {
-            if (L->esz == 4) AXS_CUDA(cudaFuncSetAttribute(k_bin_runs<float, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            else AXS_CUDA(cudaFuncSetAttribute(k_bin_runs<double, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        auto kern = L->esz == 4 ? (ks ? (const void *)k_bin_runs<float, B, true> : (const void *)k_bin_runs<float, B, false>)
+                                : (ks ? (const void *)k_bin_runs<double, B, true> : (const void *)k_bin_runs<double, B, false>);
+        if (sm > 48 * 1024) AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        if (L->esz == 4) {
+            if (ks) k_bin_runs<float, B, true><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part);
+            else k_bin_runs<float, B, false><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part);
+        } else {
+            if (ks) k_bin_runs<double, B, true><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part);
+            else k_bin_runs<double, B, false><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part);
         }
-        if (L->esz == 4)
-            k_bin_runs<float, B><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part);
-        else
-            k_bin_runs<double, B><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part);
         AXS_CUDA(cudaGetLastError());
         k_bin_final3<<<nbins, 256, 0, L->stream>>>(part, nblk, nbins, out);
         AXS_CUDA(cudaGetLastError());
@@ -929,9 +968,19 @@ static void bin_spectrum(Lattice *L, const B &binner, int nbins, std::vector<dou
         AXS_CUDA(cudaMemcpyAsync(h.data(), out, h.size() * sizeof(double), cudaMemcpyDeviceToHost, L->stream));
         AXS_CUDA(cudaStreamSynchronize(L->stream));
         psum.assign(h.begin(), h.begin() + nbins);
-        nsum.assign(h.begin() + nbins, h.begin() + 2 * nbins);
-        cnt.resize(nbins);
-        for (int b = 0; b < nbins; ++b) cnt[b] = (unsigned long long)h[2 * (size_t)nbins + b];
+        if (ks) {
+            Lattice::BinGeom g;
+            g.kind = kind;
+            g.edges = edges;
+            g.nsum.assign(h.begin() + nbins, h.begin() + 2 * nbins);
+            g.cnt.resize(nbins);
+            for (int b = 0; b < nbins; ++b) g.cnt[b] = (unsigned long long)h[2 * (size_t)nbins + b];
+            if (L->bin_geom.size() >= 8) L->bin_geom.erase(L->bin_geom.begin());
+            L->bin_geom.push_back(std::move(g));
+            geom = &L->bin_geom.back();
+        }
+        nsum = geom->nsum;
+        cnt = geom->cnt;
     }
 }
 
@@ -951,7 +1000,7 @@ void powerspec(Lattice *L, int field, double *pk, double *ks, int *count) {
     int nb = N / 2;
     std::vector<double> ps, ns;
     std::vector<unsigned long long> c;
-    bin_spectrum(L, RefBinsI{N / 2}, nb, ps, ns, c);
+    bin_spectrum(L, RefBinsI{N / 2}, 0, std::vector<int>{nb}, nb, ps, ns, c);
     float Lf = N * L->p.space_step;                     // pk_estimation.cpp:41
     for (int b = 0; b < nb; ++b) {                      // pk_estimation.cpp:117-121 / 195-199
         double k = ns[b] / (double)(int)c[b];
@@ -1006,7 +1055,7 @@ void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *c
     std::vector<double> ps, ns;
     std::vector<unsigned long long> c;
     AXS_CUDA(cudaMemcpyAsync(de2, thr.data(), nbins * sizeof(int), cudaMemcpyHostToDevice, L->stream));
-    bin_spectrum(L, LogBinsI{de2, nbins}, nbins, ps, ns, c);   // synchronises before thr goes out of scope
+    bin_spectrum(L, LogBinsI{de2, nbins}, 1, thr, nbins, ps, ns, c);   // synchronises before thr goes out of scope
     double Ld = (double)N * (double)L->p.space_step;
     double norm = pow(Ld, d) / pow((double)L->length, 2.0);
     for (int b = 0; b < nbins; ++b) {

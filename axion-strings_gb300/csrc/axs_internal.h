@@ -143,6 +143,17 @@ struct Lattice {
     // 0 = string-finder chunk counts, 1 = spectrum block partials, 2 = bin thresholds
     void *tmp[3] = {nullptr, nullptr, nullptr};
     size_t tmp_cap[3] = {0, 0, 0};
+    // per-bin |n| sums and mode counts of the spectrum binnings used so far:
+    // they depend on N and the bin edges alone, so later spectra with the same
+    // edges bin the power only (kind 0 = linear bins of output_powerspec,
+    // 1 = log bins of the axion spectrum; edges identify the binning)
+    struct BinGeom {
+        int kind;
+        std::vector<int> edges;
+        std::vector<double> nsum;
+        std::vector<unsigned long long> cnt;
+    };
+    std::vector<BinGeom> bin_geom;
     // spectral Laplacian (axs_params.laplacian = 1): complex transform plan and
     // the per-axis k^2 table (N doubles, then N floats)
     cufftHandle plan_c2c = 0;
