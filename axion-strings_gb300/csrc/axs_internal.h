@@ -78,6 +78,19 @@ struct ZLat {
     int debug_tx_excess;     // test-only: bytes the first load of each item expects but never gets
 };
 
+// The table entry that owns work item `item`: the last entry whose item_base
+// is <= item (item bases ascend from 0). Binary search: an ensemble table has
+// up to hundreds of entries, ~1 KB apart (tensor maps), read per item.
+__device__ __forceinline__ int find_lat(const ZLat *__restrict__ lats, int nlat, int64_t item) {
+    int lo = 0, hi = nlat - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (lats[mid].item_base <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // A captured interval is keyed by its length and the state it starts from
 // (current psi buffer, and where the momentum lives); it ends in a fixed state.
 struct GraphKey {

@@ -336,8 +336,7 @@ __global__ void __launch_bounds__(256) k_zmarch(const ZLat *__restrict__ lats, i
         const int64_t item = *item_bc;
         if (item >= total_items) break;
         // ---- decode the item
-        int li = 0;
-        while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+        const int li = find_lat(lats, nlat, item);
         const ZLat &Lt = lats[li];
         const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
         const int64_t local = item - Lt.item_base;
@@ -558,8 +557,7 @@ __global__ void __launch_bounds__(Z2Cfg<T, TY, TXMAX, S>::NT)
                 items[k & 1] = item;
                 mbar_arrive(smem_u32(&ifull[k & 1]));
                 if (item >= total_items) break;
-                int li = 0;
-                while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+                const int li = find_lat(lats, nlat, item);
                 const ZLat &Lt = lats[li];
                 const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
                 const int64_t local = item - Lt.item_base;
@@ -621,8 +619,7 @@ __global__ void __launch_bounds__(Z2Cfg<T, TY, TXMAX, S>::NT)
             __syncwarp();
             if (lane == 0) mbar_arrive(smem_u32(&iempty[k & 1]));
             if (item >= total_items) break;
-            int li = 0;
-            while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+            const int li = find_lat(lats, nlat, item);
             const ZLat &Lt = lats[li];
             const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
             const int64_t local = item - Lt.item_base;
@@ -844,8 +841,7 @@ __global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
                 items[k & 1] = item;
                 mbar_arrive(smem_u32(&ifull[k & 1]));
                 if (item >= total_items) break;
-                int li = 0;
-                while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+                const int li = find_lat(lats, nlat, item);
                 const ZLat &Lt = lats[li];
                 const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
                 const int64_t local = item - Lt.item_base;
@@ -925,8 +921,7 @@ __global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
             __syncwarp();
             if (lane == 0) mbar_arrive(smem_u32(&iempty[k & 1]));
             if (item >= total_items) break;
-            int li = 0;
-            while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+            const int li = find_lat(lats, nlat, item);
             const ZLat &Lt = lats[li];
             const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
             const int64_t local = item - Lt.item_base;
@@ -1926,7 +1921,7 @@ void lattice_autotune(Lattice *L) {
         log.push_back({c, ms});
         if (ms < best_ms) { best_ms = ms; best = c; }
     }
-    const int zchunks[] = {32, 64, 128};
+    const int zchunks[] = {32, 64, 128, 256};
     for (int v = 0; v < kNumZVariants; ++v) {
         if (!variant_fits(kZVariants[v], L->p, L->esz)) continue;
         const bool two = two_step(v);
@@ -2085,7 +2080,7 @@ void ensemble_autotune(Ensemble *E) {
     int reps = 6;
     StepConfig best = E->cfg;
     double best_ms = 1e30;
-    const int zchunks[] = {32, 64, 128};
+    const int zchunks[] = {32, 64, 128, 256};   // 256: whole columns of every member up to 256^3
     for (int v = 0; v < kNumZVariants; ++v) {
         if (!ensemble_variant_ok(E, v)) continue;
         const bool two = two_step(v);
@@ -2094,6 +2089,7 @@ void ensemble_autotune(Ensemble *E) {
             c.kind = 1;
             c.variant = v;
             c.zchunk = zc;
+            c.tx = variant_tx(kZVariants[v], E->members[0]->p.N, E->members[0]->esz);
             E->cfg = c;
             ensemble_table(E, 0.f, true);
             double ms = time_launches(E->stream, reps, [&] {

@@ -81,8 +81,7 @@ __global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R>::NT)
                 items[k & 1] = item;
                 mbar_arrive(smem_u32(&ifull[k & 1]));
                 if (item >= total_items) break;
-                int li = 0;
-                while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+                const int li = find_lat(lats, nlat, item);
                 const ZLat &Lt = lats[li];
                 const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
                 const int64_t local = item - Lt.item_base;
@@ -149,8 +148,7 @@ __global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R>::NT)
             __syncwarp();
             if (lane == 0) mbar_arrive(smem_u32(&iempty[k & 1]));
             if (item >= total_items) break;
-            int li = 0;
-            while (li + 1 < nlat && lats[li + 1].item_base <= item) ++li;
+            const int li = find_lat(lats, nlat, item);
             const ZLat &Lt = lats[li];
             const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
             const int64_t local = item - Lt.item_base;
