@@ -1182,6 +1182,10 @@ static const ZVariant kZVariants[] = {
     {2, 8, 64, 5, 8, -1},  {3, 8, 64, 4, 4, 16},  {3, 8, 64, 5, 4, 16},  {3, 4, 128, 5, 4, 9},
     {4, 8, 128, 6, 8, -1, 2},  {4, 4, 128, 6, 8, -1, 2},  {4, 8, 64, 8, 8, -1, 3},  {4, 4, 128, 8, 8, -1, 3},
     {4, 4, 128, 10, 8, -1, 4}, {4, 8, 64, 10, 8, -1, 4},  {4, 4, 64, 10, 8, -1, 4},
+    // 27-29: 32-wide tiles with two consumer warps (up to 4 CTAs per SM); 32
+    // divides every N that is a multiple of 32, so ensembles of mixed sizes
+    // keep every tile full
+    {2, 8, 32, 5, 8, -1},  {3, 8, 32, 4, 2, 27},  {3, 8, 32, 5, 2, 27},
 };
 static const int kNumZVariants = sizeof(kZVariants) / sizeof(kZVariants[0]);
 
@@ -1326,6 +1330,9 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
         AXS_ZV3(17, 8, 64, 4, 4, 1)
         AXS_ZV3(18, 8, 64, 5, 4, 1)
         AXS_ZV3(19, 4, 128, 5, 4, 1)
+        AXS_ZV2(27, 8, 32, 5)
+        AXS_ZV3(28, 8, 32, 4, 2, 1)
+        AXS_ZV3(29, 8, 32, 5, 2, 1)
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
 #undef AXS_ZV
@@ -1374,6 +1381,9 @@ static void prepare_zmarch(int esz, int variant) {
         AXS_ZP3(17, 8, 64, 4, 4, 1)
         AXS_ZP3(18, 8, 64, 5, 4, 1)
         AXS_ZP3(19, 4, 128, 5, 4, 1)
+        AXS_ZP2(27, 8, 32, 5)
+        AXS_ZP3(28, 8, 32, 4, 2, 1)
+        AXS_ZP3(29, 8, 32, 5, 2, 1)
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
     if (kZVariants[variant].gen == 3) prepare_zmarch(esz, kZVariants[variant].partner);
