@@ -741,7 +741,7 @@ __global__ void __launch_bounds__(Z2Cfg<T, TY, TXMAX, S>::NT)
 // different buffers: a neighbouring tile may already have stored pih_{n+1}
 // where this tile still reads pih_{n-1} in its halo.
 
-template <int TY, int TXMAX, int S, int NCW>
+template <int TY, int TXMAX, int S, int NCW, int MIDN = 2>
 struct Z3Cfg {
     static constexpr int CS = 8;                                  // bytes per complex float site
     static constexpr int NC = NCW * 32;                           // consumer threads
@@ -760,7 +760,7 @@ struct Z3Cfg {
     static constexpr int MB = (TY + 2) * TXMAX * CS;              // psi_{n+1} band, rows y0-1 .. y0+TY
     static constexpr int MID = (MB + 2 * TY * CS + 127) / 128 * 128;   // + columns x0-1 and x0+tx
     static constexpr int MID_OFF = S * SLOT;
-    static constexpr int BAR_OFF = MID_OFF + 2 * MID;
+    static constexpr int BAR_OFF = MID_OFF + MIDN * MID;          // MIDN planes of the psi_{n+1} ring
     static constexpr int SMEM = BAR_OFF + 256;
 };
 
@@ -800,10 +800,14 @@ __device__ __forceinline__ float2 update_site(float2 c, float2 xm, float2 xp, fl
     return o;
 }
 
-template <int TY, int TXMAX, int S, int NCW, int UNR>
-__global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
-    k_zmarch_2step(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity, int *derr) {
-    typedef Z3Cfg<TY, TXMAX, S, NCW> K;
+// LEAN: the centre psi_n of the in-plane slot and psi_{n+1} of planes m-1 and
+// m-2 are read back from shared memory (a three-plane psi_{n+1} ring) instead
+// of being carried in registers, so the thread fits 128 registers and three
+// CTAs share an SM (12 consumer warps instead of 8). Same arithmetic, same bits.
+template <int TY, int TXMAX, int S, int NCW, int UNR, bool LEAN>
+__device__ __forceinline__ void zmarch_2step_body(const ZLat *__restrict__ lats, int nlat, int64_t total_items,
+                                                  int *counters, int parity, int *derr) {
+    typedef Z3Cfg<TY, TXMAX, S, NCW, LEAN ? 3 : 2> K;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + K::BAR_OFF);
     uint64_t *empty = full + S;
@@ -911,6 +915,7 @@ __global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
         const int cid = tid;   // 0 .. NC-1
         int64_t q0 = 0;        // loads of the items before the current one
         int64_t g = 0;         // iterations done (completed phases of midbar)
+        int gm = 0;            // g mod 3 (LEAN: plane of the psi_{n+1} ring written next)
         for (int64_t k = 0;; ++k) {
             int w = warp_wait(smem_u32(&ifull[k & 1]), (uint32_t)((k >> 1) & 1), abort_flag);
             if (w) {
@@ -1025,17 +1030,17 @@ __global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
                 for (int j = 0; j < K::MAXV; ++j)
                     if (cid + j * K::NC < nvec) {
                         a_zm[j] = ldb4(B0, t_c[j]);
-                        a_c[j] = ldb4(B1, t_c[j]);
+                        if constexpr (!LEAN) a_c[j] = ldb4(B1, t_c[j]);
                     }
 #pragma unroll
                 for (int j = 0; j < K::MAXR; ++j)
                     if (cid + j * K::NC < nring) {
                         r_zm[j] = ldb4(B0, r_c[j]);
-                        r_cv[j] = ldb4(B1, r_c[j]);
+                        if constexpr (!LEAN) r_cv[j] = ldb4(B1, r_c[j]);
                     }
                 if (has_col) {
                     c_zm = ldb2(B0, c_z);
-                    c_cv = ldb2(B1, c_z);
+                    if constexpr (!LEAN) c_cv = ldb2(B1, c_z);
                 }
             }
             __syncwarp();
@@ -1056,40 +1061,45 @@ __global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
                     break;
                 }
                 const unsigned char *Sc = smem + sc * K::SLOT, *Sn = smem + sn * K::SLOT;
-                unsigned char *Mw = smem + K::MID_OFF + (int)(g & 1) * K::MID;
+                // psi_{n+1} ring: plane m is written, m-1 (and in LEAN mode m-2) read
+                const int gw = LEAN ? gm : (int)(g & 1);
+                unsigned char *Mw = smem + K::MID_OFF + gw * K::MID;
                 float4 b_new[K::MAXV], p_new[K::MAXV];
 #pragma unroll
                 for (int j = 0; j < K::MAXV; ++j) {
                     b_new[j] = p_new[j] = zero4;
                     if (cid + j * K::NC >= nvec) continue;
                     const float4 zp = ldb4(Sn, t_c[j]);
+                    const float4 ac = LEAN ? ldb4(Sc, t_c[j]) : a_c[j];
                     const float4 up = ldb4(Sc, t_c[j] - txb), dn = ldb4(Sc, t_c[j] + txb);
                     float4 p = ldb4(Sc, K::QB_OFF + t_c[j] - txb);
-                    const float4 o = update_vec2(a_c[j], a_zm[j], zp, up, dn, ldb2(Sc, t_l[j]), ldb2(Sc, t_r[j]), p, cf1);
+                    const float4 o = update_vec2(ac, a_zm[j], zp, up, dn, ldb2(Sc, t_l[j]), ldb2(Sc, t_r[j]), p, cf1);
                     *reinterpret_cast<float4 *>(Mw + t_c[j] - txb) = o;
                     b_new[j] = o;
                     p_new[j] = p;
-                    a_zm[j] = a_c[j];
-                    a_c[j] = zp;
+                    a_zm[j] = ac;
+                    if constexpr (!LEAN) a_c[j] = zp;
                 }
 #pragma unroll
                 for (int j = 0; j < K::MAXR; ++j) {
                     if (cid + j * K::NC >= nring) continue;
                     const float4 zp = ldb4(Sn, r_c[j]);
+                    const float4 rc = LEAN ? ldb4(Sc, r_c[j]) : r_cv[j];
                     const float4 up = ldb4(Sc, r_c[j] - txb), dn = ldb4(Sc, r_c[j] + txb);
                     float4 p = ldb4(Sc, K::QB_OFF + r_c[j] - txb);
-                    const float4 o = update_vec2(r_cv[j], r_zm[j], zp, up, dn, ldb2(Sc, r_l[j]), ldb2(Sc, r_r[j]), p, cf1);
+                    const float4 o = update_vec2(rc, r_zm[j], zp, up, dn, ldb2(Sc, r_l[j]), ldb2(Sc, r_r[j]), p, cf1);
                     *reinterpret_cast<float4 *>(Mw + r_c[j] - txb) = o;
-                    r_zm[j] = r_cv[j];
-                    r_cv[j] = zp;
+                    r_zm[j] = rc;
+                    if constexpr (!LEAN) r_cv[j] = zp;
                 }
                 if (has_col) {
                     const float2 zp = ldb2(Sn, c_z);
+                    const float2 cc = LEAN ? ldb2(Sc, c_z) : c_cv;
                     float2 p = ldb2(Sc, c_q);
-                    *reinterpret_cast<float2 *>(Mw + c_m) = update_site(c_cv, ldb2(Sc, c_xm), ldb2(Sc, c_xp), ldb2(Sc, c_ym),
+                    *reinterpret_cast<float2 *>(Mw + c_m) = update_site(cc, ldb2(Sc, c_xm), ldb2(Sc, c_xp), ldb2(Sc, c_ym),
                                                                         ldb2(Sc, c_yp), c_zm, zp, p, cf1);
-                    c_zm = c_cv;
-                    c_cv = zp;
+                    c_zm = cc;
+                    if constexpr (!LEAN) c_cv = zp;
                 }
                 // this warp is done with load i+1; at the last plane also with load i+2
                 __syncwarp();
@@ -1099,14 +1109,17 @@ __global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
                 }
                 // stage 2 on plane m-1 = za-2+i (the planes za .. zb-1)
                 if (i >= 2) {
-                    const unsigned char *Mr = smem + K::MID_OFF + (int)((g - 1) & 1) * K::MID;
+                    const int gr = LEAN ? (gm == 0 ? 2 : gm - 1) : (int)((g - 1) & 1);   // plane m-1
+                    const unsigned char *Mr = smem + K::MID_OFF + gr * K::MID;
+                    const unsigned char *Mrr = smem + K::MID_OFF + (gr == 0 ? 2 : gr - 1) * K::MID;   // m-2 (LEAN)
 #pragma unroll
                     for (int j = 0; j < K::MAXV; ++j) {
                         if (cid + j * K::NC >= nvec) continue;
                         const int mc = t_c[j] - txb;
                         const float4 up = ldb4(Mr, mc - txb), dn = ldb4(Mr, mc + txb);
+                        const float4 bc = LEAN ? ldb4(Mr, mc) : b_m1[j], bz = LEAN ? ldb4(Mrr, mc) : b_m2[j];
                         float4 p = p_m1[j];
-                        const float4 o = update_vec2(b_m1[j], b_m2[j], b_new[j], up, dn, ldb2(Mr, m_l[j]), ldb2(Mr, m_r[j]), p, cf2);
+                        const float4 o = update_vec2(bc, bz, b_new[j], up, dn, ldb2(Mr, m_l[j]), ldb2(Mr, m_r[j]), p, cf2);
                         st4(&pih_out[g_off[j]], p);
                         st4(&psi_out[g_off[j]], o);
                         g_off[j] += NN;
@@ -1114,8 +1127,10 @@ __global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
                 }
 #pragma unroll
                 for (int j = 0; j < K::MAXV; ++j) {
-                    b_m2[j] = b_m1[j];
-                    b_m1[j] = b_new[j];
+                    if constexpr (!LEAN) {
+                        b_m2[j] = b_m1[j];
+                        b_m1[j] = b_new[j];
+                    }
                     p_m1[j] = p_new[j];
                 }
                 // plane m of the psi_{n+1} ring is complete before anyone reads it;
@@ -1124,6 +1139,7 @@ __global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
                 if (lane == 0) mbar_arrive(smem_u32(midbar));
                 w = warp_wait(smem_u32(midbar), (uint32_t)(g & 1), abort_flag);
                 ++g;
+                gm = gm == 2 ? 0 : gm + 1;
                 if (w) {
                     if (w == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
                     ok = false;
@@ -1146,6 +1162,25 @@ __global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
             __threadfence();
         }
     }
+}
+
+template <int TY, int TXMAX, int S, int NCW, int UNR>
+__global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
+    k_zmarch_2step(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity, int *derr) {
+    zmarch_2step_body<TY, TXMAX, S, NCW, UNR, false>(lats, nlat, total_items, counters, parity, derr);
+}
+// 128 registers: with one producer warp per CTA, three CTAs fit the 16K
+// registers of each SM sub-partition (at most four warps each)
+template <int TY, int TXMAX, int S, int NCW>
+__global__ void __maxnreg__(128)
+    k_zmarch_2step_lean(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity,
+                        int *derr) {
+    zmarch_2step_body<TY, TXMAX, S, NCW, 1, true>(lats, nlat, total_items, counters, parity, derr);
+}
+template <int TY, int TXMAX, int S, int NCW, int UNR, bool LEAN>
+static void (*zm3_kernel())(const ZLat *, int, int64_t, int *, int, int *) {
+    if constexpr (LEAN) return k_zmarch_2step_lean<TY, TXMAX, S, NCW>;
+    else return k_zmarch_2step<TY, TXMAX, S, NCW, UNR>;
 }
 
 // ============================================================== host side
@@ -1172,7 +1207,7 @@ static int grid_for(int64_t len, int threads = 256) {
 // interval runs on the gen-2 `partner` with the same tile and launch table.
 // gen 4: k_zmarch2r (stencil radius r = 2..4, axs_step_r.cu).
 struct ZVariant {
-    int gen, ty, txmax, slots, ncw, partner, r;
+    int gen, ty, txmax, slots, ncw, partner, r, lean;
 };
 static const ZVariant kZVariants[] = {
     {1, 8, 128, 4, 0, -1}, {1, 8, 128, 5, 0, -1}, {1, 16, 128, 4, 0, -1}, {1, 4, 256, 4, 0, -1},
@@ -1186,6 +1221,9 @@ static const ZVariant kZVariants[] = {
     // divides every N that is a multiple of 32, so ensembles of mixed sizes
     // keep every tile full
     {2, 8, 32, 5, 8, -1},  {3, 8, 32, 4, 2, 27},  {3, 8, 32, 5, 2, 27},
+    // 30-31: LEAN two-step (centre values re-read from shared memory, 128
+    // registers, one more CTA per SM)
+    {3, 8, 64, 4, 4, 16, 0, 1},  {3, 8, 32, 4, 2, 27, 0, 1},
 };
 static const int kNumZVariants = sizeof(kZVariants) / sizeof(kZVariants[0]);
 
@@ -1196,8 +1234,8 @@ std::string StepConfig::describe() const {
     char b[200];
     if (kind == 0) snprintf(b, sizeof b, "generic per-site kernel");
     else if (two_step(variant))
-        snprintf(b, sizeof b, "TMA z-march variant %d (two steps per pass, halo depth 2; odd step on variant %d), tx=%d, zchunk=%d",
-                 variant, kZVariants[variant].partner, tx, zchunk);
+        snprintf(b, sizeof b, "TMA z-march variant %d (two steps per pass, halo depth 2%s; odd step on variant %d), tx=%d, zchunk=%d",
+                 variant, kZVariants[variant].lean ? ", lean" : "", kZVariants[variant].partner, tx, zchunk);
     else if (variant >= 0 && variant < kNumZVariants && kZVariants[variant].gen == 4)
         snprintf(b, sizeof b, "TMA z-march variant %d (stencil radius %d), tx=%d, zchunk=%d", variant,
                  kZVariants[variant].r, tx, zchunk);
@@ -1259,30 +1297,37 @@ static void launch_zmarch2_t(const ZLat *d, int nlat, int64_t items, int *counte
     count_launches(1);
 }
 
-template <int TY, int TXMAX, int S, int NCW, int UNR>
+template <int TY, int TXMAX, int S, int NCW, int UNR, bool LEAN>
 static int prepare_zmarch3_t() {
-    typedef Z3Cfg<TY, TXMAX, S, NCW> K;
+    typedef Z3Cfg<TY, TXMAX, S, NCW, LEAN ? 3 : 2> K;
     static int occ = -1;
     if (occ < 0) {
-        AXS_CUDA(cudaFuncSetAttribute(k_zmarch_2step<TY, TXMAX, S, NCW, UNR>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
+        const auto kern = zm3_kernel<TY, TXMAX, S, NCW, UNR, LEAN>();
+        AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
         int o = 0;
-        AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_zmarch_2step<TY, TXMAX, S, NCW, UNR>, K::NT,
-                                                               K::SMEM));
-        if (o < 1) fail(AXS_ERR_CUDA, "two-step z-march kernel does not fit on an SM");
+        AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, K::NT, K::SMEM));
+        if (o < 1) {
+            cudaFuncAttributes fa;
+            AXS_CUDA(cudaFuncGetAttributes(&fa, kern));
+            fail(AXS_ERR_CUDA,
+                 "two-step z-march kernel <%d,%d,%d,%d,%d,%d> does not fit on an SM (%d threads x %d registers, "
+                 "%d B dynamic shared memory of %d allowed, %d B static, max %d threads per block)",
+                 TY, TXMAX, S, NCW, UNR, (int)LEAN, K::NT, fa.numRegs, K::SMEM, fa.maxDynamicSharedSizeBytes,
+                 (int)fa.sharedSizeBytes, fa.maxThreadsPerBlock);
+        }
         occ = o;
     }
     return occ;
 }
 
-template <int TY, int TXMAX, int S, int NCW, int UNR>
+template <int TY, int TXMAX, int S, int NCW, int UNR, bool LEAN>
 static void launch_zmarch3_t(const ZLat *d, int nlat, int64_t items, int *counters, int parity, int *derr,
                              cudaStream_t st, int ctas_per_sm) {
-    typedef Z3Cfg<TY, TXMAX, S, NCW> K;
-    int occ = prepare_zmarch3_t<TY, TXMAX, S, NCW, UNR>();
+    typedef Z3Cfg<TY, TXMAX, S, NCW, LEAN ? 3 : 2> K;
+    int occ = prepare_zmarch3_t<TY, TXMAX, S, NCW, UNR, LEAN>();
     int per = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ) : occ;
     int64_t grid = std::min<int64_t>((int64_t)per * num_sms(), items);
-    k_zmarch_2step<TY, TXMAX, S, NCW, UNR><<<(int)grid, K::NT, K::SMEM, st>>>(d, nlat, items, counters, parity, derr);
+    zm3_kernel<TY, TXMAX, S, NCW, UNR, LEAN>()<<<(int)grid, K::NT, K::SMEM, st>>>(d, nlat, items, counters, parity, derr);
     AXS_CUDA(cudaGetLastError());
     count_launches(1);
 }
@@ -1307,7 +1352,7 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
 #define AXS_ZV3(I, TY, TX, S, W, U)                                                                       \
     case I:                                                                                               \
         if (esz != 4) fail(AXS_ERR_ARG, "two-step z-march variant %d needs complex float fields", variant); \
-        launch_zmarch3_t<TY, TX, S, W, U>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);       \
+        launch_zmarch3_t<TY, TX, S, W, U, false>(d, nlat, items, counters, parity, derr, st, ctas_per_sm); \
         break;
     switch (variant) {
         AXS_ZV(0, 8, 128, 4)
@@ -1333,6 +1378,14 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
         AXS_ZV2(27, 8, 32, 5)
         AXS_ZV3(28, 8, 32, 4, 2, 1)
         AXS_ZV3(29, 8, 32, 5, 2, 1)
+    case 30:
+        if (esz != 4) fail(AXS_ERR_ARG, "two-step z-march variant %d needs complex float fields", variant);
+        launch_zmarch3_t<8, 64, 4, 4, 1, true>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);
+        break;
+    case 31:
+        if (esz != 4) fail(AXS_ERR_ARG, "two-step z-march variant %d needs complex float fields", variant);
+        launch_zmarch3_t<8, 32, 4, 2, 1, true>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);
+        break;
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
 #undef AXS_ZV
@@ -1358,7 +1411,7 @@ static void prepare_zmarch(int esz, int variant) {
         break;
 #define AXS_ZP3(I, TY, TX, S, W, U)                               \
     case I:                                                       \
-        if (esz == 4) prepare_zmarch3_t<TY, TX, S, W, U>();       \
+        if (esz == 4) prepare_zmarch3_t<TY, TX, S, W, U, false>(); \
         break;
     switch (variant) {
         AXS_ZP(0, 8, 128, 4)
@@ -1384,6 +1437,12 @@ static void prepare_zmarch(int esz, int variant) {
         AXS_ZP2(27, 8, 32, 5)
         AXS_ZP3(28, 8, 32, 4, 2, 1)
         AXS_ZP3(29, 8, 32, 5, 2, 1)
+    case 30:
+        if (esz == 4) prepare_zmarch3_t<8, 64, 4, 4, 1, true>();
+        break;
+    case 31:
+        if (esz == 4) prepare_zmarch3_t<8, 32, 4, 2, 1, true>();
+        break;
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
     if (kZVariants[variant].gen == 3) prepare_zmarch(esz, kZVariants[variant].partner);
@@ -1404,7 +1463,7 @@ static int variant_smem(const ZVariant &v, int esz) {
         int st_m = (v.ty * 16 + 127) / 128 * 128;
         int slot = (v.ty + 4) * v.txmax * cs + 2 * (256 + st_m) + (v.ty + 2) * v.txmax * cs + 2 * st_m;
         int mid = ((v.ty + 2) * v.txmax * cs + 2 * v.ty * cs + 127) / 128 * 128;
-        return v.slots * slot + 2 * mid + 256;
+        return v.slots * slot + (v.lean ? 3 : 2) * mid + 256;
     }
     int c_bytes = (v.ty + 2) * v.txmax * cs;
     int h_pad = (v.ty * 16 + 127) / 128 * 128;

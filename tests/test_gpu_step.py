@@ -77,7 +77,7 @@ def test_kernel_variants_bit_identical(axs, oracle, precision):
 
 
 TWO_STEP = ["1,10,32", "1,11,64", "1,12,128", "1,13,16", "1,14,64", "1,15,128", "1,17,32", "1,18,64",
-            "1,19,128", "1,28,32", "1,29,64"]
+            "1,19,128", "1,28,32", "1,29,64", "1,30,32", "1,31,64"]
 
 
 @pytest.mark.parametrize("N", [64, 160])
