@@ -1169,10 +1169,20 @@ __global__ void __launch_bounds__(Z3Cfg<TY, TXMAX, S, NCW>::NT)
     k_zmarch_2step(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity, int *derr) {
     zmarch_2step_body<TY, TXMAX, S, NCW, UNR, false>(lats, nlat, total_items, counters, parity, derr);
 }
-// 128 registers: with one producer warp per CTA, three CTAs fit the 16K
-// registers of each SM sub-partition (at most four warps each)
+// Register cap for LEAN_CTAS resident CTAs of NCW + 1 warps: each of the four
+// SM sub-partitions holds 16K registers and a quarter of the warps (rounded
+// up), allocated in steps of 8 registers per thread.
+template <int NCW, int LEAN_CTAS>
+struct LeanRegs {
+    static constexpr int WARPS = (LEAN_CTAS * (NCW + 1) + 3) / 4;
+    static constexpr int R = 16384 / (32 * WARPS) / 8 * 8;
+    static constexpr int VALUE = R > 255 ? 255 : R;
+};
+// five CTAs of three warps or three of five: 128 registers (one vector per
+// thread with eight consumer warps, 96 registers, measured slower)
+template <int NCW> struct LeanCtas { static constexpr int VALUE = NCW <= 2 ? 5 : 3; };
 template <int TY, int TXMAX, int S, int NCW>
-__global__ void __maxnreg__(128)
+__global__ void __maxnreg__((LeanRegs<NCW, LeanCtas<NCW>::VALUE>::VALUE))
     k_zmarch_2step_lean(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity,
                         int *derr) {
     zmarch_2step_body<TY, TXMAX, S, NCW, 1, true>(lats, nlat, total_items, counters, parity, derr);
@@ -1386,6 +1396,7 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
         if (esz != 4) fail(AXS_ERR_ARG, "two-step z-march variant %d needs complex float fields", variant);
         launch_zmarch3_t<8, 32, 4, 2, 1, true>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);
         break;
+
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
 #undef AXS_ZV
@@ -1443,6 +1454,7 @@ static void prepare_zmarch(int esz, int variant) {
     case 31:
         if (esz == 4) prepare_zmarch3_t<8, 32, 4, 2, 1, true>();
         break;
+
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
     if (kZVariants[variant].gen == 3) prepare_zmarch(esz, kZVariants[variant].partner);
