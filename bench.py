@@ -319,7 +319,8 @@ def gpu_arm(args, dist):
     two_step = "two steps per pass" in main["desc"]
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "k_zmarch_traffic.txt")
-    tkey = "zmarch_2step_fp32_1024_per_launch_bytes:" if two_step else "zmarch_fp32_1024_per_launch_bytes:"
+    tkey = ("zmarch_2step_lean_fp32_1024_per_launch_bytes:" if "lean" in main["desc"] else
+            "zmarch_2step_fp32_1024_per_launch_bytes:") if two_step else "zmarch_fp32_1024_per_launch_bytes:"
     if args.precision == 32 and args.n == N_MAIN and os.path.exists(tfile):
         for line in open(tfile):
             if line.startswith(tkey):
