@@ -32,18 +32,19 @@ static int grid_cap(int64_t work, int threads, int per_sm) {
 static constexpr float kMargin = 1e-5f;
 
 // atan2(y, x) in float within 5e-7 rad, for the float stage above: octant
-// reduction to a = min(|x|,|y|) / max(|x|,|y|) in [0, 1], atan(a) = a P(a^2)
-// with P of degree 7 fitted to atan on [0, 1] (weighted least squares iterated
-// to equal ripple, Lawson's method; 1.4e-7 rad evaluated in float), then the
-// octant undone. Exact zeros take atan2f (the signed results on the axes).
+// reduction to a = min(|x|,|y|) / max(|x|,|y|) in [0, 1] (a fast division,
+// within 2 ulp), atan(a) = a P(a^2) with P of degree 7 fitted to atan on
+// [0, 1] (weighted least squares iterated to equal ripple, Lawson's method;
+// 1.4e-7 rad evaluated in float), then the octant undone. Exact zeros and
+// magnitudes outside [1e-30, 1e30] take atan2f (the signed results on the axes).
 __device__ constexpr float kAtanC[8] = {0.9999993443489075f,  -0.33329859375953674f, 0.19946566224098206f,
                                     -0.1390862911939621f, 0.0964219719171524f,   -0.0559123270213604f,
                                     0.021862957626581192f, -0.004054567310959101f};
 __device__ __forceinline__ float fast_atan2(float y, float x) {
     const float ax = fabsf(x), ay = fabsf(y);
     const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
-    if (mn == 0.0f) return atan2f(y, x);
-    const float a = __fdiv_rn(mn, mx);
+    if (mn == 0.0f || mx < 1e-30f || mx > 1e30f) return atan2f(y, x);
+    const float a = __fdividef(mn, mx);   // within 2 ulp for 2^-126 <= mx <= 2^126
     const float s = a * a;
     float p = kAtanC[7];
 #pragma unroll
