@@ -5,8 +5,11 @@ of one site: psi1, psi2, pi1, pi2 read and written once), with the fraction
 of the measured HBM copy bandwidth it represents.
 
 Headline workload: 3D N=1024^3, FP32 fields (FP64 time bookkeeping),
-7-point stencil, lambda=1, dx=0.5, dt=0.1, the unrescaled-coupling equation
-(prs=0, T0=0), flat k_cut=1 Gaussian start (seed 1). The state (2 x 8.6 GB
+7-point stencil, lambda=1, dx=0.5, dt=0.1, the reference's PRS step (prs=1,
+T0=0: coupling lambda/tau^2, stable at every tau; the unrescaled coupling,
+prs=0, runs the same kernels at the same speed but its radial mode outgrows
+dt = 0.1 past tau ~ 13, within a 200-step timed region), flat k_cut=1
+Gaussian start (seed 1). The state (2 x 8.6 GB
 psi buffers + 8.6 GB pi) is far larger than L2 (129 MB), so every step
 streams from HBM; no L2 flush is needed between steps.
 
@@ -16,7 +19,7 @@ start, the 96-member uneven batched ensemble, and the reference CPU path.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 For N > 1 (torchrun), each rank runs an independent replica on its own GPU
-(the single-lattice path does not shard) and rank 0 prints
+(the single lattice does not shard without a halo exchange per step) and rank 0 prints
 the aggregate.
 """
 import argparse
@@ -39,6 +42,10 @@ N_MAIN = 1024
 # written once; a two-step pass (halo depth 2) advances every site twice
 BYTES_PER_SITE = {32: 32, 64: 64}
 ENSEMBLE_SIZES = (64, 96, 128, 160, 192)
+# The end-to-end leg runs one output interval of the reference's run loop:
+# strings are searched every 20 steps (s_run.cpp cadence), so a user's host
+# round trip covers 20 steps whatever --steps times on the device.
+E2E_STEPS = 20
 
 
 def peaks():
@@ -66,7 +73,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -148,7 +155,7 @@ def cpu_port_rate(n=256, target_s=10.0, max_steps=200, min_steps=2):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
     orc = oracle_lib.load()
-    p = oracle_lib.make_params(NDIMS=3, N=n, lam=1.0, T0=0.0, dx=0.5, dt=0.1, prs=0)
+    p = oracle_lib.make_params(NDIMS=3, N=n, lam=1.0, T0=0.0, dx=0.5, dt=0.1, prs=1)
     rng = np.random.default_rng(1)
     f = [rng.standard_normal((n, n, n)).astype(np.float32) * 0.5 for _ in range(2)] + \
         [np.zeros((n, n, n), dtype=np.float32) for _ in range(2)]
@@ -182,7 +189,7 @@ def load_axs():
 
 def main_params(axs, precision, n):
     return axs.default_params(NDIMS=3, N=n, lambda_=1.0, T_initial=0.0, space_step=0.5, time_step=0.1,
-                              precision=precision, prs=0, thr=1)
+                              precision=precision, prs=1, thr=1)
 
 
 def run_lattice(axs, dist, precision, steps, warmup, with_e2e, sampler=None, n=N_MAIN):
@@ -214,32 +221,42 @@ def run_lattice(axs, dist, precision, steps, warmup, with_e2e, sampler=None, n=N
     t_spec = time.perf_counter() - t0
     rec["analysis_ms"] = {"find_strings": 1e3 * t_str, "axion_spectrum_128": 1e3 * t_spec}
     if with_e2e:
-        rec["e2e"] = e2e_leg(axs, L, dist, steps)
+        rec["e2e"] = e2e_leg(axs, L, dist, E2E_STEPS)
     L.close()
     return rec
 
 
 def e2e_leg(axs, L, dist, steps):
-    """The user's call sequence with host buffers: upload the state from
-    pinned host memory, evolve `steps` steps through axs_evolve, read the
-    step's result (the string count) and the final fields back to host."""
+    """The user's call sequence with host buffers, one output interval: upload
+    the state from pinned host memory, evolve `steps` steps through
+    axs_evolve, read the interval's result (the string count) and psi back to
+    pinned host memory. Two untimed rehearsals first: a production run repeats
+    the interval, so its CUDA graphs (one per buffer parity) are already
+    captured when the timed one runs."""
     shape = L.shape
-    bufs = [axs.PinnedBuffer(shape, np.float32) for _ in range(4)]
+    ins = [axs.PinnedBuffer(shape, np.float32) for _ in range(4)]
+    outs = [axs.PinnedBuffer(shape, np.float32) for _ in range(2)]
     f = L.download(dtype=np.float32)
-    for b, a in zip(bufs, f):
+    for b, a in zip(ins, f):
         b.array[...] = a
     del f
+
+    def interval():
+        L.upload(*[b.array for b in ins], dtype=np.float32)
+        L.evolve(steps)
+        n, _, _ = L.find_strings()
+        axs._check(axs._lib.axs_download_f32(L._h, outs[0].array.ctypes.data, outs[1].array.ctypes.data, None, None))
+        return n
+
+    for _ in range(2):
+        interval()
     dist.barrier()
     t0 = time.perf_counter()
-    L.upload(*[b.array for b in bufs], dtype=np.float32)
-    L.evolve(steps)
-    n, c, _ = L.find_strings()
-    out = axs._lib.axs_download_f32(L._h, bufs[0].array.ctypes.data, bufs[1].array.ctypes.data, None, None)
-    axs._check(out)
+    n = interval()
     wall = time.perf_counter() - t0
     dist.barrier()
     wall = dist.max(wall)
-    for b in bufs:
+    for b in ins + outs:
         b.free()
     sites = L.length
     h2d = 4 * 4 * sites
@@ -294,7 +311,7 @@ def reference_arm(args, dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n ** 3 / rate,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": "3D 1024^3 FP32 leapfrog step (prs=0, lambda=1, dx=0.5, dt=0.1)",
+            "config": {"workload": "3D 1024^3 FP32 leapfrog step (prs=1, lambda=1, dx=0.5, dt=0.1)",
                        "sample": "%d^3 lattice, %d steps" % (n, steps_done)},
             "cpu_baseline": {"value": rate, "unit": "site-updates/s", "cores": threads, "kind": "port",
                              "sample": "%d^3 FP32, %d steps of the reference-structured step (oracle port; "
@@ -348,9 +365,10 @@ def gpu_arm(args, dist):
     e2e = main.get("e2e")
     e2e_line = None
     if e2e:
-        e2e_line = {"value": sites_all * args.steps / e2e["wall_s"],      # wall_s is already the max over ranks
+        e2e_line = {"value": sites_all * E2E_STEPS / e2e["wall_s"],      # wall_s is already the max over ranks
                     "unit": "site-updates/s", "h2d_bytes_per_step": e2e["h2d_bytes_per_step"],
-                    "d2h_bytes_per_step": e2e["d2h_bytes_per_step"], "wall_s": e2e["wall_s"]}
+                    "d2h_bytes_per_step": e2e["d2h_bytes_per_step"], "wall_s": e2e["wall_s"],
+                    "steps": E2E_STEPS}
     if dist.rank != 0:
         return
     line = {
@@ -358,7 +376,7 @@ def gpu_arm(args, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": main["ms"] / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic",
-        "config": {"workload": "3D %d^3 FP%d leapfrog step, 7-point stencil, prs=0, lambda=1, dx=0.5, dt=0.1, "
+        "config": {"workload": "3D %d^3 FP%d leapfrog step, 7-point stencil, prs=1, lambda=1, dx=0.5, dt=0.1, "
                                "flat k_cut=1 start" % (args.n, args.precision), "N": args.n, "precision": "fp32 fields, fp64 tau",
                    "parallelism": "replicas" if dist.world > 1 else "single",
                    "l2": "state 25.8 GB >> 129 MB L2; no flush needed", "kernel": main["desc"]},
@@ -372,6 +390,7 @@ def gpu_arm(args, dist):
         "e2e": e2e_line,
         "gpu_launches": main["launches"],
         "analysis_ms": main.get("analysis_ms"),
+        "state_finite": bool(main.get("finite")),   # no NaN/Inf in the fields after the timed steps
         "clocks": main["clocks"],
         "fp64": fp64,
         "ensemble": ens,
@@ -382,7 +401,7 @@ def gpu_arm(args, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="axs", choices=["axs", "reference"])
     ap.add_argument("--quick", action="store_true", help="headline only (no FP64 / ensemble legs)")
