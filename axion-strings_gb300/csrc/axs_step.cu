@@ -1234,6 +1234,9 @@ static const ZVariant kZVariants[] = {
     // 30-31: LEAN two-step (centre values re-read from shared memory, 128
     // registers, one more CTA per SM)
     {3, 8, 64, 4, 4, 16, 0, 1},  {3, 8, 32, 4, 2, 27, 0, 1},
+    // 32-37: radius 2-4 with the z-neighbours in registers (R + 2 slots, float)
+    {4, 4, 128, 4, 8, -1, 2},  {4, 8, 64, 4, 8, -1, 2},  {4, 4, 128, 5, 8, -1, 3},  {4, 8, 64, 5, 8, -1, 3},
+    {4, 4, 128, 6, 8, -1, 4},  {4, 8, 64, 6, 8, -1, 4},
 };
 static const int kNumZVariants = sizeof(kZVariants) / sizeof(kZVariants[0]);
 
@@ -1509,6 +1512,7 @@ static int variant_tx(const ZVariant &v, int N, int esz) {
     if (esz == 8) txmax = std::min(txmax, 128);   // box inner dim: 2*tx doubles <= 256
     if (variant_smem(v, esz) > max_smem_optin()) return 0;
     if (N % v.ty != 0 || N < 4 || v.ty < radius(v)) return 0;
+    if (v.gen == 4 && v.slots < 2 * v.r + 2 && esz != 4) return 0;   // register z-ring: float fields only
     for (int tx = std::min(txmax, N); tx >= vs; --tx) {
         if (N % tx) continue;
         if (tx % vs) continue;

@@ -9,6 +9,10 @@
 //    aligned; only the tile rows need them: the stencil is a cross), plus the
 //    pih tile;
 //  * a ring of S >= 2R + 2 slots holding the planes z-R .. z+R and one in flight;
+//    or, with fewer slots (ZREG, float fields, one vector per thread), each
+//    thread carries psi of its vector at planes z-R .. z+R in registers and
+//    the ring holds only the planes z .. z+R still to be centres (S >= R + 2),
+//    so more CTAs share an SM;
 //  * the stencil sum formed exactly as stencil_at forms it for R > 1
 //    (c0 * psi, then per l: ((x- + x+) + (y- + y+)) + (z- + z+), fused into the
 //    sum with c_l), so every configuration is bit-identical to k_step_generic.
@@ -36,13 +40,15 @@ struct ZRCfg {
     static constexpr int SLOT = (P_OFF + TY * TXMAX * CS + 127) / 128 * 128;
     static constexpr int BAR_OFF = S * SLOT;
     static constexpr int SMEM = BAR_OFF + 256;
-    static_assert(S >= 2 * R + 2, "the ring holds 2R+1 planes and one in flight");
+    static constexpr bool ZREG = S < 2 * R + 2;                // z-neighbours in registers
+    static_assert(S >= (ZREG ? R + 2 : 2 * R + 2), "the ring holds the planes in use and one in flight");
+    static_assert(!ZREG || (sizeof(T) == 4 && MAXV == 1), "register z-ring: float fields, one vector per thread");
     static_assert(TY >= R, "halo bands must not wrap inside a box");
 };
 
 template <typename T, int TY, int TXMAX, int S, int R>
-__global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R>::NT)
-    k_zmarch2r(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity, int *derr) {
+__device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int nlat, int64_t total_items,
+                                              int *counters, int parity, int *derr) {
     typedef ZRCfg<T, TY, TXMAX, S, R> K;
     typedef typename Cplx<T>::type C;
     typedef typename Vec16<T>::type V;
@@ -166,10 +172,35 @@ __global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R>::NT)
             const bool xhalo = tx < N;
             const int nvx = tx / K::VS;
             const int nvec = nvx * TY;
+            // ZREG: psi of this thread's vector at planes z-R .. z+R (zr[R] the
+            // centre); toff is the vector's site offset in a band
+            V zr[K::ZREG ? 2 * R + 1 : 1];
+            int toff = 0;
+            if constexpr (K::ZREG) {
+                const int yy = cid < nvec ? cid / nvx : 0, xx = cid < nvec ? (cid % nvx) * K::VS : 0;
+                toff = (R + yy) * tx + xx;
+                // planes za-R .. za+R-1 (loads 0 .. 2R-1); those below the first
+                // centre are released once read
+#pragma unroll
+                for (int d = 0; d < 2 * R; ++d) {
+                    if (!ok) continue;
+                    const int wd = warp_wait(smem_u32(&full[(q0 + d) % S]), (uint32_t)(((q0 + d) / S) & 1), abort_flag);
+                    if (wd) {
+                        if (wd == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
+                        ok = false;
+                        continue;
+                    }
+                    zr[d] = *reinterpret_cast<const V *>(reinterpret_cast<const C *>(smem + ((q0 + d) % S) * K::SLOT) + toff);
+                    if (d < R) {
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(smem_u32(&empty[(q0 + d) % S]));
+                    }
+                }
+            }
             for (int t = 0; t < T_steps && ok; ++t) {
                 const int64_t qn = q0 + t + 2 * R;
                 int w = 0;
-                if (t == 0)
+                if (t == 0 && !K::ZREG)
                     for (int d = 0; d < 2 * R && !w; ++d)
                         w = warp_wait(smem_u32(&full[(q0 + d) % S]), (uint32_t)(((q0 + d) / S) & 1), abort_flag);
                 if (!w) w = warp_wait(smem_u32(&full[qn % S]), (uint32_t)((qn / S) & 1), abort_flag);
@@ -179,10 +210,11 @@ __global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R>::NT)
                     break;
                 }
                 const int z = za + t;
-                const C *Zp[2 * R + 1];   // planes z-R .. z+R
+                const C *Zp[2 * R + 1];   // planes z-R .. z+R (ZREG: only z and z+R are in the ring)
 #pragma unroll
                 for (int d = 0; d <= 2 * R; ++d) Zp[d] = reinterpret_cast<const C *>(smem + ((q0 + t + d) % S) * K::SLOT);
                 const C *Cz = Zp[R];
+                if constexpr (K::ZREG) zr[2 * R] = *reinterpret_cast<const V *>(Zp[2 * R] + toff);
                 const C *Lh = reinterpret_cast<const C *>(reinterpret_cast<const unsigned char *>(Cz) + K::C_BYTES);
                 const C *Rh = reinterpret_cast<const C *>(reinterpret_cast<const unsigned char *>(Cz) + K::C_BYTES + K::H_PAD);
                 const C *Ph = reinterpret_cast<const C *>(reinterpret_cast<const unsigned char *>(Cz) + K::P_OFF);
@@ -220,8 +252,13 @@ __global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R>::NT)
                         C ym[K::VS], yp[K::VS], zm[K::VS], zp[K::VS];
                         *reinterpret_cast<V *>(ym) = *reinterpret_cast<const V *>(&Cz[rrow - l * tx + xx]);
                         *reinterpret_cast<V *>(yp) = *reinterpret_cast<const V *>(&Cz[rrow + l * tx + xx]);
-                        *reinterpret_cast<V *>(zm) = *reinterpret_cast<const V *>(&Zp[R - l][rrow + xx]);
-                        *reinterpret_cast<V *>(zp) = *reinterpret_cast<const V *>(&Zp[R + l][rrow + xx]);
+                        if constexpr (K::ZREG) {
+                            *reinterpret_cast<V *>(zm) = zr[R - l];
+                            *reinterpret_cast<V *>(zp) = zr[R + l];
+                        } else {
+                            *reinterpret_cast<V *>(zm) = *reinterpret_cast<const V *>(&Zp[R - l][rrow + xx]);
+                            *reinterpret_cast<V *>(zp) = *reinterpret_cast<const V *>(&Zp[R + l][rrow + xx]);
+                        }
 #pragma unroll
                         for (int j = 0; j < K::VS; ++j) {
                             const C xm = win[K::RP + j - l], xp = win[K::RP + j + l];
@@ -243,10 +280,19 @@ __global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R>::NT)
                     *reinterpret_cast<V *>(&pih[off]) = *reinterpret_cast<V *>(pv);
                     *reinterpret_cast<V *>(&psi_out[off]) = *reinterpret_cast<V *>(outv);
                 }
-                // this warp is done with plane z-R (load q0+t); at the last
-                // plane also with the item's last 2R loads
+                // this warp is done with plane z-R (load q0+t; ZREG: with the
+                // centre z, load q0+t+R); at the last plane also with the
+                // item's remaining loads
                 __syncwarp();
-                if (lane == 0) {
+                if constexpr (K::ZREG) {
+                    if (lane == 0) {
+                        mbar_arrive(smem_u32(&empty[(q0 + t + R) % S]));
+                        if (t == T_steps - 1)
+                            for (int d = 1; d <= R; ++d) mbar_arrive(smem_u32(&empty[(q0 + t + R + d) % S]));
+                    }
+#pragma unroll
+                    for (int d = 0; d < 2 * R; ++d) zr[d] = zr[d + 1];
+                } else if (lane == 0) {
                     mbar_arrive(smem_u32(&empty[(q0 + t) % S]));
                     if (t == T_steps - 1)
                         for (int d = 1; d <= 2 * R; ++d) mbar_arrive(smem_u32(&empty[(q0 + t + d) % S]));
@@ -268,6 +314,25 @@ __global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R>::NT)
     }
 }
 
+template <typename T, int TY, int TXMAX, int S, int R>
+__global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R>::NT)
+    k_zmarch2r(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity, int *derr) {
+    zmarch2r_body<T, TY, TXMAX, S, R>(lats, nlat, total_items, counters, parity, derr);
+}
+// Register z-ring: 96 registers, so that two CTAs of nine warps fit the 16K
+// registers of each SM sub-partition (at most five warps each).
+template <typename T, int TY, int TXMAX, int S, int R>
+__global__ void __maxnreg__(96)
+    k_zmarch2r_zreg(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity,
+                    int *derr) {
+    zmarch2r_body<T, TY, TXMAX, S, R>(lats, nlat, total_items, counters, parity, derr);
+}
+template <typename T, int TY, int TXMAX, int S, int R>
+static void (*zr_kernel())(const ZLat *, int, int64_t, int *, int, int *) {
+    if constexpr (ZRCfg<T, TY, TXMAX, S, R>::ZREG) return k_zmarch2r_zreg<T, TY, TXMAX, S, R>;
+    else return k_zmarch2r<T, TY, TXMAX, S, R>;
+}
+
 // ---------------------------------------------------------------- host side
 
 template <typename T, int TY, int TXMAX, int S, int R>
@@ -275,10 +340,10 @@ static int prepare_r_t() {
     typedef ZRCfg<T, TY, TXMAX, S, R> K;
     static int occ = -1;
     if (occ < 0) {
-        AXS_CUDA(cudaFuncSetAttribute(k_zmarch2r<T, TY, TXMAX, S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      K::SMEM));
+        const auto kern = zr_kernel<T, TY, TXMAX, S, R>();
+        AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
         int o = 0;
-        AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_zmarch2r<T, TY, TXMAX, S, R>, K::NT, K::SMEM));
+        AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, K::NT, K::SMEM));
         if (o < 1) fail(AXS_ERR_CUDA, "radius-%d z-march kernel does not fit on an SM", R);
         occ = o;
     }
@@ -292,7 +357,7 @@ static void launch_r_t(const ZLat *d, int nlat, int64_t items, int *counters, in
     const int occ = prepare_r_t<T, TY, TXMAX, S, R>();
     const int per = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ) : occ;
     const int64_t grid = std::min<int64_t>((int64_t)per * num_sms(), items);
-    k_zmarch2r<T, TY, TXMAX, S, R><<<(int)grid, K::NT, K::SMEM, st>>>(d, nlat, items, counters, parity, derr);
+    zr_kernel<T, TY, TXMAX, S, R>()<<<(int)grid, K::NT, K::SMEM, st>>>(d, nlat, items, counters, parity, derr);
     AXS_CUDA(cudaGetLastError());
     count_launches(1);
 }
@@ -307,6 +372,14 @@ static void launch_r_t(const ZLat *d, int nlat, int64_t items, int *counters, in
     X(4, 128, 10, 4)     \
     X(8, 64, 10, 4)      \
     X(4, 64, 10, 4)
+// register z-ring shapes (S < 2R + 2): float fields only
+#define AXS_ZR_SHAPES_F(X) \
+    X(4, 128, 4, 2)        \
+    X(8, 64, 4, 2)         \
+    X(4, 128, 5, 3)        \
+    X(8, 64, 5, 3)         \
+    X(4, 128, 6, 4)        \
+    X(8, 64, 6, 4)
 
 void launch_zmarch_r(int esz, int ty, int txmax, int slots, int r, const ZLat *d, int nlat, int64_t items,
                      int *counters, int parity, int *derr, cudaStream_t st, int ctas_per_sm) {
@@ -318,6 +391,14 @@ void launch_zmarch_r(int esz, int ty, int txmax, int slots, int r, const ZLat *d
     }
     AXS_ZR_SHAPES(AXS_ZR_LAUNCH)
 #undef AXS_ZR_LAUNCH
+#define AXS_ZR_LAUNCH_F(TY, TX, S, R)                                                                     \
+    if (ty == TY && txmax == TX && slots == S && r == R) {                                                \
+        if (esz != 4) fail(AXS_ERR_ARG, "the register z-ring radius-%d kernel needs float fields", r);      \
+        launch_r_t<float, TY, TX, S, R>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);         \
+        return;                                                                                           \
+    }
+    AXS_ZR_SHAPES_F(AXS_ZR_LAUNCH_F)
+#undef AXS_ZR_LAUNCH_F
     fail(AXS_ERR_ARG, "no radius-%d z-march kernel for tile %dx%d, %d slots", r, txmax, ty, slots);
 }
 
@@ -330,6 +411,13 @@ void prepare_zmarch_r(int esz, int ty, int txmax, int slots, int r) {
     }
     AXS_ZR_SHAPES(AXS_ZR_PREP)
 #undef AXS_ZR_PREP
+#define AXS_ZR_PREP_F(TY, TX, S, R)                              \
+    if (ty == TY && txmax == TX && slots == S && r == R) {       \
+        if (esz == 4) prepare_r_t<float, TY, TX, S, R>();        \
+        return;                                                  \
+    }
+    AXS_ZR_SHAPES_F(AXS_ZR_PREP_F)
+#undef AXS_ZR_PREP_F
     fail(AXS_ERR_ARG, "no radius-%d z-march kernel for tile %dx%d, %d slots", r, txmax, ty, slots);
 }
 

@@ -272,7 +272,8 @@ def test_spectral_step_fp32_against_fp64(axs, oracle):
         assert rel(gb[q], ga[q]) <= 1e-5, (q, rel(gb[q], ga[q]))
 
 
-RADIUS_VARIANTS = {1: ["1,20,32", "1,21,64"], 2: ["1,22,64", "1,23,128"], 3: ["1,24,32", "1,25,64", "1,26,16"]}
+RADIUS_VARIANTS = {1: ["1,20,32", "1,21,64", "1,32,64", "1,33,16"], 2: ["1,22,64", "1,23,128", "1,34,32", "1,35,16"],
+                   3: ["1,24,32", "1,25,64", "1,26,16", "1,36,16", "1,37,64"]}
 
 
 @pytest.mark.parametrize("stencil", [1, 2, 3])
