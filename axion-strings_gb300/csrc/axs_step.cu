@@ -1467,6 +1467,20 @@ static void prepare_zmarch(int esz, int variant) {
 }
 
 // Dynamic shared memory of a variant (mirrors ZCfg / Z2Cfg).
+// Whether the variant's kernels (and a two-step variant's partner) can be
+// made resident on this device: the tuner skips a candidate that cannot
+// instead of failing the whole call.
+static bool variant_resident(int esz, int variant) {
+    try {
+        prepare_zmarch(esz, variant);
+        return true;
+    } catch (const Error &) {
+        cudaGetLastError();   // a refused attribute or occupancy query leaves no sticky state
+        clear_last_error();
+        return false;
+    }
+}
+
 static int variant_smem(const ZVariant &v, int esz) {
     int cs = 2 * esz;
     if (v.gen == 4) {   // mirrors ZRCfg
@@ -2008,7 +2022,7 @@ void lattice_autotune(Lattice *L) {
     }
     const int zchunks[] = {32, 64, 128, 256};
     for (int v = 0; v < kNumZVariants; ++v) {
-        if (!variant_fits(kZVariants[v], L->p, L->esz)) continue;
+        if (!variant_fits(kZVariants[v], L->p, L->esz) || !variant_resident(L->esz, v)) continue;
         const bool two = two_step(v);
         for (int zc : zchunks) {
             if (zc > L->p.N) continue;
@@ -2167,7 +2181,7 @@ void ensemble_autotune(Ensemble *E) {
     double best_ms = 1e30;
     const int zchunks[] = {32, 64, 128, 256};   // 256: whole columns of every member up to 256^3
     for (int v = 0; v < kNumZVariants; ++v) {
-        if (!ensemble_variant_ok(E, v)) continue;
+        if (!ensemble_variant_ok(E, v) || !variant_resident(E->members[0]->esz, v)) continue;
         const bool two = two_step(v);
         for (int zc : zchunks) {
             StepConfig c;
