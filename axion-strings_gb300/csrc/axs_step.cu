@@ -1944,12 +1944,11 @@ struct TuneKey {
 };
 static std::map<TuneKey, StepConfig> g_tune_cache;
 
-static double time_launches(cudaStream_t st, int reps, const std::function<void()> &fn) {
+static double time_launches(cudaStream_t st, int reps, const std::function<void()> &fn, int warm = 2) {
     cudaEvent_t a, b;
     AXS_CUDA(cudaEventCreate(&a));
     AXS_CUDA(cudaEventCreate(&b));
-    fn();
-    fn();
+    for (int w = 0; w < warm; ++w) fn();
     AXS_CUDA(cudaEventRecord(a, st));
     for (int r = 0; r < reps; ++r) fn();
     AXS_CUDA(cudaEventRecord(b, st));
@@ -1964,8 +1963,10 @@ static double time_launches(cudaStream_t st, int reps, const std::function<void(
 // Candidate steps run with dt = 0: psi_out = psi + 0*pih and pih + 0*K are
 // bit-identical copies, so the state (and tau) is unchanged. Candidates are
 // the generic kernel and every z-march variant that tiles N (one-step
-// variants, and two-step variants with halo depth 2) at z-chunks of 32, 64
-// and 128 planes; the time per step decides.
+// variants, and two-step variants with halo depth 2). Every variant is first
+// screened with one launch at one z-chunk; the three fastest are then timed
+// at every z-chunk (32 to 256 planes) at full length, and the time per step
+// decides.
 void lattice_autotune(Lattice *L) {
     L->tuned = true;
     // AXS_FORCE_CONFIG="kind,variant,zchunk" pins a configuration (tests use it
@@ -2021,28 +2022,39 @@ void lattice_autotune(Lattice *L) {
         if (ms < best_ms) { best_ms = ms; best = c; }
     }
     const int zchunks[] = {32, 64, 128, 256};
-    for (int v = 0; v < kNumZVariants; ++v) {
-        if (!variant_fits(kZVariants[v], L->p, L->esz) || !variant_resident(L->esz, v)) continue;
+    auto trial = [&](int v, int zc, int nrep, int nwarm) {
         const bool two = two_step(v);
+        StepConfig c;
+        c.kind = 1;
+        c.variant = v;
+        c.zchunk = zc;
+        L->cfg = c;
+        ensure_single_table(L);   // built with dt = 0
+        double ms = time_launches(L->stream, nrep, [&] {
+            launch_zmarch(L->esz, v, L->dzlat, 1, L->zitems, L->dcounter, L->cur, L->derr, L->stream, 0);
+            L->cur ^= 1;
+            if (two) std::swap(L->pih, L->scratch);
+        }, nwarm);
+        if (two) ms *= 0.5;   // per step
+        c.tx = L->cfg.tx;
+        log.push_back({c, ms});
+        return std::make_pair(c, ms);
+    };
+    int zc0 = 0;   // the screening z-chunk: the largest candidate up to min(N, 128)
+    for (int zc : zchunks)
+        if (zc <= L->p.N && zc <= 128) zc0 = zc;
+    std::vector<std::pair<double, int>> screen;
+    if (zc0 > 0)
+        for (int v = 0; v < kNumZVariants; ++v)
+            if (variant_fits(kZVariants[v], L->p, L->esz) && variant_resident(L->esz, v))
+                screen.push_back({trial(v, zc0, 1, 1).second, v});
+    std::sort(screen.begin(), screen.end());
+    for (size_t k = 0; k < screen.size() && k < 3; ++k)
         for (int zc : zchunks) {
             if (zc > L->p.N) continue;
-            StepConfig c;
-            c.kind = 1;
-            c.variant = v;
-            c.zchunk = zc;
-            L->cfg = c;
-            ensure_single_table(L);   // built with dt = 0
-            double ms = time_launches(L->stream, reps, [&] {
-                launch_zmarch(L->esz, v, L->dzlat, 1, L->zitems, L->dcounter, L->cur, L->derr, L->stream, 0);
-                L->cur ^= 1;
-                if (two) std::swap(L->pih, L->scratch);
-            });
-            if (two) ms *= 0.5;   // per step
-            c.tx = L->cfg.tx;
-            log.push_back({c, ms});
-            if (ms < best_ms) { best_ms = ms; best = c; }
+            auto r = trial(screen[k].second, zc, reps, 2);
+            if (r.second < best_ms) { best_ms = r.second; best = r.first; }
         }
-    }
     L->p.time_step = dt_save;
     // dt = 0 steps copied psi (and, out of place, pih) back and forth; values
     // are identical, but keep the psi buffer the caller had as current.
