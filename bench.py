@@ -187,13 +187,13 @@ def load_axs():
     return axs
 
 
-def main_params(axs, precision, n):
+def main_params(axs, precision, n, stencil=0):
     return axs.default_params(NDIMS=3, N=n, lambda_=1.0, T_initial=0.0, space_step=0.5, time_step=0.1,
-                              precision=precision, prs=1, thr=1)
+                              precision=precision, prs=1, thr=1, stencil_setting=stencil)
 
 
-def run_lattice(axs, dist, precision, steps, warmup, with_e2e, sampler=None, n=N_MAIN):
-    p = main_params(axs, precision, n)
+def run_lattice(axs, dist, precision, steps, warmup, with_e2e, sampler=None, n=N_MAIN, stencil=0):
+    p = main_params(axs, precision, n, stencil)
     L = axs.Lattice(p)
     L.init_flat(1, 1.0)
     L.evolve(warmup)                       # includes autotuning (dt = 0 trials) and graph capture
@@ -326,7 +326,7 @@ def gpu_arm(args, dist):
     hbm, peak_note = peaks()
     sampler = ClockSampler(dist.local)
     main = run_lattice(axs, dist, args.precision, args.steps, args.warmup, with_e2e=not args.no_e2e, sampler=sampler,
-                       n=args.n)
+                       n=args.n, stencil=args.stencil)
     sites_all = dist.sum(main["sites"])
     value = sites_all * args.steps / (main["ms"] * 1e-3)
     launches = max(1, main["launches"])
@@ -338,7 +338,7 @@ def gpu_arm(args, dist):
     tfile = os.path.join(ROOT, "profiles", "k_zmarch_traffic.txt")
     tkey = ("zmarch_2step_lean_fp32_1024_per_launch_bytes:" if "lean" in main["desc"] else
             "zmarch_2step_fp32_1024_per_launch_bytes:") if two_step else "zmarch_fp32_1024_per_launch_bytes:"
-    if args.precision == 32 and args.n == N_MAIN and os.path.exists(tfile):
+    if args.precision == 32 and args.n == N_MAIN and args.stencil == 0 and os.path.exists(tfile):
         for line in open(tfile):
             if line.startswith(tkey):
                 traffic = float(line.split(":", 1)[1]) / 1e9     # GB per launch, like `achieved`'s bytes
@@ -376,8 +376,9 @@ def gpu_arm(args, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": main["ms"] / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic",
-        "config": {"workload": "3D %d^3 FP%d leapfrog step, 7-point stencil, prs=1, lambda=1, dx=0.5, dt=0.1, "
-                               "flat k_cut=1 start" % (args.n, args.precision), "N": args.n, "precision": "fp32 fields, fp64 tau",
+        "config": {"workload": "3D %d^3 FP%d leapfrog step, %d-point stencil, prs=1, lambda=1, dx=0.5, dt=0.1, "
+                               "flat k_cut=1 start" % (args.n, args.precision, 1 + 6 * (args.stencil + 1)),
+                   "N": args.n, "precision": "fp32 fields, fp64 tau",
                    "parallelism": "replicas" if dist.world > 1 else "single",
                    "l2": "state 25.8 GB >> 129 MB L2; no flush needed", "kernel": main["desc"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
@@ -410,6 +411,8 @@ def main():
     ap.add_argument("--n", type=int, default=N_MAIN, help="lattice side (profiling cases use smaller N)")
     ap.add_argument("--precision", type=int, default=32, choices=[32, 64],
                     help="headline leg precision (64 only for profiling the FP64 step)")
+    ap.add_argument("--stencil", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="stencil_setting of the headline leg (1-3, radius 2-4, only for profiling those kernels)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
