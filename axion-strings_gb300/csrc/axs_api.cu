@@ -10,6 +10,8 @@
 #include <vector>
 #include <algorithm>
 
+#include <mutex>
+
 #include "axs_internal.h"
 
 struct axs_lattice {
@@ -172,9 +174,11 @@ struct Xfer {
     int64_t chunk = 0;     // elements per chunk (<= kXferChunk, <= the lattice length)
 };
 static std::map<Lattice *, Xfer> g_xfer;
+static std::mutex g_xfer_mu;   // handles may be driven from different threads
 
 static Xfer &xfer(Lattice *L) {
-    Xfer &x = g_xfer[L];
+    std::lock_guard<std::mutex> lk(g_xfer_mu);
+    Xfer &x = g_xfer[L];   // map nodes stay put: the reference outlives the lock
     if (!x.buf) {
         AXS_CUDA(cudaStreamCreateWithFlags(&x.copy, cudaStreamNonBlocking));
         for (int i = 0; i < 2; ++i) {
@@ -188,6 +192,7 @@ static Xfer &xfer(Lattice *L) {
     return x;
 }
 static void xfer_release(Lattice *L) {
+    std::lock_guard<std::mutex> lk(g_xfer_mu);
     auto it = g_xfer.find(L);
     if (it == g_xfer.end()) return;
     Xfer &x = it->second;

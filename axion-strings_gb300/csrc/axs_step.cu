@@ -20,6 +20,8 @@
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 #include <functional>
 
 #include "axs_internal.h"
@@ -1195,12 +1197,13 @@ static void (*zm3_kernel())(const ZLat *, int, int64_t, int *, int, int *) {
 
 // ============================================================== host side
 
-static int g_num_sms = 0;
+static std::atomic<int> g_num_sms{0};
 int num_sms() {
     if (!g_num_sms) {
-        int dev = 0;
+        int dev = 0, n = 0;
         AXS_CUDA(cudaGetDevice(&dev));
-        AXS_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+        AXS_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+        g_num_sms = n;
     }
     return g_num_sms;
 }
@@ -1261,7 +1264,7 @@ std::string StepConfig::describe() const {
 template <typename T, int TY, int TXMAX, int S>
 static int prepare_zmarch_t() {
     typedef ZCfg<T, TY, TXMAX, S> K;
-    static int occ = -1;
+    static std::atomic<int> occ{-1};   // first calls may race: same value
     if (occ < 0) {
         AXS_CUDA(cudaFuncSetAttribute(k_zmarch<T, TY, TXMAX, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
         int o = 0;
@@ -1287,7 +1290,7 @@ static void launch_zmarch_t(const ZLat *d, int nlat, int64_t items, int *counter
 template <typename T, int TY, int TXMAX, int S>
 static int prepare_zmarch2_t() {
     typedef Z2Cfg<T, TY, TXMAX, S> K;
-    static int occ = -1;
+    static std::atomic<int> occ{-1};   // first calls may race: same value
     if (occ < 0) {
         AXS_CUDA(cudaFuncSetAttribute(k_zmarch2<T, TY, TXMAX, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
         int o = 0;
@@ -1313,7 +1316,7 @@ static void launch_zmarch2_t(const ZLat *d, int nlat, int64_t items, int *counte
 template <int TY, int TXMAX, int S, int NCW, int UNR, bool LEAN>
 static int prepare_zmarch3_t() {
     typedef Z3Cfg<TY, TXMAX, S, NCW, LEAN ? 3 : 2> K;
-    static int occ = -1;
+    static std::atomic<int> occ{-1};   // first calls may race: same value
     if (occ < 0) {
         const auto kern = zm3_kernel<TY, TXMAX, S, NCW, UNR, LEAN>();
         AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
@@ -1501,11 +1504,12 @@ static int variant_smem(const ZVariant &v, int esz) {
 }
 
 static int max_smem_optin() {
-    static int m = 0;
+    static std::atomic<int> m{0};
     if (!m) {
-        int dev = 0;
+        int dev = 0, v = 0;
         AXS_CUDA(cudaGetDevice(&dev));
-        AXS_CUDA(cudaDeviceGetAttribute(&m, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        AXS_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        m = v;
     }
     return m;
 }
@@ -1943,6 +1947,7 @@ struct TuneKey {
     }
 };
 static std::map<TuneKey, StepConfig> g_tune_cache;
+static std::mutex g_tune_mu;   // lattices may be tuned from different threads
 
 static double time_launches(cudaStream_t st, int reps, const std::function<void()> &fn, int warm = 2) {
     cudaEvent_t a, b;
@@ -1987,18 +1992,22 @@ void lattice_autotune(Lattice *L) {
         }
     }
     TuneKey key{L->p.N, L->p.NDIMS, L->esz, L->p.stencil_setting};
-    auto hit = g_tune_cache.find(key);
-    if (hit != g_tune_cache.end()) {
-        if (hit->second.kind != L->cfg.kind || hit->second.variant != L->cfg.variant || hit->second.zchunk != L->cfg.zchunk)
-            clear_graphs(L->graphs);
-        L->cfg = hit->second;
-        L->zlat_variant = -1;
-        return;
-    }
-    if (!zmarch_supported(L->p)) {
-        L->cfg.kind = 0;
-        g_tune_cache[key] = L->cfg;
-        return;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto hit = g_tune_cache.find(key);
+        if (hit != g_tune_cache.end()) {
+            if (hit->second.kind != L->cfg.kind || hit->second.variant != L->cfg.variant ||
+                hit->second.zchunk != L->cfg.zchunk)
+                clear_graphs(L->graphs);
+            L->cfg = hit->second;
+            L->zlat_variant = -1;
+            return;
+        }
+        if (!zmarch_supported(L->p)) {
+            L->cfg.kind = 0;
+            g_tune_cache[key] = L->cfg;
+            return;
+        }
     }
     float dt_save = L->p.time_step;
     L->p.time_step = 0.0f;
@@ -2069,7 +2078,10 @@ void lattice_autotune(Lattice *L) {
     L->cfg = best;
     L->zlat_variant = -1;   // rebuild the table with the real dt before the next step
     clear_graphs(L->graphs);
-    g_tune_cache[key] = best;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = best;
+    }
     if (env_flag("AXS_TUNE_LOG", false)) {
         for (auto &e : log) fprintf(stderr, "[axs autotune N=%d] %-60s %.4f ms/step\n", L->p.N, e.first.describe().c_str(), e.second);
         fprintf(stderr, "[axs autotune N=%d] chose %s\n", L->p.N, best.describe().c_str());

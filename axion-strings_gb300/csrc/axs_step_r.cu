@@ -18,6 +18,7 @@
 //    sum with c_l), so every configuration is bit-identical to k_step_generic.
 // One pass per step: 32 B (FP32) / 64 B (FP64) per site-update, as for radius 1.
 #include <algorithm>
+#include <atomic>
 
 #include "axs_internal.h"
 #include "axs_tma.cuh"
@@ -338,7 +339,7 @@ static void (*zr_kernel())(const ZLat *, int, int64_t, int *, int, int *) {
 template <typename T, int TY, int TXMAX, int S, int R>
 static int prepare_r_t() {
     typedef ZRCfg<T, TY, TXMAX, S, R> K;
-    static int occ = -1;
+    static std::atomic<int> occ{-1};   // first calls may race: same value
     if (occ < 0) {
         const auto kern = zr_kernel<T, TY, TXMAX, S, R>();
         AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
