@@ -17,7 +17,8 @@
  *   - The fields are the reference's rescaled field psi = tau*phi ("phi1",
  *     "phi2") and its conformal-time derivative ("phidot1", "phidot2"),
  *     exactly the arrays of struct _all_data (src/standard/s_internal.hpp:6-20).
- *   - One CUDA stream per handle; calls on one handle are not thread-safe.
+ *   - One CUDA stream per handle; calls on one handle are not thread-safe,
+ *     calls on different handles may come from different threads.
  *     Calls that return host results synchronise that stream.
  */
 #ifndef AXS_H
