@@ -745,7 +745,9 @@ int axs_inject_wait_timeout(axs_lattice *h) {
     Lattice *L = &h->L;
     if (L->in_ensemble) fail(AXS_ERR_STATE, "inject on a lattice that is not an ensemble member");
     if (!L->tuned) lattice_autotune(L);
-    if (L->cfg.kind != 1) fail(AXS_ERR_STATE, "the step kernel in use (%s) has no device-side waits", L->cfg.describe().c_str());
+    if (L->cfg.kind != 1 || L->p.laplacian != 0)
+        fail(AXS_ERR_STATE, "the step kernel in use (%s) has no device-side waits",
+             L->p.laplacian != 0 ? "spectral Laplacian step" : L->cfg.describe().c_str());
     L->debug_tx_excess = 16;
     L->zlat_variant = -1;
     clear_graphs(L->graphs);
@@ -769,7 +771,11 @@ int axs_ensemble_describe(axs_ensemble *e, char *buf, size_t len) {
 int axs_describe(axs_lattice *h, char *buf, size_t len) {
     API_BEGIN
     CHECK_HANDLE(h);
-    if (buf && len) snprintf(buf, len, "%s", h->L.cfg.describe().c_str());
+    if (buf && len) {
+        if (h->L.p.laplacian == 1)
+            snprintf(buf, len, "spectral Laplacian step (cuFFT transform pair of the complex field per step)");
+        else snprintf(buf, len, "%s", h->L.cfg.describe().c_str());
+    }
     API_END
 }
 

@@ -1812,6 +1812,9 @@ int lattice_advance(Lattice *L, int max_steps) {
         AXS_CUDA(cudaGetLastError());
         count_launches(1);
         L->fresh = 0;
+    } else if (L->p.laplacian == 1) {   // the spectral step whatever the configuration says
+        if (L->esz == 4) spectral_step_t<float>(L);
+        else spectral_step_t<double>(L);
     } else if (L->cfg.kind == 1) {
         if (!single_table_valid(L)) ensure_single_table(L);
         int kv = L->cfg.variant;
@@ -1825,9 +1828,6 @@ int lattice_advance(Lattice *L, int max_steps) {
             L->debug_tx_excess = 0;
             L->zlat_variant = -1;
         }
-    } else if (L->p.laplacian == 1) {
-        if (L->esz == 4) spectral_step_t<float>(L);
-        else spectral_step_t<double>(L);
     } else {
         if (L->esz == 4) launch_generic_dispatch<float>(L, cin, cout);
         else launch_generic_dispatch<double>(L, cin, cout);
@@ -1858,7 +1858,7 @@ static bool env_flag(const char *name, bool dflt) {
 }
 
 static void prepare_tables(Lattice *L) {
-    if (L->cfg.kind == 1 && !single_table_valid(L)) ensure_single_table(L);
+    if (L->cfg.kind == 1 && L->p.laplacian == 0 && !single_table_valid(L)) ensure_single_table(L);
 }
 
 static uint64_t mix_state(uint64_t h, const Lattice *m) {
@@ -1937,13 +1937,17 @@ void lattice_evolve(Lattice *L, int nsteps) {
 }
 
 // ---------------------------------------------------------------- autotune
+// Everything that decides which kernels can run: the shape, the precision,
+// the stencil radius and the Laplacian (a spectral lattice never takes a
+// finite-difference configuration tuned for the same shape).
 struct TuneKey {
-    int n, ndims, esz, stencil;
+    int n, ndims, esz, stencil, laplacian;
     bool operator<(const TuneKey &o) const {
         if (n != o.n) return n < o.n;
         if (ndims != o.ndims) return ndims < o.ndims;
         if (esz != o.esz) return esz < o.esz;
-        return stencil < o.stencil;
+        if (stencil != o.stencil) return stencil < o.stencil;
+        return laplacian < o.laplacian;
     }
 };
 static std::map<TuneKey, StepConfig> g_tune_cache;
@@ -1991,7 +1995,7 @@ void lattice_autotune(Lattice *L) {
             return;
         }
     }
-    TuneKey key{L->p.N, L->p.NDIMS, L->esz, L->p.stencil_setting};
+    TuneKey key{L->p.N, L->p.NDIMS, L->esz, L->p.stencil_setting, L->p.laplacian};
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto hit = g_tune_cache.find(key);

@@ -272,6 +272,28 @@ def test_spectral_step_fp32_against_fp64(axs, oracle):
         assert rel(gb[q], ga[q]) <= 1e-5, (q, rel(gb[q], ga[q]))
 
 
+def test_spectral_after_finite_difference_lattice_of_same_shape(axs, oracle):
+    """A finite-difference lattice tunes (and caches) a z-march configuration
+    for its shape; a spectral lattice of the same shape and precision created
+    afterwards still takes the spectral step (the tuning is keyed by the
+    Laplacian too): it agrees with an FP64 spectral run from the same start
+    (the finite-difference step would differ at the 1e-2 level)."""
+    N = 128
+    with axs.Lattice(params(axs, 3, N, 32)) as F:
+        F.init_thermal(3)
+        F.evolve(4)
+    f = oracle.init_thermal(orc(params(axs, 3, N, 64, laplacian=1)), 23)
+    with axs.Lattice(params(axs, 3, N, 32, laplacian=1)) as B, \
+            axs.Lattice(params(axs, 3, N, 64, laplacian=1)) as A:
+        for L in (A, B):
+            L.upload(*f)
+            L.evolve(10)
+            assert "spectral" in L.describe(), L.describe()
+        ga, gb = A.download(), B.download()
+    for q in range(4):
+        assert rel(gb[q], ga[q]) <= 1e-5, (q, rel(gb[q], ga[q]))
+
+
 RADIUS_VARIANTS = {1: ["1,20,32", "1,21,64", "1,32,64", "1,33,16"], 2: ["1,22,64", "1,23,128", "1,34,32", "1,35,16"],
                    3: ["1,24,32", "1,25,64", "1,26,16", "1,36,16", "1,37,64"]}
 
