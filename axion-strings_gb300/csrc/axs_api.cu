@@ -744,7 +744,7 @@ int axs_inject_wait_timeout(axs_lattice *h) {
     CHECK_HANDLE(h);
     Lattice *L = &h->L;
     if (L->in_ensemble) fail(AXS_ERR_STATE, "inject on a lattice that is not an ensemble member");
-    if (!L->tuned) lattice_autotune(L);
+    if (!L->tuned) lattice_evolve(L, 0);   // the configuration the next step will use (tuned unless AXS_AUTOTUNE=0)
     if (L->cfg.kind != 1 || L->p.laplacian != 0)
         fail(AXS_ERR_STATE, "the step kernel in use (%s) has no device-side waits",
              L->p.laplacian != 0 ? "spectral Laplacian step" : L->cfg.describe().c_str());
