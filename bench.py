@@ -298,6 +298,12 @@ def run_ensemble(axs, dist, steps, warmup, master_seed=2026):
 
 
 # --------------------------------------------------------------------- arms
+def workload_name(n, precision, stencil=0):
+    """The workload both arms measure (the reference arm on a sample of it)."""
+    return ("3D %d^3 FP%d leapfrog step, %d-point stencil, prs=1, lambda=1, dx=0.5, dt=0.1, flat k_cut=1 start"
+            % (n, precision, 1 + 6 * (stencil + 1)))
+
+
 def reference_arm(args, dist):
     """The reference's CPU path: the oracle port of vvsl_field_rescaled
     (reference loop structure) on the host cores; oracle/_ref is x86-only."""
@@ -311,7 +317,7 @@ def reference_arm(args, dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n ** 3 / rate,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": "3D 1024^3 FP32 leapfrog step (prs=1, lambda=1, dx=0.5, dt=0.1)",
+            "config": {"workload": workload_name(args.n, 32), "N": args.n, "precision": "fp32 fields",
                        "sample": "%d^3 lattice, %d steps" % (n, steps_done)},
             "cpu_baseline": {"value": rate, "unit": "site-updates/s", "cores": threads, "kind": "port",
                              "sample": "%d^3 FP32, %d steps of the reference-structured step (oracle port; "
@@ -376,8 +382,7 @@ def gpu_arm(args, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": main["ms"] / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic",
-        "config": {"workload": "3D %d^3 FP%d leapfrog step, %d-point stencil, prs=1, lambda=1, dx=0.5, dt=0.1, "
-                               "flat k_cut=1 start" % (args.n, args.precision, 1 + 6 * (args.stencil + 1)),
+        "config": {"workload": workload_name(args.n, args.precision, args.stencil),
                    "N": args.n, "precision": "fp32 fields, fp64 tau",
                    "parallelism": "replicas" if dist.world > 1 else "single",
                    "l2": "state 25.8 GB >> 129 MB L2; no flush needed", "kernel": main["desc"]},
