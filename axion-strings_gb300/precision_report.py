@@ -1,5 +1,5 @@
 """FP32 (compensated reductions) against plain FP64 on the GPU, from the same
-seeded start: the errors the precision form is judged by.
+seeded start: the errors by which the precision form is assessed.
 
   1. field relative error after 10 steps of the physical equation (prs = 0)
      from the flat k_cut = 1 start: ||x32 - x64|| / ||x64|| per field;
