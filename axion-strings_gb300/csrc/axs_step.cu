@@ -1851,6 +1851,12 @@ void count_launches(int64_t n) {
 }
 int64_t total_launches() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
+// AXS_FORCE_CONFIG pins a configuration; it applies with AXS_AUTOTUNE=0 too.
+static bool forced_config() {
+    const char *f = getenv("AXS_FORCE_CONFIG");
+    return f && *f;
+}
+
 static bool env_flag(const char *name, bool dflt) {
     const char *v = getenv(name);
     if (!v || !*v) return dflt;
@@ -1893,7 +1899,7 @@ static cudaGraphExec_t capture(cudaStream_t st, StepFn fn, int64_t *launches) {
 
 void lattice_evolve(Lattice *L, int nsteps) {
     if (!L->tuned) {
-        if (env_flag("AXS_AUTOTUNE", true)) lattice_autotune(L);
+        if (env_flag("AXS_AUTOTUNE", true) || forced_config()) lattice_autotune(L);
         L->tuned = true;
     }
     if (nsteps <= 0) return;
@@ -2257,7 +2263,7 @@ std::string ensemble_describe(const Ensemble *E) {
 
 void ensemble_evolve(Ensemble *E, int nsteps) {
     if (!E->tuned) {
-        if (env_flag("AXS_AUTOTUNE", true)) ensemble_autotune(E);
+        if (env_flag("AXS_AUTOTUNE", true) || forced_config()) ensemble_autotune(E);
         E->tuned = true;
     }
     if (nsteps <= 0) return;
