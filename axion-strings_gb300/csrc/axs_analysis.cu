@@ -700,28 +700,39 @@ template <> __device__ __forceinline__ FF mode_power<double>(const double2 &f) {
 // k_bin_final3 as before (three rows: power, |n|, count). With KS false only the power row is summed (the
 // |n| and count rows, which depend on N and the bin edges alone, stay zero;
 // the power sums are the same bits either way).
+// Large spectra run in pieces that fit shared memory: a row of the half
+// spectrum is taken in segments of `seg` modes (each segment is binned like a
+// row: bins still only grow along it), and the bins in passes of `nbp`, this
+// launch summing bins b0 .. b0+nbp-1 only (modes of other bins are skipped).
+// One segment per row and one pass is the common case.
 template <typename T, typename B, bool KS>
 __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *__restrict__ F, int N, int ndims,
-                                                  B binner, int nbins,
+                                                  B binner, int nbins, int seg, int b0, int nbp,
                                                   double *__restrict__ partials) {
     typedef typename Cplx<T>::type C;
-    extern __shared__ double hist[];   // [4 warps][3][nbins], bin table, [4 warps][nh] staged rows
+    extern __shared__ double hist[];   // [4 warps][3][nbp], bin table, [4 warps][seg] staged row segments
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nh = N / 2 + 1;
-    for (int i = threadIdx.x; i < 4 * 3 * nbins; i += blockDim.x) hist[i] = 0.0;
-    const B bins = binner.staged(hist + 4 * 3 * nbins);
-    // staged rows start 16-byte aligned (complex double rows are read as double2)
-    C *stage = reinterpret_cast<C *>(hist + (((4 * 3 + B::kSmemTable) * nbins + 1) & ~1)) + (size_t)w * nh;
+    const int nseg = (nh + seg - 1) / seg;
+    const int b1 = b0 + nbp;
+    for (int i = threadIdx.x; i < 4 * 3 * nbp; i += blockDim.x) hist[i] = 0.0;
+    const B bins = binner.staged(hist + 4 * 3 * nbp);
+    // staged segments start 16-byte aligned (complex double modes are read as double2)
+    C *stage = reinterpret_cast<C *>(hist + ((4 * 3 * nbp + B::kSmemTable * nbins + 1) & ~1)) + (size_t)w * seg;
     __syncthreads();
-    double *hp = hist + (size_t)w * 3 * nbins;
-    double *hk = hp + nbins;
-    double *hc = hk + nbins;
+    double *hp = hist + (size_t)w * 3 * nbp;   // indexed by bin - b0
+    double *hk = hp + nbp;
+    double *hc = hk + nbp;
+    auto in_pass = [&](int bb) { return bb >= b0 && bb < b1; };
     const int64_t rows = ndims == 2 ? (int64_t)N : (int64_t)N * N;
+    const int64_t units = rows * nseg;
     const int64_t nwarps = (int64_t)gridDim.x * 4;
-    const int chunk = (nh + 31) / 32;
-    const int lo = min(nh, lane * chunk), hi = min(nh, lo + chunk);
-    for (int64_t r = (int64_t)blockIdx.x * 4 + w; r < rows; r += nwarps) {
-        // |n|^2 = ix^2 + fy^2 + fz^2 <= 3 (N/2)^2 < 2^24 for N <= 4096: int
+    for (int64_t u = (int64_t)blockIdx.x * 4 + w; u < units; u += nwarps) {
+        const int64_t r = u / nseg;
+        const int s0 = (int)(u - r * nseg) * seg, sl = min(seg, nh - s0);
+        const int chunk = (sl + 31) / 32;
+        const int lo = s0 + min(sl, lane * chunk), hi = s0 + min(sl, lane * chunk + chunk);
+        // |n|^2 = ix^2 + fy^2 (+ fz^2) <= 2 (N/2)^2 < 2^31 in 2D (N <= 32768), 3 (N/2)^2 in 3D (N <= 4096): int
         int c2;
         if (ndims == 2) {
             const int fy = r < N / 2 ? (int)r : (int)r - N;
@@ -731,8 +742,8 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
             const int fz = iz < N / 2 ? iz : iz - N, fy = iy < N / 2 ? iy : iy - N;
             c2 = fy * fy + fz * fz;
         }
-        const C *row = F + r * nh;
-        for (int ix = lane; ix < nh; ix += 32) stage[ix] = row[ix];
+        const C *row = F + r * nh + s0;
+        for (int ix = lane; ix < sl; ix += 32) stage[ix] = row[ix];
         __syncwarp();
         int b = -1, fb = -1, lb = -1;
         FF v{0.f, 0.f}, kk{0.f, 0.f}, fv{0.f, 0.f}, fk{0.f, 0.f};
@@ -743,11 +754,11 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
             if (nb != b) {
                 if (b >= 0) {
                     if (fb < 0) { fb = b; fv = v; fk = kk; fc = c; }
-                    else {   // a run inside the slice: no other lane has this bin in this row
-                        ff_acc(hp + b, v);
+                    else if (in_pass(b)) {   // a run inside the slice: no other lane has this bin in this segment
+                        ff_acc(hp + (b - b0), v);
                         if constexpr (KS) {
-                            ff_acc(hk + b, kk);
-                            ff_acc(hc + b, FF{(float)c, 0.f});
+                            ff_acc(hk + (b - b0), kk);
+                            ff_acc(hc + (b - b0), FF{(float)c, 0.f});
                         }
                     }
                 }
@@ -755,18 +766,27 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
                 v = kk = FF{0.f, 0.f};
                 c = 0;
             }
-            if (nb >= 0) {
+            if (in_pass(nb)) {
                 const int wt = (ix == 0 || 2 * ix == N) ? 1 : 2;
                 const float fw = (float)wt;   // x1 or x2: exact in float-float
-                const FF p = mode_power<T>(stage[ix]);
+                const FF p = mode_power<T>(stage[ix - s0]);
                 v = ff_add(v, FF{fw * p.hi, fw * p.lo});
                 if constexpr (KS) {
-                    // |n| = sqrt(n2) as float-float: hi = sqrtf (correctly rounded), the residual
-                    // n2 - hi^2 is exact in float (that of a correctly rounded square
-                    // root always is) and lo = residual / (2 hi); n2 < 2^24 is exact in float
-                    const float n2f = (float)n2;
-                    const float shi = sqrtf(n2f);
-                    const float2 sq = make_float2(shi, shi > 0.0f ? __fdiv_rn(fmaf(-shi, shi, n2f), 2.0f * shi) : 0.0f);
+                    // |n| = sqrt(n2) as float-float. Below 2^24, n2 is exact in float:
+                    // hi = sqrtf (correctly rounded), the residual n2 - hi^2 is exact
+                    // in float (that of a correctly rounded square root always is)
+                    // and lo = residual / (2 hi). Above (large 2D lattices), from the
+                    // double square root (this pass runs once per binning).
+                    float2 sq;
+                    if (n2 < (1 << 24)) {
+                        const float n2f = (float)n2;
+                        const float shi = sqrtf(n2f);
+                        sq = make_float2(shi, shi > 0.0f ? __fdiv_rn(fmaf(-shi, shi, n2f), 2.0f * shi) : 0.0f);
+                    } else {
+                        const double rd = sqrt((double)n2);
+                        const float shi = (float)rd;
+                        sq = make_float2(shi, (float)(rd - (double)shi));
+                    }
                     kk = ff_add(kk, FF{fw * sq.x, fw * sq.y});
                     c += wt;
                 }
@@ -799,33 +819,33 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
             }
         }
         const int nextb = __shfl_down_sync(0xffffffffu, fb, 1);
-        if (fb >= 0 && (lane == 31 || nextb != fb)) {
-            ff_acc(hp + fb, fv);
+        if (in_pass(fb) && (lane == 31 || nextb != fb)) {
+            ff_acc(hp + (fb - b0), fv);
             if constexpr (KS) {
-                ff_acc(hk + fb, fk);
-                ff_acc(hc + fb, FF{(float)fc, 0.f});
+                ff_acc(hk + (fb - b0), fk);
+                ff_acc(hc + (fb - b0), FF{(float)fc, 0.f});
             }
         }
         __syncwarp();
-        if (lb >= 0) {
-            ff_acc(hp + lb, lv);
+        if (in_pass(lb)) {
+            ff_acc(hp + (lb - b0), lv);
             if constexpr (KS) {
-                ff_acc(hk + lb, lk);
-                ff_acc(hc + lb, FF{(float)lc, 0.f});
+                ff_acc(hk + (lb - b0), lk);
+                ff_acc(hc + (lb - b0), FF{(float)lc, 0.f});
             }
         }
         __syncwarp();
     }
     __syncthreads();
-    for (int bn = threadIdx.x; bn < nbins; bn += blockDim.x) {
+    for (int bn = threadIdx.x; bn < nbp; bn += blockDim.x) {
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             double acc = 0.0;
             for (int ww = 0; ww < 4; ++ww) {
-                const float2 h = reinterpret_cast<const float2 *>(hist)[(size_t)ww * 3 * nbins + (size_t)q * nbins + bn];
+                const float2 h = reinterpret_cast<const float2 *>(hist)[(size_t)ww * 3 * nbp + (size_t)q * nbp + bn];
                 acc += (double)h.x + (double)h.y;
             }
-            partials[((int64_t)blockIdx.x * 3 + q) * nbins + bn] = acc;
+            partials[((int64_t)blockIdx.x * 3 + q) * nbp + bn] = acc;
         }
     }
 }
@@ -938,51 +958,74 @@ static void bin_spectrum(Lattice *L, const B &binner, int kind, const std::vecto
     for (const Lattice::BinGeom &g : L->bin_geom)
         if (g.kind == kind && g.edges == edges) geom = &g;
     const bool ks = geom == nullptr;
-    int N = L->p.N;
-    int64_t half = (L->p.NDIMS == 2 ? (int64_t)N : (int64_t)N * N) * (N / 2 + 1);
+    const int N = L->p.N;
     const int nh = N / 2 + 1;
-    size_t sm = (size_t)(((4 * 3 + B::kSmemTable) * nbins + 1) & ~1) * sizeof(double) + (size_t)4 * nh * 2 * L->esz;
+    // shared memory of one block: 4 warp histograms of nbp bins x 3 rows, the
+    // bin table, 4 staged segments of seg modes. Whole rows and every bin in
+    // one pass when they fit (up to N ~ 3000); else segments of 2048 modes,
+    // then passes over the bins.
+    auto smem_of = [&](int nbp, int seg) {
+        return (size_t)((4 * 3 * nbp + B::kSmemTable * nbins + 1) & ~1) * sizeof(double) + (size_t)4 * seg * 2 * L->esz;
+    };
+    const size_t cap = 200 * 1024;
+    int nbp = nbins, seg = nh;
+    while (smem_of(nbp, seg) > cap) {
+        if (seg > 2048) seg = 2048;
+        else if (nbp > 512) nbp = (nbp + 1) / 2;
+        else if (seg > 256) seg /= 2;
+        else fail(AXS_ERR_ARG, "spectrum binning with %d bins does not fit shared memory", nbins);
+    }
+    const size_t sm = smem_of(nbp, seg);
     // as many 4-warp blocks as fit on the SMs (up to 16 per SM): the per-warp
     // histograms leave this kernel latency-bound at low occupancy
     int per_sm = (int)std::max<size_t>(1, std::min<size_t>(16, (size_t)(200 * 1024) / std::max<size_t>(sm, 1)));
     const int64_t rows = L->p.NDIMS == 2 ? (int64_t)N : (int64_t)N * N;
-    int nblk = (int)std::min<int64_t>((int64_t)num_sms() * per_sm, (rows + 3) / 4);   // whole rows per warp
-    (void)half;
-    double *part = (double *)lattice_tmp(L, 1, (size_t)nblk * 3 * nbins * sizeof(double) + (size_t)3 * nbins * sizeof(double));
-    double *out = part + (size_t)nblk * 3 * nbins;
-    {
-        auto kern = L->esz == 4 ? (ks ? (const void *)k_bin_runs<float, B, true> : (const void *)k_bin_runs<float, B, false>)
-                                : (ks ? (const void *)k_bin_runs<double, B, true> : (const void *)k_bin_runs<double, B, false>);
-        if (sm > 48 * 1024) AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const int64_t units = rows * ((nh + seg - 1) / seg);
+    int nblk = (int)std::min<int64_t>((int64_t)num_sms() * per_sm, (units + 3) / 4);   // whole segments per warp
+    double *part = (double *)lattice_tmp(L, 1, (size_t)nblk * 3 * nbp * sizeof(double) + (size_t)3 * nbp * sizeof(double));
+    double *out = part + (size_t)nblk * 3 * nbp;
+    auto kern = L->esz == 4 ? (ks ? (const void *)k_bin_runs<float, B, true> : (const void *)k_bin_runs<float, B, false>)
+                            : (ks ? (const void *)k_bin_runs<double, B, true> : (const void *)k_bin_runs<double, B, false>);
+    if (sm > 48 * 1024) AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    psum.assign(nbins, 0.0);
+    std::vector<double> nk(ks ? nbins : 0, 0.0), cc(ks ? nbins : 0, 0.0);
+    std::vector<double> h(3 * (size_t)nbp);
+    for (int b0 = 0; b0 < nbins; b0 += nbp) {
+        const int nb = std::min(nbp, nbins - b0);
         if (L->esz == 4) {
-            if (ks) k_bin_runs<float, B, true><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part);
-            else k_bin_runs<float, B, false><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part);
+            if (ks) k_bin_runs<float, B, true><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, seg, b0, nb, part);
+            else k_bin_runs<float, B, false><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, seg, b0, nb, part);
         } else {
-            if (ks) k_bin_runs<double, B, true><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part);
-            else k_bin_runs<double, B, false><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, part);
+            if (ks) k_bin_runs<double, B, true><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, seg, b0, nb, part);
+            else k_bin_runs<double, B, false><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, seg, b0, nb, part);
         }
         AXS_CUDA(cudaGetLastError());
-        k_bin_final3<<<nbins, 256, 0, L->stream>>>(part, nblk, nbins, out);
+        k_bin_final3<<<nb, 256, 0, L->stream>>>(part, nblk, nb, out);
         AXS_CUDA(cudaGetLastError());
         count_launches(2);
-        std::vector<double> h(3 * (size_t)nbins);
-        AXS_CUDA(cudaMemcpyAsync(h.data(), out, h.size() * sizeof(double), cudaMemcpyDeviceToHost, L->stream));
+        AXS_CUDA(cudaMemcpyAsync(h.data(), out, 3 * (size_t)nb * sizeof(double), cudaMemcpyDeviceToHost, L->stream));
         AXS_CUDA(cudaStreamSynchronize(L->stream));
-        psum.assign(h.begin(), h.begin() + nbins);
-        if (ks) {
-            Lattice::BinGeom g;
-            g.kind = kind;
-            g.edges = edges;
-            g.nsum.assign(h.begin() + nbins, h.begin() + 2 * nbins);
-            g.cnt.resize(nbins);
-            for (int b = 0; b < nbins; ++b) g.cnt[b] = (unsigned long long)h[2 * (size_t)nbins + b];
-            if (L->bin_geom.size() >= 8) L->bin_geom.erase(L->bin_geom.begin());
-            L->bin_geom.push_back(std::move(g));
-            geom = &L->bin_geom.back();
+        for (int b = 0; b < nb; ++b) {
+            psum[b0 + b] = h[b];
+            if (ks) {
+                nk[b0 + b] = h[(size_t)nb + b];
+                cc[b0 + b] = h[2 * (size_t)nb + b];
+            }
         }
-        nsum = geom->nsum;
-        cnt = geom->cnt;
     }
+    if (ks) {
+        Lattice::BinGeom g;
+        g.kind = kind;
+        g.edges = edges;
+        g.nsum = nk;
+        g.cnt.resize(nbins);
+        for (int b = 0; b < nbins; ++b) g.cnt[b] = (unsigned long long)cc[b];
+        if (L->bin_geom.size() >= 8) L->bin_geom.erase(L->bin_geom.begin());
+        L->bin_geom.push_back(std::move(g));
+        geom = &L->bin_geom.back();
+    }
+    nsum = geom->nsum;
+    cnt = geom->cnt;
 }
 
 void powerspec(Lattice *L, int field, double *pk, double *ks, int *count) {

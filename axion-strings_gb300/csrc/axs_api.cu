@@ -85,7 +85,10 @@ static void validate(const axs_params &p) {
     if (p.precision != AXS_F32 && p.precision != AXS_F64) fail(AXS_ERR_ARG, "precision must be 32 or 64");
     if (!(p.space_step > 0.0f)) fail(AXS_ERR_ARG, "space_step must be positive");
     if (!std::isfinite(p.time_step)) fail(AXS_ERR_ARG, "time_step must be finite");
-    if (p.N > 4096) fail(AXS_ERR_ARG, "N=%d exceeds the supported maximum 4096", p.N);
+    // 3D: |n|^2 of the spectrum binner stays below 2^24 (4096^3 would not fit
+    // the device anyway); 2D: in-plane offsets and |n|^2 stay below 2^31
+    const int nmax = p.NDIMS == 2 ? 32768 : 4096;
+    if (p.N > nmax) fail(AXS_ERR_ARG, "N=%d exceeds the supported maximum %d for %dD", p.N, nmax, p.NDIMS);
     if (p.form != 0 && p.form != 1) fail(AXS_ERR_ARG, "form must be 0 (field-rescaled) or 1 (Hamiltonian)");
     if (p.laplacian != 0 && p.laplacian != 1) fail(AXS_ERR_ARG, "laplacian must be 0 (stencil) or 1 (spectral)");
 }

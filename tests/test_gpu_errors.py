@@ -8,7 +8,8 @@ pytestmark = pytest.mark.gpu
 
 
 def test_invalid_parameters_are_rejected(axs):
-    for bad in [dict(N=31), dict(NDIMS=4), dict(stencil_setting=7), dict(precision=16), dict(N=2)]:
+    for bad in [dict(N=31), dict(NDIMS=4), dict(stencil_setting=7), dict(precision=16), dict(N=2), dict(N=4098),
+                dict(nd=2, N=32770)]:
         with pytest.raises(axs.AxsError) as e:
             axs.Lattice(params(axs, **{"nd": 3, "N": 32, "precision": 64, **bad}))
         assert e.value.code == axs.ERR_ARG
