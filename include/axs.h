@@ -61,7 +61,8 @@ typedef struct axs_params {
     int          enable_PRS;       /* read and ignored by the standard path, as in the reference */
     float        T_initial;        /* T_0: thermal mass term and thermal init           */
     int          NDIMS;            /* 2 or 3                                            */
-    int          N;                /* points per side, even                             */
+    int          N;                /* points per side, even, >= 4; at most 4096 (3D) or */
+                                   /* 32768 (2D)                                        */
     float        space_step;       /* dx                                                */
     float        time_step;        /* dt                                                */
     int          stencil_setting;  /* 0..3 -> stencil radius 1..4                       */
