@@ -100,6 +100,8 @@ _sig("axs_ensemble_destroy", [_vp])
 _sig("axs_ensemble_member", [_vp, ctypes.c_int, ctypes.POINTER(_vp)])
 _sig("axs_ensemble_evolve", [_vp, ctypes.c_int])
 _sig("axs_ensemble_evolve_timed", [_vp, ctypes.c_int, _dp])
+_sig("axs_ensemble_find_strings", [_vp, ctypes.c_void_p, ctypes.c_void_p])
+_sig("axs_ensemble_axion_spectrum", [_vp, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p])
 _sig("axs_inject_wait_timeout", [_vp])
 _sig("axs_autotune", [_vp])
 _sig("axs_describe", [_vp, ctypes.c_char_p, ctypes.c_size_t])
@@ -368,6 +370,21 @@ class Ensemble:
         b = ctypes.create_string_buffer(256)
         _check(_lib.axs_ensemble_describe(self._h, b, 256))
         return b.value.decode()
+
+    def find_strings(self):
+        """(n_plaquettes, num_cores) per member, one batched call."""
+        n = len(self.members)
+        npl, nco = np.zeros(n, np.int64), np.zeros(n, np.int64)
+        _check(_lib.axs_ensemble_find_strings(self._h, npl.ctypes.data, nco.ctypes.data))
+        return npl, nco
+
+    def axion_spectrum(self, nbins=128):
+        """(kmean, pk, count), each (members, nbins), one batched call."""
+        n = len(self.members)
+        k, pk = np.zeros((n, nbins)), np.zeros((n, nbins))
+        cnt = np.zeros((n, nbins), np.int64)
+        _check(_lib.axs_ensemble_axion_spectrum(self._h, int(nbins), k.ctypes.data, pk.ctypes.data, cnt.ctypes.data))
+        return k, pk, cnt
 
     def close(self):
         if self._h:

@@ -944,16 +944,25 @@ static void ensure_fft(Lattice *L) {
 }
 
 static void exec_r2c(Lattice *L) {
+    AXS_CUFFT(cufftSetStream(L->plan_r2c, L->stream));   // the stream of this call (batched calls use a pool)
     if (L->esz == 4) AXS_CUFFT(cufftExecR2C(L->plan_r2c, (cufftReal *)L->fft_in, (cufftComplex *)L->fft_out));
     else AXS_CUFFT(cufftExecD2Z(L->plan_r2c, (cufftDoubleReal *)L->fft_in, (cufftDoubleComplex *)L->fft_out));
 }
 
-// Bin the current fft_out; returns per-bin sums (pk, |n|) and weighted counts.
-// The |n| sums and counts of a binning (kind, edges) are computed by its first
-// call and reused afterwards, when the kernel sums the power alone.
+// A binning in flight: its result rows land in `host` (3 x nbins doubles,
+// pass by pass) when the stream reaches them. The |n| sums and counts of a
+// binning (kind, edges) are computed by its first call and reused
+// afterwards, when the kernel sums the power alone.
+struct BinPending {
+    int nbins = 0, nbp = 0, kind = 0;
+    bool ks = false;
+    std::vector<int> edges;
+    const double *host = nullptr;
+};
+
 template <typename B>
-static void bin_spectrum(Lattice *L, const B &binner, int kind, const std::vector<int> &edges, int nbins,
-                         std::vector<double> &psum, std::vector<double> &nsum, std::vector<unsigned long long> &cnt) {
+static BinPending bin_spectrum_enqueue(Lattice *L, const B &binner, int kind, const std::vector<int> &edges, int nbins,
+                                       double *host) {
     const Lattice::BinGeom *geom = nullptr;
     for (const Lattice::BinGeom &g : L->bin_geom)
         if (g.kind == kind && g.edges == edges) geom = &g;
@@ -987,9 +996,6 @@ static void bin_spectrum(Lattice *L, const B &binner, int kind, const std::vecto
     auto kern = L->esz == 4 ? (ks ? (const void *)k_bin_runs<float, B, true> : (const void *)k_bin_runs<float, B, false>)
                             : (ks ? (const void *)k_bin_runs<double, B, true> : (const void *)k_bin_runs<double, B, false>);
     if (sm > 48 * 1024) AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    psum.assign(nbins, 0.0);
-    std::vector<double> nk(ks ? nbins : 0, 0.0), cc(ks ? nbins : 0, 0.0);
-    std::vector<double> h(3 * (size_t)nbp);
     for (int b0 = 0; b0 < nbins; b0 += nbp) {
         const int nb = std::min(nbp, nbins - b0);
         if (L->esz == 4) {
@@ -1003,20 +1009,48 @@ static void bin_spectrum(Lattice *L, const B &binner, int kind, const std::vecto
         k_bin_final3<<<nb, 256, 0, L->stream>>>(part, nblk, nb, out);
         AXS_CUDA(cudaGetLastError());
         count_launches(2);
-        AXS_CUDA(cudaMemcpyAsync(h.data(), out, 3 * (size_t)nb * sizeof(double), cudaMemcpyDeviceToHost, L->stream));
-        AXS_CUDA(cudaStreamSynchronize(L->stream));
+        // rows (power, |n|, count) of this pass at host[3 b0 ..]; the next pass
+        // overwrites `out` only after this copy (stream order)
+        AXS_CUDA(cudaMemcpyAsync(host + 3 * (size_t)b0, out, 3 * (size_t)nb * sizeof(double), cudaMemcpyDeviceToHost,
+                                 L->stream));
+    }
+    BinPending pd;
+    pd.nbins = nbins;
+    pd.nbp = nbp;
+    pd.kind = kind;
+    pd.ks = ks;
+    pd.edges = edges;
+    pd.host = host;
+    return pd;
+}
+
+// After the stream reached the copies: per-bin power sums, |n| sums and
+// counts (the latter two from the lattice's cache of this binning, filled by
+// its first call).
+static void bin_spectrum_finish(Lattice *L, const BinPending &pd, std::vector<double> &psum, std::vector<double> &nsum,
+                                std::vector<unsigned long long> &cnt) {
+    const int nbins = pd.nbins;
+    psum.assign(nbins, 0.0);
+    std::vector<double> nk(pd.ks ? nbins : 0, 0.0), cc(pd.ks ? nbins : 0, 0.0);
+    for (int b0 = 0; b0 < nbins; b0 += pd.nbp) {
+        const int nb = std::min(pd.nbp, nbins - b0);
+        const double *h = pd.host + 3 * (size_t)b0;
         for (int b = 0; b < nb; ++b) {
             psum[b0 + b] = h[b];
-            if (ks) {
+            if (pd.ks) {
                 nk[b0 + b] = h[(size_t)nb + b];
                 cc[b0 + b] = h[2 * (size_t)nb + b];
             }
         }
     }
-    if (ks) {
+    const Lattice::BinGeom *geom = nullptr;
+    for (const Lattice::BinGeom &g : L->bin_geom)
+        if (g.kind == pd.kind && g.edges == pd.edges) geom = &g;
+    if (!geom) {
+        if (!pd.ks) fail(AXS_ERR_STATE, "internal: spectrum binning geometry missing");
         Lattice::BinGeom g;
-        g.kind = kind;
-        g.edges = edges;
+        g.kind = pd.kind;
+        g.edges = pd.edges;
         g.nsum = nk;
         g.cnt.resize(nbins);
         for (int b = 0; b < nbins; ++b) g.cnt[b] = (unsigned long long)cc[b];
@@ -1026,6 +1060,17 @@ static void bin_spectrum(Lattice *L, const B &binner, int kind, const std::vecto
     }
     nsum = geom->nsum;
     cnt = geom->cnt;
+}
+
+// Bin the current fft_out; returns per-bin sums (pk, |n|) and weighted counts.
+// A pageable destination makes each copy complete before the call returns.
+template <typename B>
+static void bin_spectrum(Lattice *L, const B &binner, int kind, const std::vector<int> &edges, int nbins,
+                         std::vector<double> &psum, std::vector<double> &nsum, std::vector<unsigned long long> &cnt) {
+    std::vector<double> h(3 * (size_t)nbins);
+    const BinPending pd = bin_spectrum_enqueue(L, binner, kind, edges, nbins, h.data());
+    AXS_CUDA(cudaStreamSynchronize(L->stream));
+    bin_spectrum_finish(L, pd, psum, nsum, cnt);
 }
 
 void powerspec(Lattice *L, int field, double *pk, double *ks, int *count) {
@@ -1058,7 +1103,16 @@ void powerspec(Lattice *L, int field, double *pk, double *ks, int *count) {
     }
 }
 
-void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *count) {
+// The axion spectrum of one lattice in flight: the field, the transform and
+// the binning are enqueued; thresholds travel from `thr_host` (page-locked
+// for a truly asynchronous copy, or nullptr for the lattice's own pageable
+// copy) and the result rows land in `host` (3 x nbins doubles).
+struct AxionPending {
+    BinPending bin;
+    std::vector<int> thr;
+};
+
+static AxionPending axion_spectrum_enqueue(Lattice *L, int nbins, double *host, int *thr_host) {
     if (nbins < 1) fail(AXS_ERR_ARG, "nbins must be >= 1");
     if (L->p.form != 0) fail(AXS_ERR_STATE, "the axion kinetic spectrum is defined on the field-rescaled variables (form 0)");
     ensure_fft(L);
@@ -1089,19 +1143,31 @@ void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *c
     AXS_CUDA(cudaGetLastError());
     count_launches(1);
     exec_r2c(L);
-    int d = L->p.NDIMS, N = L->p.N;
-    double ratio = sqrt((double)d) * (double)N / 2.0;
+    const int d = L->p.NDIMS, N = L->p.N;
+    const double ratio = sqrt((double)d) * (double)N / 2.0;
     // bin b starts at |n| = t_b = ratio^(b/nbins); for integer n2 the test
     // n2 >= t_b^2 is n2 >= ceil(t_b^2)
-    std::vector<int> thr(nbins, 0);
-    for (int b = 1; b < nbins; ++b) { double t = exp(log(ratio) * (double)b / (double)nbins); thr[b] = (int)ceil(t * t); }
+    AxionPending pd;
+    pd.thr.assign(nbins, 0);
+    for (int b = 1; b < nbins; ++b) { double t = exp(log(ratio) * (double)b / (double)nbins); pd.thr[b] = (int)ceil(t * t); }
     int *de2 = (int *)lattice_tmp(L, 2, nbins * sizeof(int));
+    const int *src = pd.thr.data();
+    if (thr_host) {
+        memcpy(thr_host, pd.thr.data(), nbins * sizeof(int));
+        src = thr_host;
+    }
+    AXS_CUDA(cudaMemcpyAsync(de2, src, nbins * sizeof(int), cudaMemcpyHostToDevice, L->stream));
+    pd.bin = bin_spectrum_enqueue(L, LogBinsI{de2, nbins}, 1, pd.thr, nbins, host);
+    return pd;
+}
+
+static void axion_spectrum_finish(Lattice *L, const AxionPending &pd, double *kmean, double *pk, int64_t *count) {
+    const int nbins = pd.bin.nbins, d = L->p.NDIMS, N = L->p.N;
     std::vector<double> ps, ns;
     std::vector<unsigned long long> c;
-    AXS_CUDA(cudaMemcpyAsync(de2, thr.data(), nbins * sizeof(int), cudaMemcpyHostToDevice, L->stream));
-    bin_spectrum(L, LogBinsI{de2, nbins}, 1, thr, nbins, ps, ns, c);   // synchronises before thr goes out of scope
-    double Ld = (double)N * (double)L->p.space_step;
-    double norm = pow(Ld, d) / pow((double)L->length, 2.0);
+    bin_spectrum_finish(L, pd.bin, ps, ns, c);
+    const double Ld = (double)N * (double)L->p.space_step;
+    const double norm = pow(Ld, d) / pow((double)L->length, 2.0);
     for (int b = 0; b < nbins; ++b) {
         count[b] = (int64_t)c[b];
         if (c[b]) {
@@ -1112,6 +1178,116 @@ void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *c
             pk[b] = 0.0;
         }
     }
+}
+
+void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *count) {
+    std::vector<double> h(3 * (size_t)std::max(nbins, 1));
+    const AxionPending pd = axion_spectrum_enqueue(L, nbins, h.data(), nullptr);
+    AXS_CUDA(cudaStreamSynchronize(L->stream));
+    axion_spectrum_finish(L, pd, kmean, pk, count);
+}
+
+// ---------------------------------------------------------------- batched over an ensemble
+//
+// Per member the same kernels as the single-lattice calls, enqueued back to
+// back on the ensemble's stream with the results copied into one page-locked
+// buffer, and a single synchronisation: the members' results are the bits of
+// the per-member calls.
+
+static void *ensemble_pinned(Ensemble *E, size_t bytes) {
+    if (E->hpin_cap < bytes) {
+        if (E->hpin) AXS_CUDA(cudaFreeHost(E->hpin));
+        E->hpin = nullptr;
+        E->hpin_cap = 0;
+        AXS_CUDA(cudaHostAlloc(&E->hpin, bytes, cudaHostAllocDefault));
+        E->hpin_cap = bytes;
+    }
+    return E->hpin;
+}
+
+// Members run on a pool of streams forked from and joined back into the
+// ensemble's stream; `fn(L)` enqueues one member's work on L->stream.
+template <typename Fn>
+static void ensemble_fan_out(Ensemble *E, Fn fn) {
+    const size_t n = E->members.size(), k = std::min<size_t>(8, n);
+    while (E->pool.size() < k) {
+        cudaStream_t s;
+        cudaEvent_t ev;
+        AXS_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        E->pool.push_back(s);
+        AXS_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        E->pool_ev.push_back(ev);
+    }
+    if (!E->ev_fork) AXS_CUDA(cudaEventCreateWithFlags(&E->ev_fork, cudaEventDisableTiming));
+    AXS_CUDA(cudaEventRecord(E->ev_fork, E->stream));
+    for (size_t j = 0; j < k; ++j) AXS_CUDA(cudaStreamWaitEvent(E->pool[j], E->ev_fork, 0));
+    for (size_t i = 0; i < n; ++i) {
+        Lattice *L = E->members[i];
+        cudaStream_t own = L->stream;
+        L->stream = E->pool[i % k];
+        try {
+            fn(L, i);
+        } catch (...) {
+            L->stream = own;
+            throw;
+        }
+        L->stream = own;
+    }
+    for (size_t j = 0; j < k; ++j) {
+        AXS_CUDA(cudaEventRecord(E->pool_ev[j], E->pool[j]));
+        AXS_CUDA(cudaStreamWaitEvent(E->stream, E->pool_ev[j], 0));
+    }
+}
+
+void ensemble_release_pool(Ensemble *E) {
+    for (cudaStream_t s : E->pool) cudaStreamDestroy(s);
+    for (cudaEvent_t e : E->pool_ev) cudaEventDestroy(e);
+    if (E->ev_fork) cudaEventDestroy(E->ev_fork);
+    E->pool.clear();
+    E->pool_ev.clear();
+    E->ev_fork = nullptr;
+}
+
+void ensemble_find_strings(Ensemble *E, int64_t *nplaq, int64_t *ncores) {
+    const size_t n = E->members.size();
+    if (E->members[0]->p.NDIMS == 2) {   // 2D: the neighbouring-pair count needs each member's list
+        for (size_t i = 0; i < n; ++i) find_strings(E->members[i], nullptr, nullptr, &nplaq[i], &ncores[i]);
+        return;
+    }
+    int64_t *hc = (int64_t *)ensemble_pinned(E, n * sizeof(int64_t));
+    ensemble_fan_out(E, [&](Lattice *L, size_t i) {
+        ensure_mask(L);
+        const double accept = (double)(0.5f * (1.0f - L->p.thr / 100.0f));   // string_finding.cpp:8,40
+        AXS_CUDA(cudaMemsetAsync(L->dcount, 0, 2 * sizeof(int64_t), L->stream));
+        unsigned long long *cnt = (unsigned long long *)L->dcount;
+        if (L->esz == 4) launch_cores<float>(L, false, accept, cnt);
+        else launch_cores<double>(L, false, accept, cnt);
+        AXS_CUDA(cudaMemcpyAsync(&hc[i], L->dcount, sizeof(int64_t), cudaMemcpyDeviceToHost, L->stream));
+    });
+    AXS_CUDA(cudaStreamSynchronize(E->stream));
+    for (size_t i = 0; i < n; ++i) {
+        Lattice *L = E->members[i];
+        L->last_nplaq = hc[i];
+        L->list_valid = false;
+        nplaq[i] = hc[i];
+        ncores[i] = hc[i];   // 3D: every flagged plaquette counts (s_run.cpp:112-131)
+    }
+}
+
+void ensemble_axion_spectrum(Ensemble *E, int nbins, double *kmean, double *pk, int64_t *count) {
+    if (nbins < 1) fail(AXS_ERR_ARG, "nbins must be >= 1");
+    const size_t n = E->members.size();
+    const size_t per = 3 * (size_t)nbins * sizeof(double) + (((size_t)nbins * sizeof(int) + 15) & ~(size_t)15);
+    char *base = (char *)ensemble_pinned(E, n * per);
+    std::vector<AxionPending> pend(n);
+    ensemble_fan_out(E, [&](Lattice *L, size_t i) {
+        double *h = (double *)(base + i * per);
+        int *t = (int *)(base + i * per + 3 * (size_t)nbins * sizeof(double));
+        pend[i] = axion_spectrum_enqueue(L, nbins, h, t);
+    });
+    AXS_CUDA(cudaStreamSynchronize(E->stream));
+    for (size_t i = 0; i < n; ++i)
+        axion_spectrum_finish(E->members[i], pend[i], kmean + i * nbins, pk + i * nbins, count + i * nbins);
 }
 
 // ============================================================== reductions

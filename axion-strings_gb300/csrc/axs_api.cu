@@ -694,6 +694,8 @@ int axs_ensemble_destroy(axs_ensemble *e) {
     API_BEGIN
     if (!e) return AXS_OK;
     cudaStreamSynchronize(e->E.stream);
+    if (e->E.hpin) cudaFreeHost(e->E.hpin);
+    ensemble_release_pool(&e->E);
     clear_graphs(e->E.graphs);
     dfree(e->E.dzlat);
     dfree(e->E.dcounter);
@@ -739,6 +741,20 @@ int axs_ensemble_evolve_timed(axs_ensemble *e, int nsteps, double *ms) {
     if (ms) *ms = t;
     check_device_error_flag(e->E.derr, e->E.stream);
     for (Lattice *m : e->E.members) m->last_nplaq = -1;
+    API_END
+}
+
+int axs_ensemble_find_strings(axs_ensemble *e, int64_t *n_plaquettes, int64_t *num_cores) {
+    API_BEGIN
+    if (!e || !n_plaquettes || !num_cores) fail(AXS_ERR_ARG, "null argument");
+    ensemble_find_strings(&e->E, n_plaquettes, num_cores);
+    API_END
+}
+
+int axs_ensemble_axion_spectrum(axs_ensemble *e, int nbins, double *kmean, double *pk, int64_t *count) {
+    API_BEGIN
+    if (!e || !kmean || !pk || !count) fail(AXS_ERR_ARG, "null argument");
+    ensemble_axion_spectrum(&e->E, nbins, kmean, pk, count);
     API_END
 }
 

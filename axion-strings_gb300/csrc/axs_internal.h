@@ -189,6 +189,15 @@ struct Ensemble {
     std::vector<int> tab_cur;
     std::vector<void *> tab_pih;   // 2 per member
     std::map<GraphKey, GraphEntry> graphs;
+    // page-locked host buffer of the batched analysis calls (grow only): the
+    // members' results land here asynchronously, one synchronisation per call
+    void *hpin = nullptr;
+    size_t hpin_cap = 0;
+    // streams of the batched analysis: members' kernels run concurrently
+    // (small members fill few SMs each), joined back by events
+    std::vector<cudaStream_t> pool;
+    std::vector<cudaEvent_t> pool_ev;
+    cudaEvent_t ev_fork = nullptr;
 };
 
 // ---- step module (axs_step.cu)
@@ -207,6 +216,10 @@ void launch_zmarch_r(int esz, int ty, int txmax, int slots, int r, const ZLat *d
                      int *counters, int parity, int *derr, cudaStream_t st, int ctas_per_sm);
 void prepare_zmarch_r(int esz, int ty, int txmax, int slots, int r);
 std::string ensemble_describe(const Ensemble *E);
+// ---- batched analysis over the members (axs_analysis.cu)
+void ensemble_find_strings(Ensemble *E, int64_t *nplaq, int64_t *ncores);
+void ensemble_axion_spectrum(Ensemble *E, int nbins, double *kmean, double *pk, int64_t *count);
+void ensemble_release_pool(Ensemble *E);
 void launch_sync_pi(Lattice *L);                      // scratch <- pi_n
 void launch_laplacian(Lattice *L, int comp, double *dout);
 void launch_unpack(Lattice *L, const void *src, int which, int comp, void *dst_real, int dst_is_double);

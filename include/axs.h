@@ -248,6 +248,14 @@ int axs_ensemble_destroy(axs_ensemble *e);
 int axs_ensemble_member(axs_ensemble *e, int i, axs_lattice **out);
 int axs_ensemble_evolve(axs_ensemble *e, int nsteps);
 int axs_ensemble_evolve_timed(axs_ensemble *e, int nsteps, double *ms);
+/* axs_find_strings of every member in one call (cores2/cores3,
+ * string_finding.cpp:3-86, per member): n_plaquettes[i], num_cores[i] for
+ * member i. The members' kernels run back to back with one synchronisation;
+ * the results are those of the per-member calls. */
+int axs_ensemble_find_strings(axs_ensemble *e, int64_t *n_plaquettes, int64_t *num_cores);
+/* axs_axion_spectrum of every member in one call: member i's bins at
+ * kmean/pk/count[i*nbins ..]; one synchronisation, the per-member bits. */
+int axs_ensemble_axion_spectrum(axs_ensemble *e, int nbins, double *kmean, double *pk, int64_t *count);
 
 /* ---- tuning and diagnostics ------------------------------------------------------------ */
 

@@ -68,3 +68,25 @@ def test_two_step_members_bit_identical_to_one_step_alone(axs, force, monkeypatc
 def test_ensemble_rejects_mixed_precision(axs):
     with pytest.raises(axs.AxsError):
         axs.Ensemble([params(axs, 3, 32, 32), params(axs, 3, 32, 64)])
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_batched_analysis_equals_per_member_calls(axs, precision):
+    """axs_ensemble_find_strings / axs_ensemble_axion_spectrum (every member's
+    kernels back to back, one synchronisation) give the per-member calls'
+    bits, on the first call of a binning and on later ones."""
+    specs = [(64, 1.0, 41), (32, 0.6, 42), (48, 2.0, 43), (64, 3.0, 44)]
+    plist = [params(axs, 3, N, precision, lambda_=lam, T_initial=0.0, prs=1) for N, lam, _ in specs]
+    with axs.Ensemble(plist) as E:
+        for m, (_, _, seed) in zip(E.members, specs):
+            m.init_flat(seed, 1.0)
+        E.evolve(12)
+        for rep in range(2):
+            npl, nco = E.find_strings()
+            k, pk, cnt = E.axion_spectrum(24)
+            for i, m in enumerate(E.members):
+                n1, c1, _ = m.find_strings()
+                assert (n1, c1) == (npl[i], nco[i])
+                k1, pk1, cnt1 = m.axion_spectrum(24)
+                assert np.array_equal(k1, k[i]) and np.array_equal(pk1, pk[i]) and np.array_equal(cnt1, cnt[i])
+            E.evolve(2)
