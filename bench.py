@@ -292,9 +292,19 @@ def run_ensemble(axs, dist, steps, warmup, master_seed=2026):
     sites = sum(int(p.N) ** 3 for p in plist)
     sites_all = dist.sum(sites)
     ms_max = dist.max(ms)
+    # per-output analysis of every member, batched (wall time of the
+    # synchronising calls; the first call of a binning plans the transforms)
+    E.find_strings()
+    E.axion_spectrum(128)
+    t0 = time.perf_counter()
+    E.find_strings()
+    t1 = time.perf_counter()
+    E.axion_spectrum(128)
+    t2 = time.perf_counter()
     E.close()
     return {"members": n_total, "sites": int(sites_all), "ms": ms_max, "launches": launches,
-            "sizes": [int(s) for s in sizes], "master_seed": master_seed}
+            "sizes": [int(s) for s in sizes], "master_seed": master_seed,
+            "analysis_ms": {"find_strings_all_members": 1e3 * (t1 - t0), "axion_spectrum_128_all_members": 1e3 * (t2 - t1)}}
 
 
 # --------------------------------------------------------------------- arms
@@ -361,7 +371,8 @@ def gpu_arm(args, dist):
         ens = {"value": re, "unit": "site-updates/s", "members": e["members"], "sites": e["sites"],
                "ms_per_step": e["ms"] / args.steps,
                "hbm_frac": re / dist.world * 32 * e["launches"] / args.steps / 1e9 / hbm,
-               "master_seed": e["master_seed"], "launches_per_step": e["launches"] / args.steps}
+               "master_seed": e["master_seed"], "launches_per_step": e["launches"] / args.steps,
+               "analysis_ms": e["analysis_ms"]}
     cpu = None
     if dist.rank == 0 and not args.no_cpu:
         rate, steps_done, secs, threads = cpu_port_rate(n=256, target_s=10.0)
