@@ -1221,6 +1221,12 @@ static void ensemble_fan_out(Ensemble *E, Fn fn) {
     if (!E->ev_fork) AXS_CUDA(cudaEventCreateWithFlags(&E->ev_fork, cudaEventDisableTiming));
     AXS_CUDA(cudaEventRecord(E->ev_fork, E->stream));
     for (size_t j = 0; j < k; ++j) AXS_CUDA(cudaStreamWaitEvent(E->pool[j], E->ev_fork, 0));
+    auto join = [&] {   // the ensemble's stream waits for everything enqueued on the pool
+        for (size_t j = 0; j < k; ++j) {
+            cudaEventRecord(E->pool_ev[j], E->pool[j]);
+            cudaStreamWaitEvent(E->stream, E->pool_ev[j], 0);
+        }
+    };
     for (size_t i = 0; i < n; ++i) {
         Lattice *L = E->members[i];
         cudaStream_t own = L->stream;
@@ -1229,14 +1235,13 @@ static void ensemble_fan_out(Ensemble *E, Fn fn) {
             fn(L, i);
         } catch (...) {
             L->stream = own;
+            join();   // later work on the ensemble stays ordered after what did get enqueued
             throw;
         }
         L->stream = own;
     }
-    for (size_t j = 0; j < k; ++j) {
-        AXS_CUDA(cudaEventRecord(E->pool_ev[j], E->pool[j]));
-        AXS_CUDA(cudaStreamWaitEvent(E->stream, E->pool_ev[j], 0));
-    }
+    join();
+    AXS_CUDA(cudaGetLastError());
 }
 
 void ensemble_release_pool(Ensemble *E) {
