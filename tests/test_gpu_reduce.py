@@ -8,13 +8,20 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("precision,tol", [(64, 1e-12), (32, 2e-6)])
-@pytest.mark.parametrize("nd,N", [(2, 64), (3, 32)])
-def test_background_and_energies(axs, oracle, precision, tol, nd, N):
-    p = params(axs, nd, N, precision, T_initial=0.0)
+@pytest.mark.parametrize("nd,N,stencil,steps,prs", [
+    (2, 64, 0, 15, 1), (3, 32, 0, 15, 1),
+    (3, 20, 0, 15, 1),    # columns past the edge of the 32 x 8 blocks
+    (3, 36, 0, 9, 0),
+    (3, 32, 0, 0, 1),     # a fresh state: pih holds pi_0
+    (3, 24, 1, 15, 1),    # radius 2: pi_n formed in scratch first
+])
+def test_background_and_energies(axs, oracle, precision, tol, nd, N, stencil, steps, prs):
+    p = params(axs, nd, N, precision, T_initial=0.0, stencil_setting=stencil, prs=prs)
     op = orc(p)
     with axs.Lattice(p) as L:
         L.init_flat(6, 1.0)
-        L.evolve(15)
+        if steps:
+            L.evolve(steps)
         g = L.download()
         tau, _ = L.time
         bg = L.background()
