@@ -881,7 +881,7 @@ __global__ void k_gather_axion(const typename Cplx<T>::type *__restrict__ psi, c
 // thread; offsets within a plane are 32-bit (N^2 < 2^31) to keep the float
 // thread within 64 registers (4 blocks per SM). N >= 4, so z + 3 < 2N.
 template <typename T>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_axion_zcol(const typename Cplx<T>::type *__restrict__ psi,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_axion_zcol(const typename Cplx<T>::type *__restrict__ psi,
                                                        const typename Cplx<T>::type *__restrict__ pih,
                                                        T *__restrict__ dst, const double *clock, int N, double dt,
                                                        double inv_dx2, double lambda, double T0sq3, int prs, int fresh,
@@ -895,38 +895,49 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_axion_zcol(cons
     const int col = y * N + x;
     const int xm = y * N + (x == 0 ? N - 1 : x - 1) - col, xp = y * N + (x == N - 1 ? 0 : x + 1) - col;
     const int ym = (y == 0 ? N - 1 : y - 1) * N + x - col, yp = (y == N - 1 ? 0 : y + 1) * N + x - col;
-    auto plane = [N](int z) { return z >= N ? z - N : z; };   // for z < 2N
     // column values: psi planes z-1, z, z+1 in use, z+2 and z+3 in flight;
     // pih plane z in use, z+1 and z+2 in flight; neighbours of plane z in use
-    // (loaded last iteration), those of z+1 in flight
+    // (loaded last iteration), those of z+1 in flight. Column pointers advance
+    // a plane per site and wrap once near the end; two sites per trip (N is
+    // even), so the register rotation is renaming.
+    const int64_t len = NN * N;
     C zm = psi[(int64_t)(N - 1) * NN + col], zc = psi[col];
     C zp = psi[NN + col], zq = psi[2 * NN + col];
     C pc = pih[col], pq = pih[NN + col];
     C a, b, d, e;
     if (!fresh) { a = psi[col + xm]; b = psi[col + xp]; d = psi[col + ym]; e = psi[col + yp]; }
-    for (int z = 0; z < N; ++z) {
-        const int64_t base = (int64_t)z * NN;
-        const int64_t b1 = (int64_t)plane(z + 1) * NN;
-        const C zr = psi[(int64_t)plane(z + 3) * NN + col];
-        const C pr = pih[(int64_t)plane(z + 2) * NN + col];
-        C p = pc;
-        if (!fresh) {   // a fresh state holds pi_0 itself (the reference's ker is zero)
-            const C na = psi[b1 + col + xm], nb = psi[b1 + col + xp], nd = psi[b1 + col + ym], ne = psi[b1 + col + yp];
-            const T L1 = lap7<T>(zc.x, a.x, b.x, d.x, e.x, zm.x, zp.x);
-            const T L2 = lap7<T>(zc.y, a.y, b.y, d.y, e.y, zm.y, zp.y);
-            sync_pi_site<T>(zc.x, zc.y, L1, L2, p.x, p.y, c);
-            a = na;
-            b = nb;
-            d = nd;
-            e = ne;
+    const C *s3 = psi + 3 * NN + col, *p2 = pih + 2 * NN + col, *s1 = psi + NN + col;   // planes z+3, z+2, z+1
+    T *out = dst + col;
+    for (int z = 0; z < N; z += 2) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int zz = z + h;
+            const C zr = *(zz + 3 < N ? s3 : s3 - len);
+            const C pr = *(zz + 2 < N ? p2 : p2 - len);
+            const C *q1 = zz + 1 < N ? s1 : s1 - len;
+            s3 += NN;
+            p2 += NN;
+            s1 += NN;
+            C p = pc;
+            if (!fresh) {   // a fresh state holds pi_0 itself (the reference's ker is zero)
+                const C na = q1[xm], nb = q1[xp], nd = q1[ym], ne = q1[yp];
+                const T L1 = lap7<T>(zc.x, a.x, b.x, d.x, e.x, zm.x, zp.x);
+                const T L2 = lap7<T>(zc.y, a.y, b.y, d.y, e.y, zm.y, zp.y);
+                sync_pi_site<T>(zc.x, zc.y, L1, L2, p.x, p.y, c);
+                a = na;
+                b = nb;
+                d = nd;
+                e = ne;
+            }
+            *out = axion_f<T>(zc.x, zc.y, p.x, p.y, itau);
+            out += NN;
+            zm = zc;
+            zc = zp;
+            zp = zq;
+            zq = zr;
+            pc = pq;
+            pq = pr;
         }
-        dst[base + col] = axion_f<T>(zc.x, zc.y, p.x, p.y, itau);
-        zm = zc;
-        zc = zp;
-        zp = zq;
-        zq = zr;
-        pc = pq;
-        pq = pr;
     }
 }
 
@@ -1388,9 +1399,18 @@ __global__ void __launch_bounds__(256) k_energies(const typename Cplx<T>::type *
 // neighbouring threads' loads of the same plane. 16 B from DRAM per site
 // instead of 40 B through scratch. Blocks are 256 threads over 32 x 8 columns
 // (threads past the edge add nothing); each block writes its partial sums at
-// its index, so the totals are deterministic. N >= 4, so z + 3 < 2N.
+// its index, so the totals are deterministic.
+//
+// The kernel is issue-bound, so the march is arranged for few instructions per
+// site: three column pointers advance a plane per site (wrapping once, near the
+// end), two sites per trip (N is even) so the register rotation is renaming,
+// the two sites' terms are added in plain T before one compensated add, and
+// the energies' constant factors (1/2 tau^-2, 1/2 (tau dx)^-2, lambda/4) are
+// applied to the column sums: the sums are of (pi - psi/tau)^2, of the
+// squared differences of psi and of (|psi|^2/tau^2 - 1)^2. Float energies fit
+// 64 registers (4 CTAs per SM); the background's atan2f needs 80 (3). N >= 4.
 template <typename T, int KIND>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_reduce_zcol(const typename Cplx<T>::type *__restrict__ psi,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? (KIND == 1 ? 4 : 3) : 2) k_reduce_zcol(const typename Cplx<T>::type *__restrict__ psi,
                                                          const typename Cplx<T>::type *__restrict__ pih,
                                                          double *__restrict__ partials, const double *clock, int N,
                                                          double dt, double inv_dx2, double lambda, double T0sq3,
@@ -1403,65 +1423,82 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_reduce_zcol(con
     const int x = (int)(blockIdx.x % bx) * 32 + (threadIdx.x & 31), y = (int)(blockIdx.x / bx) * 8 + (threadIdx.x >> 5);
     if (x < N && y < N) {
         const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs, form);
-        const T it = (T)(1.0 / tau), idx = (T)(1.0 / dx), q = (T)(0.25 * lam_eff);
+        const T it = (T)(1.0 / tau), it2 = (T)(1.0 / (tau * tau));
         const bool nbrs = KIND == 1 || !fresh;   // the energies' differences need them even for pi_0
-        const int64_t NN = (int64_t)N * N;
+        const int64_t NN = (int64_t)N * N, len = NN * N;
         const int col = y * N + x;
         const int xm = y * N + (x == 0 ? N - 1 : x - 1) - col, xp = y * N + (x == N - 1 ? 0 : x + 1) - col;
         const int ym = (y == 0 ? N - 1 : y - 1) * N + x - col, yp = (y == N - 1 ? 0 : y + 1) * N + x - col;
-        auto plane = [N](int z) { return z >= N ? z - N : z; };   // for z < 2N
-        C zm = psi[(int64_t)(N - 1) * NN + col], zc = psi[col];
+        // column values: psi planes z-1, z, z+1 in use, z+2 and z+3 in flight;
+        // pih plane z in use, z+1 and z+2 in flight; neighbours of plane z in
+        // use (loaded a site earlier), those of z+1 in flight
+        C zm = psi[(N - 1) * NN + col], zc = psi[col];
         C zp = psi[NN + col], zq = psi[2 * NN + col];
         C pc = pih[col], pq = pih[NN + col];
         C a, b, d, e;
         if (nbrs) { a = psi[col + xm]; b = psi[col + xp]; d = psi[col + ym]; e = psi[col + yp]; }
-        for (int z = 0; z < N; ++z) {
-            const int64_t b1 = (int64_t)plane(z + 1) * NN;
-            const C zr = psi[(int64_t)plane(z + 3) * NN + col];
-            const C pr = pih[(int64_t)plane(z + 2) * NN + col];
-            C na, nb, nd, ne;
-            if (nbrs) { na = psi[b1 + col + xm]; nb = psi[b1 + col + xp]; nd = psi[b1 + col + ym]; ne = psi[b1 + col + yp]; }
-            C p = pc;
-            if (!fresh) {   // a fresh state holds pi_0 itself (the reference's ker is zero)
-                const T L1 = lap7<T>(zc.x, a.x, b.x, d.x, e.x, zm.x, zp.x);
-                const T L2 = lap7<T>(zc.y, a.y, b.y, d.y, e.y, zm.y, zp.y);
-                sync_pi_site<T>(zc.x, zc.y, L1, L2, p.x, p.y, c);
+        const C *s3 = psi + 3 * NN + col, *p2 = pih + 2 * NN + col, *s1 = psi + NN + col;   // planes z+3, z+2, z+1
+        for (int z = 0; z < N; z += 2) {
+            T t[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) t[k] = 0;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int zz = z + h;
+                const C zr = *(zz + 3 < N ? s3 : s3 - len);
+                const C pr = *(zz + 2 < N ? p2 : p2 - len);
+                const C *q1 = zz + 1 < N ? s1 : s1 - len;
+                s3 += NN;
+                p2 += NN;
+                s1 += NN;
+                C na, nb, nd, ne;
+                if (nbrs) { na = q1[xm]; nb = q1[xp]; nd = q1[ym]; ne = q1[yp]; }
+                C p = pc;
+                if (!fresh) {   // a fresh state holds pi_0 itself (the reference's ker is zero)
+                    const T L1 = lap7<T>(zc.x, a.x, b.x, d.x, e.x, zm.x, zp.x);
+                    const T L2 = lap7<T>(zc.y, a.y, b.y, d.y, e.y, zm.y, zp.y);
+                    sync_pi_site<T>(zc.x, zc.y, L1, L2, p.x, p.y, c);
+                }
+                if (KIND == 0) {
+                    t[0] += zc.x;
+                    t[1] += zc.y;
+                    t[2] += p.x;
+                    t[3] += p.y;
+                    t[4] += fabs(atan2(zc.x, zc.y));
+                    t[5] += sqrt(zc.x * zc.x + zc.y * zc.y);
+                } else {   // differences in the order x, y, z
+                    const T e1 = fma(-zc.x, it, p.x), e2 = fma(-zc.y, it, p.y);
+                    t[0] += fma(e1, e1, e2 * e2);
+                    T g1 = b.x - zc.x, g2 = b.y - zc.y;
+                    T g = fma(g1, g1, g2 * g2);
+                    g1 = e.x - zc.x;
+                    g2 = e.y - zc.y;
+                    g = fma(g1, g1, fma(g2, g2, g));
+                    g1 = zp.x - zc.x;
+                    g2 = zp.y - zc.y;
+                    t[1] += fma(g1, g1, fma(g2, g2, g));
+                    const T r = fma(it2, fma(zc.x, zc.x, zc.y * zc.y), (T)-1);
+                    t[2] += r * r;
+                }
+                if (nbrs) { a = na; b = nb; d = nd; e = ne; }
+                zm = zc;
+                zc = zp;
+                zp = zq;
+                zq = zr;
+                pc = pq;
+                pq = pr;
             }
-            if (KIND == 0) {
-                acc[0].add(zc.x);
-                acc[1].add(zc.y);
-                acc[2].add(p.x);
-                acc[3].add(p.y);
-                acc[4].add(fabs(atan2(zc.x, zc.y)));
-                acc[5].add(sqrt(zc.x * zc.x + zc.y * zc.y));
-            } else {   // k_energies' terms, differences in the order x, y, z
-                const T f1 = zc.x * it, f2 = zc.y * it;
-                const T d1 = (p.x - f1) * it, d2 = (p.y - f2) * it;
-                acc[0].add((T)0.5 * (d1 * d1 + d2 * d2));
-                T g = 0;
-                T g1 = (b.x * it - f1) * idx, g2 = (b.y * it - f2) * idx;
-                g += g1 * g1 + g2 * g2;
-                g1 = (e.x * it - f1) * idx;
-                g2 = (e.y * it - f2) * idx;
-                g += g1 * g1 + g2 * g2;
-                g1 = (zp.x * it - f1) * idx;
-                g2 = (zp.y * it - f2) * idx;
-                g += g1 * g1 + g2 * g2;
-                acc[1].add((T)0.5 * g);
-                const T r = f1 * f1 + f2 * f2 - (T)1;
-                acc[2].add(q * r * r);
-            }
-            if (nbrs) { a = na; b = nb; d = nd; e = ne; }
-            zm = zc;
-            zc = zp;
-            zp = zq;
-            zq = zr;
-            pc = pq;
-            pq = pr;
+#pragma unroll
+            for (int k = 0; k < K; ++k) acc[k].add(t[k]);
         }
     }
     double v[K];
     for (int k = 0; k < K; ++k) v[k] = acc[k].value();
+    if (KIND == 1) {
+        v[0] *= 0.5 / (tau * tau);
+        v[1] *= 0.5 / (tau * tau * dx * dx);
+        v[2] *= 0.25 * lam_eff;
+    }
     block_reduce_store<K>(v, partials);
 }
 

@@ -220,6 +220,12 @@ def run_lattice(axs, dist, precision, steps, warmup, with_e2e, sampler=None, n=N
     L.axion_spectrum(128)
     t_spec = time.perf_counter() - t0
     rec["analysis_ms"] = {"find_strings": 1e3 * t_str, "axion_spectrum_128": 1e3 * t_spec}
+    for name, fn in (("background", L.background), ("energies", L.energies)):
+        fn()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            fn()
+        rec["analysis_ms"][name] = 1e3 * (time.perf_counter() - t0) / 3
     if with_e2e:
         rec["e2e"] = e2e_leg(axs, L, dist, E2E_STEPS)
     L.close()
