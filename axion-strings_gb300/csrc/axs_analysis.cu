@@ -157,8 +157,16 @@ __global__ void __launch_bounds__(256) k_cores(const typename Cplx<T>::type *__r
 // z-chunk; the normalised angles n = (theta+pi)/(2pi) of the tile's sites (one
 // site of halo in +x and +y) are computed once per site into a two-plane
 // shared ring (k_cores evaluates them once per corner, six times per site).
-// Same float n, same margin test, same double replay: same decisions.
+// Each thread owns a run of four cells along x in one row and keeps the angles
+// of plane z (rows y, y+1, five sites each) and the circular distances of
+// their y-edges in registers, so per plane it reads ten angles of plane z+1
+// (two 16-byte and two 4-byte shared loads) and forms 21 edge distances for
+// its four cells instead of 32; the four mask bytes go out as one 32-bit store
+// when N is a multiple of 4. The edge sums keep k_cores' association order:
+// same float sums, same margin test, same double replay, same decisions.
 static constexpr int kCX = 64, kCY = 16, kCZ = 32;   // cells per block tile; 256 threads x 4 cells
+static_assert(kCZ * 4 <= 128, "two 64-bit words of margin bits per thread");
+static constexpr int kRS = kCX + 4;                   // shared row stride: 16-byte aligned rows, +x halo at kCX
 
 template <typename T>
 __global__ void __launch_bounds__(256, 3) k_cores3_tiled(const typename Cplx<T>::type *__restrict__ psi,
@@ -167,40 +175,38 @@ __global__ void __launch_bounds__(256, 3) k_cores3_tiled(const typename Cplx<T>:
     typedef typename Cplx<T>::type C;
     constexpr int NS = (kCX + 1) * (kCY + 1);   // sites of a plane tile with its +x/+y halo
     constexpr int PER = (NS + 255) / 256;
-    __shared__ float nsm[2][kCY + 1][kCX + 1];
+    __shared__ __align__(16) float nsm[2][kCY + 1][kRS];
     Corner<T, false> cn{psi, nullptr};
     const float acc_f = (float)accept;
     const int64_t NN = (int64_t)N * N;
     const int x0 = blockIdx.x * kCX, y0 = blockIdx.y * kCY, z0 = blockIdx.z * kCZ;
     const int z1 = min(N, z0 + kCZ);
     const int tid = threadIdx.x;
-    const int cx = tid % 32, cy = tid / 32;
+    const int lx = 4 * (tid & 15), ly = tid >> 4;   // the thread's cells: (lx .. lx+3, ly) of the tile
+    const int gx = x0 + lx, gy = y0 + ly;
     unsigned long long local = 0;
     // Per-thread offsets do not depend on z: the tile sites this thread loads
-    // (in-plane offset, shared index; -1 when outside) and its two cells.
+    // (in-plane offset, shared index; -1 when outside).
     int so[PER], si[PER];
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
         const int s = tid + k * 256;
         const int sx = s % (kCX + 1), sy = s / (kCX + 1);
-        int gx = x0 + sx, gy = y0 + sy;
+        int sgx = x0 + sx, sgy = y0 + sy;
         si[k] = -1;
         so[k] = 0;
-        if (s >= NS || gx > N || gy > N) continue;
-        gx = gx >= N ? gx - N : gx;
-        gy = gy >= N ? gy - N : gy;
-        so[k] = gy * N + gx;
-        si[k] = sy * (kCX + 1) + sx;
+        if (s >= NS || sgx > N || sgy > N) continue;
+        sgx = sgx >= N ? sgx - N : sgx;
+        sgy = sgy >= N ? sgy - N : sgy;
+        so[k] = sgy * N + sgx;
+        si[k] = sy * kRS + sx;
     }
-    // cells (cx + 32 (c & 1), cy + 8 (c >> 1)) of the tile
-    int co[4];
-    bool cv[4];
+    const bool row_ok = gy < N;
+    const bool packed = row_ok && (N & 3) == 0 && gx < N;   // then gx + 3 < N and the store is 4-byte aligned
+    int vmask = 0;   // bit j: cell (gx + j, gy) is in the lattice
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        const int x = x0 + cx + 32 * (c & 1), y = y0 + cy + 8 * (c >> 1);
-        cv[c] = x < N && y < N;
-        co[c] = cv[c] ? y * N + x : 0;
-    }
+    for (int j = 0; j < 4; ++j) vmask |= (row_ok && gx + j < N) ? 1 << j : 0;
+    unsigned long long unc0 = 0, unc1 = 0;   // bit 4 (z - z0) + j: cell within the float margin (kCZ = 32 planes)
     C pre[PER];   // psi of the next plane's tile, loaded one plane ahead
     auto load = [&](int z) {
         const C *pl = psi + (int64_t)(z >= N ? z - N : z) * NN;
@@ -214,35 +220,90 @@ __global__ void __launch_bounds__(256, 3) k_cores3_tiled(const typename Cplx<T>:
         for (int k = 0; k < PER; ++k)
             if (si[k] >= 0) dst[si[k]] = fmaf(fast_atan2((float)pre[k].x, (float)pre[k].y), 0.15915494309189535f, 0.5f);
     };
+    // angles of rows ly, ly+1 at x = lx .. lx+4 of a buffered plane
+    auto read = [&](int buf, float (&r0)[5], float (&r1)[5]) {
+        const float4 u = *reinterpret_cast<const float4 *>(&nsm[buf][ly][lx]);
+        const float4 v = *reinterpret_cast<const float4 *>(&nsm[buf][ly + 1][lx]);
+        r0[0] = u.x; r0[1] = u.y; r0[2] = u.z; r0[3] = u.w; r0[4] = nsm[buf][ly][lx + 4];
+        r1[0] = v.x; r1[1] = v.y; r1[2] = v.z; r1[3] = v.w; r1[4] = nsm[buf][ly + 1][lx + 4];
+    };
+    float a0[5], a1[5], ya[5];   // plane z: rows y, y+1 and their y-edge distances
     load(z0);
     store(0);
     load(z0 + 1);
-    for (int z = z0; z < z1; ++z) {
-        const int cur = (z - z0) & 1;
-        store(cur ^ 1);                 // plane z+1
+    __syncthreads();
+    read(0, a0, a1);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) ya[i] = circf(a0[i], a1[i]);
+    // One plane: plane z+1 goes into buffer nb, the one last read two planes
+    // ago (every thread is past the previous barrier, so done with it).
+    auto plane_step = [&](const int z, const int nb) {
+        store(nb);
         if (z + 2 <= z1) load(z + 2);   // in flight while plane z is evaluated
         __syncthreads();
-        uint8_t *mz = mask + (int64_t)z * NN;
+        float b0[5], b1[5], yb[5];
+        read(nb, b0, b1);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            if (!cv[c]) continue;
-            const int lx = cx + 32 * (c & 1), ly = cy + 8 * (c >> 1);
-            const float f000 = nsm[cur][ly][lx], f100 = nsm[cur ^ 1][ly][lx], f110 = nsm[cur ^ 1][ly + 1][lx],
-                        f010 = nsm[cur][ly + 1][lx], f011 = nsm[cur][ly + 1][lx + 1], f001 = nsm[cur][ly][lx + 1];
-            const float e_000_100 = circf(f000, f100);
-            const float e_011_001 = circf(f011, f001);
-            const float sa = e_000_100 + circf(f100, f110) + circf(f110, f010);
-            const float sb = e_000_100 + circf(f100, f011) + e_011_001;   // plaquette b, string_finding.cpp:54-57
-            const float sc = circf(f000, f010) + circf(f010, f011) + e_011_001;
+        for (int i = 0; i < 5; ++i) yb[i] = circf(b0[i], b1[i]);
+        unsigned word = 0;
+        int nflag = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            // f000 = a0[j], f001 = a0[j+1], f010 = a1[j], f011 = a1[j+1],
+            // f100 = b0[j], f110 = b1[j]
+            const float e_000_100 = circf(a0[j], b0[j]);
+            const float sa = e_000_100 + yb[j] + circf(b1[j], a1[j]);
+            const float sb = e_000_100 + circf(b0[j], a1[j + 1]) + ya[j + 1];   // plaquette b, string_finding.cpp:54-57
+            const float sc = ya[j] + circf(a1[j], a1[j + 1]) + ya[j + 1];
             const float mx = fmaxf(sa, fmaxf(sb, sc));
-            int flag;
-            if (mx > acc_f + kMargin) flag = 1;
-            else if (mx < acc_f - kMargin) flag = 0;
-            else flag = cell3_exact<T, false>(cn, x0 + lx, y0 + ly, z, N, accept);
-            mz[co[c]] = (uint8_t)flag;
-            local += flag;
+            int flag = 0;
+            if ((vmask >> j) & 1) {
+                if (mx > acc_f + kMargin) flag = 1;
+                else if (!(mx < acc_f - kMargin)) {   // within the margin: the double replay, after the march
+                    const int b = (z - z0) * 4 + j;
+                    if (b < 64) unc0 |= 1ull << b;
+                    else unc1 |= 1ull << (b - 64);
+                }
+            }
+            word |= (unsigned)flag << (8 * j);
+            nflag += flag;
         }
-        __syncthreads();   // plane z's buffer is refilled with plane z+2 next
+        uint8_t *mz = mask + (int64_t)z * NN + (int64_t)gy * N + gx;
+        if (packed) *reinterpret_cast<unsigned *>(mz) = word;
+        else if (row_ok) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (gx + j < N) mz[j] = (uint8_t)(word >> (8 * j));
+        }
+        local += nflag;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            a0[i] = b0[i];
+            a1[i] = b1[i];
+            ya[i] = yb[i];
+        }
+    };
+    // two planes per trip (a chunk has an even number of planes: N and kCZ
+    // are even), so the buffer indices are constants and the carried
+    // registers alternate instead of moving
+    for (int z = z0; z < z1; z += 2) {
+        plane_step(z, 1);
+        plane_step(z + 1, 0);
+    }
+    // The cells within the float margin (written 0 above) take the exact
+    // double decision here, where little else is live across the call.
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+        unsigned long long u = h ? unc1 : unc0;
+        while (u) {
+            const int b = __ffsll((long long)u) - 1 + 64 * h;
+            u &= u - 1;
+            const int zz = z0 + (b >> 2), j = b & 3;
+            if (cell3_exact<T, false>(cn, gx + j, gy, zz, N, accept)) {
+                mask[(int64_t)zz * NN + (int64_t)gy * N + gx + j] = 1;
+                ++local;
+            }
+        }
     }
     for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
     if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
@@ -1326,21 +1387,67 @@ template <> struct Acc<double> {
     __device__ __forceinline__ double value() const { return s; }
 };
 
+// |theta| = |atan2(phi1, phi2)| for the background mean: float fields take
+// fast_atan2 (within 5e-7 rad, a tenth of the float means' 2e-6 tolerance
+// relative to a mean |theta| near pi/2), FP64 fields the library atan2.
+__device__ __forceinline__ float abs_theta(float a, float b) { return fabsf(fast_atan2(a, b)); }
+__device__ __forceinline__ double abs_theta(double a, double b) { return fabs(atan2(a, b)); }
+
+// Two neighbouring sites q = 2i, 2i+1 (one 16-byte load for float fields).
+__device__ __forceinline__ void load_pair(const float2 *__restrict__ a, int64_t i, float2 (&v)[2]) {
+    const float4 w = reinterpret_cast<const float4 *>(a)[i];
+    v[0] = make_float2(w.x, w.y);
+    v[1] = make_float2(w.z, w.w);
+}
+__device__ __forceinline__ void load_pair(const double2 *__restrict__ a, int64_t i, double2 (&v)[2]) {
+    v[0] = a[2 * i];
+    v[1] = a[2 * i + 1];
+}
+
+// Background means (s_run.cpp:135-150) of psi and pi_n in one streaming pass
+// over psi and pih, for every lattice kind. pi_n = pih + dt/2 K(psi) needs no
+// neighbours for its mean: on a periodic lattice every site is the neighbour
+// of as many sites as the stencil has points, so the Laplacian part of K sums
+// to W sum(psi), W the sum of the stencil's weights (zero for the 5- and
+// 7-point stencils, ~1e-7 for the reference's float weights of radius 2-4;
+// the spectral operator has no k = 0 mode). The kernel sums the mean of pih
+// plus the local part of the half kick and the host adds dt/2 W/dx^2 mean(psi).
+// That equals the mean of the per-site pi_n up to rounding (FP64: within
+// 1e-12 of the oracle's per-site sums) and reads 16 B per site instead of
+// k_sync_pi's 24 B plus 16 B. Two sites per trip
+// (N^d is even), their terms added before one compensated add; the grid is
+// one wave of resident blocks.
 template <typename T>
-__global__ void __launch_bounds__(256) k_background(const typename Cplx<T>::type *__restrict__ psi,
-                                                    const typename Cplx<T>::type *__restrict__ pi, int64_t len,
-                                                    double *__restrict__ partials) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_background(const typename Cplx<T>::type *__restrict__ psi,
+                                                       const typename Cplx<T>::type *__restrict__ pih,
+                                                       const double *clock, int64_t len, double dt, double lambda,
+                                                       double T0sq3, int prs, int form, int fresh,
+                                                       double *__restrict__ partials) {
+    typedef typename Cplx<T>::type C;
+    const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, 0.0, lambda, T0sq3, prs, form);
     Acc<T> a[6];
-    int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
-        auto f = psi[m];
-        auto p = pi[m];
-        a[0].add(f.x);
-        a[1].add(f.y);
-        a[2].add(p.x);
-        a[3].add(p.y);
-        a[4].add(fabs(atan2(f.x, f.y)));
-        a[5].add(sqrt(f.x * f.x + f.y * f.y));
+    const int64_t npair = len >> 1;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+#pragma unroll 2
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npair; i += stride) {
+        C f[2], p[2];
+        load_pair(psi, i, f);
+        load_pair(pih, i, p);
+        T t[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) t[k] = 0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (!fresh) sync_pi_site<T>(f[h].x, f[h].y, (T)0, (T)0, p[h].x, p[h].y, c);   // a fresh pih is pi_0
+            t[0] += f[h].x;
+            t[1] += f[h].y;
+            t[2] += p[h].x;
+            t[3] += p[h].y;
+            t[4] += abs_theta(f[h].x, f[h].y);
+            t[5] += sqrt(f[h].x * f[h].x + f[h].y * f[h].y);
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a[k].add(t[k]);
     }
     double v[6];
     for (int k = 0; k < 6; ++k) v[k] = a[k].value();
@@ -1390,8 +1497,9 @@ __global__ void __launch_bounds__(256) k_energies(const typename Cplx<T>::type *
     block_reduce_store<3>(v, partials);
 }
 
-// Background means (KIND 0) and energy densities (KIND 1) of a 3D radius-1
-// lattice in one pass over psi and pih. pi_n is formed per site with
+// Energy densities of a 3D radius-1 lattice in one pass over psi and pih
+// (the kinetic term is quadratic in pi_n, so unlike the background means it
+// needs the full half kick per site). pi_n is formed per site with
 // k_sync_pi's arithmetic and never stored, and each thread marches one (x, y)
 // column through z as k_axion_zcol does: psi's z-neighbours stay in registers
 // and the in-plane neighbours (also the x+1, y+1 forward differences of the
@@ -1405,26 +1513,25 @@ __global__ void __launch_bounds__(256) k_energies(const typename Cplx<T>::type *
 // site: three column pointers advance a plane per site (wrapping once, near the
 // end), two sites per trip (N is even) so the register rotation is renaming,
 // the two sites' terms are added in plain T before one compensated add, and
-// the energies' constant factors (1/2 tau^-2, 1/2 (tau dx)^-2, lambda/4) are
-// applied to the column sums: the sums are of (pi - psi/tau)^2, of the
-// squared differences of psi and of (|psi|^2/tau^2 - 1)^2. Float energies fit
-// 64 registers (4 CTAs per SM); the background's atan2f needs 80 (3). N >= 4.
-template <typename T, int KIND>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? (KIND == 1 ? 4 : 3) : 2) k_reduce_zcol(const typename Cplx<T>::type *__restrict__ psi,
+// the constant factors (1/2 tau^-2, 1/2 (tau dx)^-2, lambda/4) are applied to
+// the column sums: the sums are of (pi - psi/tau)^2, of the squared
+// differences of psi and of (|psi|^2/tau^2 - 1)^2. Float fields fit 64
+// registers (4 CTAs per SM). N >= 4.
+template <typename T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_energies_zcol(const typename Cplx<T>::type *__restrict__ psi,
                                                          const typename Cplx<T>::type *__restrict__ pih,
                                                          double *__restrict__ partials, const double *clock, int N,
                                                          double dt, double inv_dx2, double lambda, double T0sq3,
                                                          int prs, int form, int fresh, double tau, double dx,
                                                          double lam_eff) {
     typedef typename Cplx<T>::type C;
-    constexpr int K = KIND == 0 ? 6 : 3;
+    constexpr int K = 3;
     Acc<T> acc[K];
     const int bx = (N + 31) / 32;
     const int x = (int)(blockIdx.x % bx) * 32 + (threadIdx.x & 31), y = (int)(blockIdx.x / bx) * 8 + (threadIdx.x >> 5);
     if (x < N && y < N) {
         const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs, form);
         const T it = (T)(1.0 / tau), it2 = (T)(1.0 / (tau * tau));
-        const bool nbrs = KIND == 1 || !fresh;   // the energies' differences need them even for pi_0
         const int64_t NN = (int64_t)N * N, len = NN * N;
         const int col = y * N + x;
         const int xm = y * N + (x == 0 ? N - 1 : x - 1) - col, xp = y * N + (x == N - 1 ? 0 : x + 1) - col;
@@ -1436,7 +1543,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (KIND == 1 ? 4 : 3) : 2)
         C zp = psi[NN + col], zq = psi[2 * NN + col];
         C pc = pih[col], pq = pih[NN + col];
         C a, b, d, e;
-        if (nbrs) { a = psi[col + xm]; b = psi[col + xp]; d = psi[col + ym]; e = psi[col + yp]; }
+        { a = psi[col + xm]; b = psi[col + xp]; d = psi[col + ym]; e = psi[col + yp]; }
         const C *s3 = psi + 3 * NN + col, *p2 = pih + 2 * NN + col, *s1 = psi + NN + col;   // planes z+3, z+2, z+1
         for (int z = 0; z < N; z += 2) {
             T t[K];
@@ -1452,21 +1559,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (KIND == 1 ? 4 : 3) : 2)
                 p2 += NN;
                 s1 += NN;
                 C na, nb, nd, ne;
-                if (nbrs) { na = q1[xm]; nb = q1[xp]; nd = q1[ym]; ne = q1[yp]; }
+                { na = q1[xm]; nb = q1[xp]; nd = q1[ym]; ne = q1[yp]; }
                 C p = pc;
                 if (!fresh) {   // a fresh state holds pi_0 itself (the reference's ker is zero)
                     const T L1 = lap7<T>(zc.x, a.x, b.x, d.x, e.x, zm.x, zp.x);
                     const T L2 = lap7<T>(zc.y, a.y, b.y, d.y, e.y, zm.y, zp.y);
                     sync_pi_site<T>(zc.x, zc.y, L1, L2, p.x, p.y, c);
                 }
-                if (KIND == 0) {
-                    t[0] += zc.x;
-                    t[1] += zc.y;
-                    t[2] += p.x;
-                    t[3] += p.y;
-                    t[4] += fabs(atan2(zc.x, zc.y));
-                    t[5] += sqrt(zc.x * zc.x + zc.y * zc.y);
-                } else {   // differences in the order x, y, z
+                {   // differences in the order x, y, z
                     const T e1 = fma(-zc.x, it, p.x), e2 = fma(-zc.y, it, p.y);
                     t[0] += fma(e1, e1, e2 * e2);
                     T g1 = b.x - zc.x, g2 = b.y - zc.y;
@@ -1480,7 +1580,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (KIND == 1 ? 4 : 3) : 2)
                     const T r = fma(it2, fma(zc.x, zc.x, zc.y * zc.y), (T)-1);
                     t[2] += r * r;
                 }
-                if (nbrs) { a = na; b = nb; d = nd; e = ne; }
+                a = na; b = nb; d = nd; e = ne;
                 zm = zc;
                 zc = zp;
                 zp = zq;
@@ -1494,11 +1594,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (KIND == 1 ? 4 : 3) : 2)
     }
     double v[K];
     for (int k = 0; k < K; ++k) v[k] = acc[k].value();
-    if (KIND == 1) {
-        v[0] *= 0.5 / (tau * tau);
-        v[1] *= 0.5 / (tau * tau * dx * dx);
-        v[2] *= 0.25 * lam_eff;
-    }
+    v[0] *= 0.5 / (tau * tau);
+    v[1] *= 0.5 / (tau * tau * dx * dx);
+    v[2] *= 0.25 * lam_eff;
     block_reduce_store<K>(v, partials);
 }
 
@@ -1521,43 +1619,41 @@ static double *ensure_partials(Lattice *L, int nblocks, int K) {
     return L->dpartials;
 }
 
-// The fused z-column reductions serve 3D lattices with the radius-1
-// finite-difference Laplacian; the others form pi_n in scratch first.
-static bool reduce_zcol(const Lattice *L) {
+// The z-column energies serve 3D lattices with the radius-1 finite-difference
+// Laplacian; the others form pi_n in scratch first.
+static bool energies_zcol(const Lattice *L) {
     return L->p.NDIMS == 3 && L->p.stencil_setting == 0 && L->p.laplacian == 0;
 }
 static int zcol_blocks(int N) { return ((N + 31) / 32) * ((N + 7) / 8); }
 
-template <typename T, int KIND>
-static void launch_reduce_zcol(Lattice *L, double *part, double lam_eff) {
-    typedef typename Cplx<T>::type C;
-    const axs_params &p = L->p;
-    const double dx = p.space_step, T0 = p.T_initial;
-    k_reduce_zcol<T, KIND><<<zcol_blocks(p.N), 256, 0, L->stream>>>(
-        (const C *)L->psi[L->cur], (const C *)L->pih, part, L->dclock + L->cur, p.N, (double)p.time_step,
-        1.0 / (dx * dx), (double)p.lambda, (T0 * T0) / 3.0, p.prs, p.form, L->fresh, L->tau, dx, lam_eff);
-}
-
 void background(Lattice *L, double out[6]) {
-    int g;
-    double *part;
-    if (reduce_zcol(L)) {
-        g = zcol_blocks(L->p.N);
-        part = ensure_partials(L, g, 6);
-        if (L->esz == 4) launch_reduce_zcol<float, 0>(L, part, 0.0);
-        else launch_reduce_zcol<double, 0>(L, part, 0.0);
-    } else {
-        launch_sync_pi(L);
-        g = reduce_grid(L->length);
-        part = ensure_partials(L, g, 6);
-        if (L->esz == 4) k_background<float><<<g, 256, 0, L->stream>>>((const float2 *)L->psi[L->cur], (const float2 *)L->scratch, L->length, part);
-        else k_background<double><<<g, 256, 0, L->stream>>>((const double2 *)L->psi[L->cur], (const double2 *)L->scratch, L->length, part);
-    }
+    const axs_params &p = L->p;
+    const double T0 = p.T_initial;
+    const int resident = L->esz == 4 ? 4 : 2;   // k_background's blocks per SM
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>((L->length / 2 + 255) / 256, (int64_t)num_sms() * resident));
+    double *part = ensure_partials(L, g, 6);
+    if (L->esz == 4)
+        k_background<float><<<g, 256, 0, L->stream>>>((const float2 *)L->psi[L->cur], (const float2 *)L->pih,
+                                                       L->dclock + L->cur, L->length, (double)p.time_step,
+                                                       (double)p.lambda, (T0 * T0) / 3.0, p.prs, p.form, L->fresh, part);
+    else
+        k_background<double><<<g, 256, 0, L->stream>>>((const double2 *)L->psi[L->cur], (const double2 *)L->pih,
+                                                        L->dclock + L->cur, L->length, (double)p.time_step,
+                                                        (double)p.lambda, (T0 * T0) / 3.0, p.prs, p.form, L->fresh, part);
     AXS_CUDA(cudaGetLastError());
     count_launches(1);
     double s[6];
     sum_partials(part, g, 6, s, L->stream);
     for (int k = 0; k < 6; ++k) out[k] = s[k] / (double)L->length;   // s_run.cpp:149
+    if (!L->fresh && p.laplacian == 0) {   // the stencil's share of the half kick: W mean(psi)
+        double W = (double)stencil_coef(p.stencil_setting, p.NDIMS, 0);
+        for (int l = 1; l <= p.stencil_setting + 1; ++l)
+            W += 2.0 * p.NDIMS * (double)stencil_coef(p.stencil_setting, p.NDIMS, l);
+        const double dx = p.space_step;
+        const double kidx2 = 0.5 * (double)p.time_step / (dx * dx) * (p.form == 1 ? L->tau * L->tau : 1.0);
+        out[2] += kidx2 * W * out[0];
+        out[3] += kidx2 * W * out[1];
+    }
 }
 
 void energies(Lattice *L, double out[3]) {
@@ -1566,11 +1662,21 @@ void energies(Lattice *L, double out[3]) {
     double dx = L->p.space_step;
     int g;
     double *part;
-    if (reduce_zcol(L)) {
-        g = zcol_blocks(L->p.N);
+    if (energies_zcol(L)) {
+        const axs_params &p = L->p;
+        const double T0 = p.T_initial;
+        g = zcol_blocks(p.N);
         part = ensure_partials(L, g, 3);
-        if (L->esz == 4) launch_reduce_zcol<float, 1>(L, part, lam);
-        else launch_reduce_zcol<double, 1>(L, part, lam);
+        if (L->esz == 4)
+            k_energies_zcol<float><<<g, 256, 0, L->stream>>>(
+                (const float2 *)L->psi[L->cur], (const float2 *)L->pih, part, L->dclock + L->cur, p.N,
+                (double)p.time_step, 1.0 / (dx * dx), (double)p.lambda, (T0 * T0) / 3.0, p.prs, p.form, L->fresh,
+                L->tau, dx, lam);
+        else
+            k_energies_zcol<double><<<g, 256, 0, L->stream>>>(
+                (const double2 *)L->psi[L->cur], (const double2 *)L->pih, part, L->dclock + L->cur, p.N,
+                (double)p.time_step, 1.0 / (dx * dx), (double)p.lambda, (T0 * T0) / 3.0, p.prs, p.form, L->fresh,
+                L->tau, dx, lam);
     } else {
         launch_sync_pi(L);
         g = reduce_grid(L->length);

@@ -30,6 +30,22 @@ def near_threshold_theta(rng, nd, N, accept, frac=0.3):
     return flat_n.reshape(th.shape) * 2 * np.pi - np.pi
 
 
+def cell_sums3(n, z, y, x):
+    """The three loop sums of cores3 (string_finding.cpp:34-86) for the cell
+    with corner (i, j, k) = (z, y, x) of the normalised angles n."""
+    N = n.shape[0]
+    zp, yp, xp = (z + 1) % N, (y + 1) % N, (x + 1) % N
+
+    def c(a, b):
+        return min(abs(b - a), 1 - abs(b - a))
+
+    d000, d100, d110 = n[z, y, x], n[zp, y, x], n[zp, yp, x]
+    d010, d011, d001 = n[z, yp, x], n[z, yp, xp], n[z, y, xp]
+    return np.array([c(d000, d100) + c(d100, d110) + c(d110, d010),
+                     c(d000, d100) + c(d100, d011) + c(d011, d001),
+                     c(d000, d010) + c(d010, d011) + c(d011, d001)])
+
+
 def num_cores2_ascending(N, offsets):
     """s_run.cpp:101-109 over a list in ascending offset order."""
     offs = np.sort(np.asarray(offsets, dtype=np.int64))

@@ -8,15 +8,22 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("precision,tol", [(64, 1e-12), (32, 2e-6)])
-@pytest.mark.parametrize("nd,N,stencil,steps,prs", [
-    (2, 64, 0, 15, 1), (3, 32, 0, 15, 1),
-    (3, 20, 0, 15, 1),    # columns past the edge of the 32 x 8 blocks
-    (3, 36, 0, 9, 0),
-    (3, 32, 0, 0, 1),     # a fresh state: pih holds pi_0
-    (3, 24, 1, 15, 1),    # radius 2: pi_n formed in scratch first
+@pytest.mark.parametrize("nd,N,stencil,steps,prs,lap", [
+    (2, 64, 0, 15, 1, 0), (3, 32, 0, 15, 1, 0),
+    (3, 20, 0, 15, 1, 0),    # columns past the edge of the 32 x 8 blocks
+    (3, 36, 0, 9, 0, 0),
+    (3, 32, 0, 0, 1, 0),     # a fresh state: pih holds pi_0
+    (3, 24, 1, 15, 1, 0),    # radius 2: the energies form pi_n in scratch first
+    (3, 16, 0, 6, 1, 1),     # spectral Laplacian
+    (2, 48, 3, 12, 1, 0),    # radius 4 in 2D
 ])
-def test_background_and_energies(axs, oracle, precision, tol, nd, N, stencil, steps, prs):
-    p = params(axs, nd, N, precision, T_initial=0.0, stencil_setting=stencil, prs=prs)
+def test_background_and_energies(axs, oracle, precision, tol, nd, N, stencil, steps, prs, lap):
+    """The device's background means take the mean of pi_n without the
+    Laplacian part of the half kick (it sums to zero over the periodic
+    lattice); the oracle averages the per-site pi_n that download() forms with
+    the full stencil, so these cases also check that cancellation for every
+    stencil and the spectral operator."""
+    p = params(axs, nd, N, precision, T_initial=0.0, stencil_setting=stencil, prs=prs, laplacian=lap)
     op = orc(p)
     with axs.Lattice(p) as L:
         L.init_flat(6, 1.0)

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from gpu_util import orc, params
-from strings_util import accept_value, near_threshold_theta
+from strings_util import accept_value, cell_sums3, near_threshold_theta
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
@@ -69,6 +69,43 @@ def test_from_field_agrees_with_host_atan2(axs, oracle, precision, N):
     mism = int(np.count_nonzero(mask_g != mask_o))
     print("device-theta mismatches:", mism, "of", mask_o.size, "flagged", n_o)
     assert mism <= max(2, n_o // 100000)
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+@pytest.mark.parametrize("N", [30, 36, 68])
+def test_from_field_near_threshold(axs, oracle, precision, N):
+    """psi = (sin theta, cos theta) for a theta with many plaquette sums at
+    the threshold, so many cells fall within the float stage's margin and take
+    the double replay (N = 30 also leaves rows whose length is not a multiple
+    of four cells). Compared with the oracle on numpy's atan2 of the same
+    stored field. FP32: the rounding of psi moves those sums ~1e-7 off the
+    threshold, far more than an ulp of atan2, so the masks agree. FP64: the
+    sums stay within a few ulp of it, where the device's and numpy's atan2
+    may round differently; every cell that differs must be such a cell."""
+    p = params(axs, 3, N, precision)
+    rng = np.random.default_rng(N)
+    th = near_threshold_theta(rng, 3, N, accept_value(1))
+    dt = np.float32 if precision == 32 else np.float64
+    with axs.Lattice(p) as L:
+        L.init_flat(1, 1.0)
+        f = list(L.download())
+        f[0] = np.sin(th).astype(dt)
+        f[1] = np.cos(th).astype(dt)
+        L.upload(*f)
+        g = L.download()
+        n_g, _, mask_g = L.find_strings(want_mask=True)
+    theta = np.arctan2(g[0].astype(np.float64), g[1].astype(np.float64))
+    n_o, mask_o = oracle.cores(orc(p), theta)
+    mism = int(np.count_nonzero(mask_g != mask_o))
+    print("near-threshold mismatches:", mism, "of", mask_o.size, "flagged", n_o)
+    assert n_o > 0 and n_g == int(np.count_nonzero(mask_g))
+    if precision == 32:
+        assert mism == 0
+    else:
+        assert mism <= 10
+        n = (theta + np.pi) / (2 * np.pi)
+        for z, y, x in zip(*np.nonzero(mask_g != mask_o)):
+            assert np.abs(cell_sums3(n, z, y, x) - accept_value(1)).min() < 1e-12, (z, y, x)
 
 
 def test_xi_matches_reference_float_formula(axs, oracle):
