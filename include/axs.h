@@ -211,7 +211,11 @@ int axs_powerspec_noalloc(const void *spectrum, int NDIMS, int N, int precision,
 
 /* The six background means of s_run.cpp:135-150: phi1, phi2, phidot1, phidot2,
  * |atan2(phi1,phi2)|, |phi|. Deterministic FP64 (Kahan-compensated FP32 per
- * thread on the FP32 path). */
+ * thread on the FP32 path). The phidot means equal the means of the per-site
+ * synchronised momentum to rounding; they are formed from the means of pih
+ * and of the local part of the half kick, plus the stencil weights' sum times
+ * the mean field (the Laplacian's share on a periodic lattice), so the call
+ * streams the state once. */
 int axs_background(axs_lattice *h, double out[6]);
 /* Mean kinetic, gradient and potential energy densities of phi = psi/tau
  * (no reference counterpart). */
