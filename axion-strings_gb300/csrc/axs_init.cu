@@ -74,13 +74,16 @@ __global__ void k_fill_kspace(double2 *__restrict__ buf, const double *__restric
 // (init.cpp:323-330 / 393-400); re -> component 0, im -> component 1 of dst,
 // times `scale`. Optionally accumulates sum |v|^2 (before scaling) per block.
 // Rows as in k_fill_kspace (N is even, so the sign follows x + the row's
-// indices). When N^d is a power of two, x / N^d is x * (1 / N^d) exactly.
+// indices). When N^d is a power of two, x / N^d is x * (1 / N^d) exactly, and
+// (x / N^d) * scale is x * (scale / N^d) to the bit: one multiplication per
+// component (GB300's FP64 rate makes each one count); otherwise the division.
 template <typename T>
 __global__ void k_finish(const double2 *__restrict__ buf, T *__restrict__ dst, int N, int ndims, double norm,
                          int norm_pow2, double scale, int write, double *partials) {
     double acc[1] = {0.0};
-    const double inv = 1.0 / norm;
+    const double f = scale / norm;   // exact when norm_pow2
     const int64_t rows = ndims == 2 ? (int64_t)N : (int64_t)N * N;
+    typedef typename Cplx<T>::type C;
     for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
         const int rs = ndims == 2 ? (int)r : (int)(r / N) + (int)(r % N);
         for (int x = threadIdx.x; x < N; x += blockDim.x) {
@@ -88,20 +91,30 @@ __global__ void k_finish(const double2 *__restrict__ buf, T *__restrict__ dst, i
             double2 v = buf[m];
             if ((rs + x) & 1) { v.x = -v.x; v.y = -v.y; }
             if (norm_pow2) {
-                v.x *= inv;
-                v.y *= inv;
+                if (partials) acc[0] += v.x * v.x + v.y * v.y;   // times 1/norm^2 (exact) afterwards
+                if (write) {
+                    C o;
+                    o.x = (T)(v.x * f);
+                    o.y = (T)(v.y * f);
+                    reinterpret_cast<C *>(dst)[m] = o;
+                }
             } else {
                 v.x = v.x / norm;
                 v.y = v.y / norm;
-            }
-            if (partials) acc[0] += v.x * v.x + v.y * v.y;
-            if (write) {
-                dst[2 * m] = (T)(v.x * scale);
-                dst[2 * m + 1] = (T)(v.y * scale);
+                if (partials) acc[0] += v.x * v.x + v.y * v.y;
+                if (write) {
+                    C o;
+                    o.x = (T)(v.x * scale);
+                    o.y = (T)(v.y * scale);
+                    reinterpret_cast<C *>(dst)[m] = o;
+                }
             }
         }
     }
-    if (partials) block_reduce_store<1>(acc, partials);
+    if (partials) {
+        if (norm_pow2) acc[0] *= (1.0 / norm) * (1.0 / norm);
+        block_reduce_store<1>(acc, partials);
+    }
 }
 
 template <typename T>
