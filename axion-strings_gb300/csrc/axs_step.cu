@@ -1240,6 +1240,10 @@ static const ZVariant kZVariants[] = {
     // 32-37: radius 2-4 with the z-neighbours in registers (R + 2 slots, float)
     {4, 4, 128, 4, 8, -1, 2},  {4, 8, 64, 4, 8, -1, 2},  {4, 4, 128, 5, 8, -1, 3},  {4, 8, 64, 5, 8, -1, 3},
     {4, 4, 128, 6, 8, -1, 4},  {4, 8, 64, 6, 8, -1, 4},
+    // 38: one-step 32x16 tiles (the partner of 39-40); 39-40: LEAN two-step on
+    // 32x16 tiles with four consumer warps, three CTAs per SM: the y halo is
+    // 4 rows per 16 instead of per 8, and 32 divides every ensemble size
+    {2, 16, 32, 5, 8, -1},  {3, 16, 32, 4, 4, 38, 0, 1},  {3, 16, 32, 5, 4, 38, 0, 1},
 };
 static const int kNumZVariants = sizeof(kZVariants) / sizeof(kZVariants[0]);
 
@@ -1402,6 +1406,15 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
         if (esz != 4) fail(AXS_ERR_ARG, "two-step z-march variant %d needs complex float fields", variant);
         launch_zmarch3_t<8, 32, 4, 2, 1, true>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);
         break;
+        AXS_ZV2(38, 16, 32, 5)
+    case 39:
+        if (esz != 4) fail(AXS_ERR_ARG, "two-step z-march variant %d needs complex float fields", variant);
+        launch_zmarch3_t<16, 32, 4, 4, 1, true>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);
+        break;
+    case 40:
+        if (esz != 4) fail(AXS_ERR_ARG, "two-step z-march variant %d needs complex float fields", variant);
+        launch_zmarch3_t<16, 32, 5, 4, 1, true>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);
+        break;
 
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
@@ -1459,6 +1472,13 @@ static void prepare_zmarch(int esz, int variant) {
         break;
     case 31:
         if (esz == 4) prepare_zmarch3_t<8, 32, 4, 2, 1, true>();
+        break;
+        AXS_ZP2(38, 16, 32, 5)
+    case 39:
+        if (esz == 4) prepare_zmarch3_t<16, 32, 4, 4, 1, true>();
+        break;
+    case 40:
+        if (esz == 4) prepare_zmarch3_t<16, 32, 5, 4, 1, true>();
         break;
 
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);

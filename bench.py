@@ -307,8 +307,9 @@ def run_ensemble(axs, dist, steps, warmup, master_seed=2026):
     t1 = time.perf_counter()
     E.axion_spectrum(128)
     t2 = time.perf_counter()
+    desc = E.describe()
     E.close()
-    return {"members": n_total, "sites": int(sites_all), "ms": ms_max, "launches": launches,
+    return {"members": n_total, "sites": int(sites_all), "ms": ms_max, "launches": launches, "desc": desc,
             "sizes": [int(s) for s in sizes], "master_seed": master_seed,
             "analysis_ms": {"find_strings_all_members": 1e3 * (t1 - t0), "axion_spectrum_128_all_members": 1e3 * (t2 - t1)}}
 
@@ -377,7 +378,7 @@ def gpu_arm(args, dist):
         ens = {"value": re, "unit": "site-updates/s", "members": e["members"], "sites": e["sites"],
                "ms_per_step": e["ms"] / args.steps,
                "hbm_frac": re / dist.world * 32 * e["launches"] / args.steps / 1e9 / hbm,
-               "master_seed": e["master_seed"], "launches_per_step": e["launches"] / args.steps,
+               "master_seed": e["master_seed"], "launches_per_step": e["launches"] / args.steps, "kernel": e["desc"],
                "analysis_ms": e["analysis_ms"]}
     cpu = None
     if dist.rank == 0 and not args.no_cpu:

@@ -39,7 +39,7 @@ def test_members_bit_identical_to_alone(axs, precision):
             assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("force", ["1,10,32", "1,13,64", "1,12,128", "1,28,128", "1,31,128"])
+@pytest.mark.parametrize("force", ["1,10,32", "1,13,64", "1,12,128", "1,28,128", "1,31,128", "1,39,64"])
 def test_two_step_members_bit_identical_to_one_step_alone(axs, force, monkeypatch):
     """An ensemble on a two-step variant (halo depth 2, momentum out of place)
     matches each member run alone with the one-step kernel, over even and odd

@@ -61,7 +61,7 @@ def test_kernel_variants_bit_identical(axs, oracle, precision):
     f = oracle.init_thermal(op, 5)
     outs = []
     for force in ["0,0,64", "1,0,32", "1,1,64", "1,2,64", "1,3,128", "1,4,32",
-                  "1,5,64", "1,6,32", "1,7,64", "1,8,128", "1,9,16", "1,16,32", "1,27,64"]:
+                  "1,5,64", "1,6,32", "1,7,64", "1,8,128", "1,9,16", "1,16,32", "1,27,64", "1,38,32"]:
         os.environ["AXS_FORCE_CONFIG"] = force
         try:
             with axs.Lattice(p) as L:
@@ -77,7 +77,7 @@ def test_kernel_variants_bit_identical(axs, oracle, precision):
 
 
 TWO_STEP = ["1,10,32", "1,11,64", "1,12,128", "1,13,16", "1,14,64", "1,15,128", "1,17,32", "1,18,64",
-            "1,19,128", "1,28,32", "1,29,64", "1,30,32", "1,31,64"]
+            "1,19,128", "1,28,32", "1,29,64", "1,30,32", "1,31,64", "1,39,32", "1,40,64"]
 
 
 @pytest.mark.parametrize("N", [64, 160])
