@@ -1,5 +1,6 @@
 // Per-output analysis on the device: plaquette string finder, power spectra
 // after cuFFT, background means, energies and the finiteness check.
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -684,6 +685,11 @@ struct RefBinsI {
         while ((b + 2) * (b + 2) <= n2) ++b;
         return b;
     }
+    // the least n2' > n2 whose bin may differ from b = bin(n2)
+    __device__ __forceinline__ int upper(int b, int n2) const {
+        if (b >= 0) return min((b + 2) * (b + 2), half * half);
+        return n2 == 0 ? 1 : INT_MAX;   // the origin, or past the last bin for good
+    }
 };
 struct LogBinsI {
     const int *thr;   // thr[b] for b = 1..nbins-1 (thr[0] = 0)
@@ -708,6 +714,11 @@ struct LogBinsI {
         if (b < 0) return bin(n2);
         while (b + 1 < nbins && thr[b + 1] <= n2) ++b;
         return b;
+    }
+    // the least n2' > n2 whose bin may differ from b = bin(n2)
+    __device__ __forceinline__ int upper(int b, int) const {
+        if (b >= 0) return b + 1 < nbins ? thr[b + 1] : INT_MAX;
+        return 1;   // b < 0 only at the origin (n2 = 0)
     }
 };
 
@@ -807,11 +818,17 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
         for (int ix = lane; ix < sl; ix += 32) stage[ix] = row[ix];
         __syncwarp();
         int b = -1, fb = -1, lb = -1;
+        int up = 0;          // the bin is looked up again once n2 reaches this
+        bool inp = false;    // in_pass(b)
         FF v{0.f, 0.f}, kk{0.f, 0.f}, fv{0.f, 0.f}, fk{0.f, 0.f};
         int c = 0, fc = 0;
         for (int ix = lo; ix < hi; ++ix) {
             const int n2 = ix * ix + c2;
-            const int nb = bins.next(b, n2);
+            int nb = b;
+            if (n2 >= up) {
+                nb = bins.next(b, n2);
+                up = bins.upper(nb, n2);
+            }
             if (nb != b) {
                 if (b >= 0) {
                     if (fb < 0) { fb = b; fv = v; fk = kk; fc = c; }
@@ -824,10 +841,11 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
                     }
                 }
                 b = nb;
+                inp = in_pass(b);
                 v = kk = FF{0.f, 0.f};
                 c = 0;
             }
-            if (in_pass(nb)) {
+            if (inp) {
                 const int wt = (ix == 0 || 2 * ix == N) ? 1 : 2;
                 const float fw = (float)wt;   // x1 or x2: exact in float-float
                 const FF p = mode_power<T>(stage[ix - s0]);
