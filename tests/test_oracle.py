@@ -129,6 +129,38 @@ def test_strings_golden(oracle):
             assert num_cores2_ascending(N, np.flatnonzero(mask)) == int(z["num_cores_serial"])
 
 
+def _stencil_weight_sum(setting, nd):
+    """Sum of the float stencil weights of build_coefficient_matrix
+    (s_integrate.cpp:9-14): centre + 2 nd sum of the off-centre weights."""
+    f = np.float32
+    c = {0: [f(-2.0) * f(nd), f(1.0)],
+         1: [f(-5.0) / f(2.0) * f(nd), f(4.0) / f(3.0), f(-1.0) / f(12.0)],
+         2: [f(-49.0) / f(18.0) * f(nd), f(3.0) / f(2.0), f(-3.0) / f(20.0), f(1.0) / f(90.0)],
+         3: [f(-205.0) / f(72.0) * f(nd), f(8.0) / f(5.0), f(-1.0) / f(5.0), f(8.0) / f(315.0), f(-1.0) / f(560.0)]}[setting]
+    return float(c[0]) + 2 * nd * sum(float(x) for x in c[1:])
+
+
+@pytest.mark.parametrize("nd,N", [(2, 24), (3, 12)])
+@pytest.mark.parametrize("setting", [0, 1, 2, 3, "spectral"])
+def test_laplacian_sums_to_weight_sum_times_field_sum(oracle, nd, N, setting):
+    """On a periodic lattice every site is the neighbour of as many sites as
+    the stencil has points, so sum_m L(m) = W/dx^2 sum_m f(m), W the sum of the
+    stencil's weights (0 for 5 and 7 points, ~1e-7 for the float weights of
+    radius 2-4; 0 for the spectral operator). The background means of the
+    device rely on it: the Laplacian's share of mean(pi_n) is formed from
+    mean(psi) instead of per site."""
+    dx = 0.5
+    spectral = setting == "spectral"
+    p = oracle_lib.make_params(NDIMS=nd, N=N, dx=dx, stencil=0 if spectral else setting,
+                               laplacian=1 if spectral else 0)
+    f = np.random.default_rng(3).standard_normal((N,) * nd) + 0.7
+    lap = oracle.laplacian(p, f)
+    W = 0.0 if spectral else _stencil_weight_sum(setting, nd)
+    assert abs(lap.sum() - W / dx ** 2 * f.sum()) <= 1e-12 * np.abs(lap).sum()
+    if not spectral and setting > 0:
+        assert W != 0.0   # the float weights leave a small remainder, so the term matters
+
+
 @pytest.mark.parametrize("nd,N", [(2, 32), (3, 16)])
 def test_spectral_laplacian_plane_wave(oracle, nd, N):
     """The spectral Laplacian of a lattice plane wave is exactly -k^2 times it,
