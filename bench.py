@@ -14,7 +14,10 @@ psi buffers + 8.6 GB pi) is far larger than L2 (129 MB), so every step
 streams from HBM; no L2 flush is needed between steps.
 
 Also reported (extra keys): the plain FP64 step on the same lattice and
-start, the 96-member uneven batched ensemble, and the reference CPU path.
+start, the 96-member uneven batched ensemble (with the kernel its tuner
+kept), the reference CPU path, and the wall time of the per-output analysis
+calls on the headline lattice (`analysis_ms`: string finder, 128-bin axion
+spectrum, background means, energies) and on the ensemble.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
