@@ -56,6 +56,9 @@ struct RunConfig {
     int spectrum_bins = 128;
     int final_step = 0;            // > 0 overrides the light-crossing final step
     int check_finite = 0;          // 1: NaN/Inf check at every output step
+    char gpu_restart_file[kMaxLen] = {0};     // start from this axs_checkpoint file instead of
+                                              // gaussian_thermal; the run continues at its step
+    char gpu_checkpoint_file[kMaxLen] = {0};  // write an axs_checkpoint file after the last step
 };
 
 // read_parameter_file (src/common/read_parameters.cpp:182-238): every

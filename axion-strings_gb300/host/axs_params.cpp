@@ -62,6 +62,8 @@ int read_parameter_file(const char *fname, RunConfig &c, std::string &err) {
         {"spectrum_bins", INT, &c.spectrum_bins, false, false},
         {"final_step", INT, &c.final_step, false, false},
         {"check_finite", INT, &c.check_finite, false, false},
+        {"gpu_restart_file", STRING, c.gpu_restart_file, false, false},
+        {"gpu_checkpoint_file", STRING, c.gpu_checkpoint_file, false, false},
     };
     FILE *fd = fopen(fname, "r");
     if (!fd) {

@@ -25,6 +25,24 @@ struct Physics {
     float string_tension() const { return logf(m_saxion_initial / hubble_parameter()); }
 };
 
+bool read_file(const char *path, std::vector<unsigned char> &buf) {
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return false;
+    unsigned char chunk[1 << 16];
+    size_t n;
+    while ((n = fread(chunk, 1, sizeof chunk, fp)) > 0) buf.insert(buf.end(), chunk, chunk + n);
+    bool ok = !ferror(fp);
+    fclose(fp);
+    return ok;
+}
+
+bool write_file(const char *path, const std::vector<unsigned char> &buf) {
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return false;
+    bool ok = fwrite(buf.data(), 1, buf.size(), fp) == buf.size();
+    return fclose(fp) == 0 && ok;
+}
+
 bool every(int tstep, int n, int final_step, int enabled) {   // s_run.cpp:14-24
     if (!enabled) return false;
     int period = final_step / (n - 1);
@@ -55,8 +73,21 @@ int run_standard(const RunConfig &c, Output &o, std::string &err) {
     struct Guard { axs_lattice *h; ~Guard() { axs_destroy(h); } } guard{h};
     long long length = (c.NDIMS == 3) ? (long long)c.N * c.N * c.N : (long long)c.N * c.N;
 
-    if (c.init_mode == 1) CHECK(axs_init_flat(h, c.seed, c.k_cut));
-    else CHECK(axs_init_gaussian_thermal(h, c.seed));   // s_run.cpp:61
+    int64_t start_step = 0;
+    if (c.gpu_restart_file[0]) {
+        // resume: the exact device state of an axs_checkpoint file, at its step
+        std::vector<unsigned char> buf;
+        if (!read_file(c.gpu_restart_file, buf)) {
+            err = std::string("cannot read restart file ") + c.gpu_restart_file;
+            return AXS_ERR_ARG;
+        }
+        CHECK(axs_restore(h, buf.data(), buf.size()));
+        CHECK(axs_get_time(h, nullptr, &start_step));
+    } else if (c.init_mode == 1) {
+        CHECK(axs_init_flat(h, c.seed, c.k_cut));
+    } else {
+        CHECK(axs_init_gaussian_thermal(h, c.seed));   // s_run.cpp:61
+    }
 
     Physics ph{c.lambda, sqrtf(c.lambda), 1.0};
     if (c.save_snapshots) fprintf(o.snapshot_timings, "snapshot,tau,hubble_scale,string_tension,\n");
@@ -80,7 +111,7 @@ int run_standard(const RunConfig &c, Output &o, std::string &err) {
 
     std::vector<double> f1, f2;
     int n_snapshots_written = 0;
-    int tstep = 0;
+    int tstep = (int)start_step;
     while (tstep < final_step) {
         CHECK(axs_get_time(h, &ph.tau, nullptr));
         if (c.check_finite) {
@@ -169,6 +200,17 @@ int run_standard(const RunConfig &c, Output &o, std::string &err) {
         while (next < final_step && !is_output(next)) ++next;
         CHECK(axs_evolve(h, next - tstep));   // vvsl_field_rescaled x (next - tstep), s_run.cpp:215
         tstep = next;
+    }
+    if (c.gpu_checkpoint_file[0]) {
+        size_t bytes = 0;
+        CHECK(axs_checkpoint_size(h, &bytes));
+        std::vector<unsigned char> buf(bytes);
+        CHECK(axs_checkpoint(h, buf.data(), bytes));
+        if (!write_file(c.gpu_checkpoint_file, buf)) {
+            err = std::string("cannot write checkpoint file ") + c.gpu_checkpoint_file;
+            return AXS_ERR_ARG;
+        }
+        fprintf(o.main, "  Saving checkpoint... at %s\n", c.gpu_checkpoint_file);
     }
     return AXS_OK;
 }

@@ -73,10 +73,31 @@ def xi_run(n, interval, spec_every, seed=1, nbins=128):
         t += step
     a.close()
     b.close()
-    sig = [r for r in rows if r["n64"] >= 1000]
-    worst = max((abs(r["xi32"] - r["xi64"]) / r["xi64"] for r in sig), default=None)
     return {"equation": "PRS (prs=1)", "final_step": final_step, "interval": interval, "wall_s": time.time() - t0,
-            "xi_max_rel_diff_where_n64>=1000": worst, "samples": rows, "spectra": spectra}
+            "xi_summary": xi_summary(rows), "samples": rows, "spectra": spectra}
+
+
+def xi_summary(rows):
+    """xi(tau) of FP32 against FP64 over every sample with strings (n64 > 0):
+    the largest relative difference and the sample it occurs at, the same
+    over samples with n64 >= 1000, and the plaquette-count differences in
+    units of sqrt(n64) (the Poisson scatter of a count, to judge whether a
+    large relative difference at a low count is more than one or two cells)."""
+    def rel(r):
+        return abs(r["xi32"] - r["xi64"]) / r["xi64"]
+    live = [r for r in rows if r["n64"] > 0]
+    big = [r for r in live if r["n64"] >= 1000]
+    worst = max(live, key=rel, default=None)
+    return {
+        "samples_with_strings": len(live),
+        "samples_identical_count": sum(r["n32"] == r["n64"] for r in live),
+        "xi_max_rel_diff": rel(worst) if worst else None,
+        "xi_worst_sample": worst,
+        "xi_max_rel_diff_where_n64>=1000": max((rel(r) for r in big), default=None),
+        "count_max_abs_diff": max((abs(r["n32"] - r["n64"]) for r in live), default=None),
+        "count_max_diff_over_sqrt_n64": max((abs(r["n32"] - r["n64"]) / np.sqrt(r["n64"]) for r in live), default=None),
+        "samples_within_1pct": sum(rel(r) <= 0.01 for r in live),
+    }
 
 
 def main():

@@ -276,6 +276,124 @@ void orc_vvsl_step_f32(const orc_params *p, float *phi1, float *phi2, float *pi1
     memcpy(ker2, ker2n, sizeof(float) * len);
 }
 
+/* ------------------------------------------------ timing port of the CPU path */
+
+struct orc_csr {
+    long rows;
+    int per_row;      /* 1 + 2 * NDIMS * radius entries in every row */
+    int *col;         /* MKL_INT column indices, rows * per_row */
+    float *val;
+};
+
+/* The periodic matrix of build_coefficient_matrix (s_integrate.cpp:5-149) with
+ * every entry of a row stored, which is how mkl_sparse_?_mv applies the
+ * reference's symmetric/upper handle: row m lists the centre and then, for
+ * each l, the +l/-l neighbours along each axis (stencil_row's order). */
+orc_csr *orc_csr_build(const orc_params *p) {
+    double cd[5];
+    int nc = stencil_coefficients(p->stencil_setting, p->NDIMS, cd);
+    long N = p->N, len = lattice_length(p);
+    orc_csr *A = (orc_csr *)malloc(sizeof(orc_csr));
+    if (!A) return NULL;
+    A->rows = len;
+    A->per_row = 1 + 2 * p->NDIMS * (nc - 1);
+    A->col = (int *)malloc(sizeof(int) * (size_t)len * A->per_row);
+    A->val = (float *)malloc(sizeof(float) * (size_t)len * A->per_row);
+    if (!A->col || !A->val) {
+        orc_csr_free(A);
+        return NULL;
+    }
+    #pragma omp parallel for schedule(static)
+    for (long m = 0; m < len; ++m) {
+        int *c = A->col + m * A->per_row;
+        float *v = A->val + m * A->per_row;
+        int q = 0;
+        c[q] = (int)m; v[q++] = (float)cd[0];
+        for (int l = 1; l < nc; ++l) {
+            long o[6];
+            int no;
+            if (p->NDIMS == 2) {
+                long i = m % N, j = m / N;
+                o[0] = wrap(i + l, N) + N * j; o[1] = wrap(i - l, N) + N * j;
+                o[2] = i + N * wrap(j + l, N); o[3] = i + N * wrap(j - l, N);
+                no = 4;
+            } else {
+                long i = m / (N * N), j = (m / N) % N, k = m % N;
+                o[0] = (wrap(i + l, N) * N + j) * N + k; o[1] = (wrap(i - l, N) * N + j) * N + k;
+                o[2] = (i * N + wrap(j + l, N)) * N + k; o[3] = (i * N + wrap(j - l, N)) * N + k;
+                o[4] = (i * N + j) * N + wrap(k + l, N); o[5] = (i * N + j) * N + wrap(k - l, N);
+                no = 6;
+            }
+            for (int e = 0; e < no; ++e) { c[q] = (int)o[e]; v[q++] = (float)cd[l]; }
+        }
+    }
+    return A;
+}
+
+void orc_csr_free(orc_csr *A) {
+    if (!A) return;
+    free(A->col);
+    free(A->val);
+    free(A);
+}
+
+/* y = alpha * A x (mkl_wrapper_sparse_mv, mkl_wrapper.cpp:11-17, beta = 0). */
+static void csr_mv_f32(const orc_csr *A, float alpha, const float *x, float *y) {
+    int w = A->per_row;
+    #pragma omp parallel for schedule(static)
+    for (long m = 0; m < A->rows; ++m) {
+        const int *c = A->col + m * w;
+        const float *v = A->val + m * w;
+        float acc = 0.0f;
+        for (int q = 0; q < w; ++q) acc += v[q] * x[c[q]];
+        y[m] = alpha * acc;
+    }
+}
+
+/* vvsl_field_rescaled (s_integrate.cpp:305-348) as the reference runs it:
+ * six passes over the lattice with the Laplacian as two sparse
+ * matrix-vector products (s_integrate.cpp:321-324), float data. Used to time
+ * the CPU path: it has the reference's passes and memory traffic (the
+ * matrix's indices and values streamed per step), where orc_vvsl_step_f32
+ * recomputes neighbour offsets with integer divisions. Arithmetic equals
+ * orc_vvsl_step_f32 but for the summation order within a row. */
+void orc_ref_step_f32(const orc_params *p, const orc_csr *A, float *phi1, float *phi2, float *pi1, float *pi2,
+                      float *ker1, float *ker2, float *ker1n, float *ker2n, float *tau) {
+    long len = lattice_length(p);
+    float dt = p->time_step;
+    #pragma omp parallel for schedule(static)
+    for (long i = 0; i < len; ++i) {
+        phi1[i] += dt * (pi1[i] + 0.5f * ker1[i] * dt);
+        phi2[i] += dt * (pi2[i] + 0.5f * ker2[i] * dt);
+    }
+    *tau = *tau + dt;
+    double dx = (double)p->space_step;
+    float alpha = (float)(1.0f / (dx * dx));
+    csr_mv_f32(A, alpha, phi1, ker1n);
+    csr_mv_f32(A, alpha, phi2, ker2n);
+    double t = *tau;
+    double coef = potential_coefficient(p, t);
+    double T0 = p->T_initial;
+    double shift = (T0 * T0) / (3.0f);
+    #pragma omp parallel for schedule(static)
+    for (long i = 0; i < len; ++i) {
+        double a = phi1[i], b = phi2[i];
+        double br = a * a + b * b - t * t + shift;
+        ker1n[i] = (float)((double)ker1n[i] + coef * a * br);
+        ker2n[i] = (float)((double)ker2n[i] + coef * b * br);
+    }
+    #pragma omp parallel for schedule(static)
+    for (long i = 0; i < len; ++i) {
+        pi1[i] += 0.5f * (ker1[i] + ker1n[i]) * dt;
+        pi2[i] += 0.5f * (ker2[i] + ker2n[i]) * dt;
+    }
+    #pragma omp parallel for schedule(static)
+    for (long i = 0; i < len; ++i) {
+        ker1[i] = ker1n[i];
+        ker2[i] = ker2n[i];
+    }
+}
+
 /* ---------------------------------------------------------------- strings */
 
 /* min(|d|, 1-|d|) of string_finding.cpp:22-24 */

@@ -71,6 +71,16 @@ void orc_vvsl_hamiltonian_step(const orc_params *p, double *phi1, double *phi2, 
 void orc_vvsl_step_f32(const orc_params *p, float *phi1, float *phi2, float *pi1, float *pi2,
                        float *ker1, float *ker2, float *ker1n, float *ker2n, float *tau);
 
+/* Timing port of the CPU path (bench.py's CPU legs): build_coefficient_matrix's
+ * matrix (s_integrate.cpp:5-149) as CSR with full rows, and the float step of
+ * vvsl_field_rescaled in the reference's six passes with the Laplacian as two
+ * sparse matrix-vector products (s_integrate.cpp:321-324). */
+typedef struct orc_csr orc_csr;
+orc_csr *orc_csr_build(const orc_params *p);
+void orc_csr_free(orc_csr *A);
+void orc_ref_step_f32(const orc_params *p, const orc_csr *A, float *phi1, float *phi2, float *pi1, float *pi2,
+                      float *ker1, float *ker2, float *ker1n, float *ker2n, float *tau);
+
 /* cores2 / cores3 (src/common/string_finding.cpp:3-86). mask[m] = 1 where the
  * cell with base corner m is flagged. Returns the number of flagged cells. */
 int64_t orc_cores(const orc_params *p, const double *theta, uint8_t *mask);
@@ -86,7 +96,10 @@ void orc_powerspec(const orc_params *p, const double *data_real, const double *d
                    double *pk, double *ks, int *count);
 
 /* gaussian_thermal (src/common/init.cpp:33-200) with orc_normal() deviates.
- * The 3D k=0 phidot amplitude, left uninitialised by init.cpp:377-378, is 0. */
+ * The 3D k=0 phidot amplitude, left unset by init.cpp:163-164 (which assign
+ * `amplitude` twice), is 0. Built with GCC -O2 the reference keeps the value
+ * of the loop's previous mode there, so its phidot1/phidot2 exceed these by a
+ * constant (tests/golden/make_golden.py measures it). */
 void orc_gaussian_thermal(const orc_params *p, uint64_t seed,
                           double *phi1, double *phi2, double *phidot1, double *phidot2);
 

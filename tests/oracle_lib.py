@@ -11,6 +11,15 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 REF_DIR = os.path.join(ORACLE_DIR, "_ref")
 
+
+def reference_checkout():
+    """The reference checkout's root folder, or None where there is none:
+    $AXS_REFERENCE_DIR when set, else a folder named `reference` beside this
+    repository (the layout of the development container; the GPU machines
+    have no checkout)."""
+    d = os.environ.get("AXS_REFERENCE_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
+    return d if os.path.isdir(os.path.join(d, "src")) else None
+
 _vp = ctypes.c_void_p
 _dp = ctypes.POINTER(ctypes.c_double)
 
@@ -46,6 +55,10 @@ class Oracle:
             "orc_laplacian": ([P, _vp, _vp], None),
             "orc_vvsl_step": ([P, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _dp], None),
             "orc_vvsl_step_f32": ([P, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_float)], None),
+            "orc_csr_build": ([P], _vp),
+            "orc_csr_free": ([_vp], None),
+            "orc_ref_step_f32": ([P, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_float)],
+                                 None),
             "orc_vvsl_hamiltonian_step": ([P, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _dp], None),
             "orc_cores": ([P, _vp, _vp], ctypes.c_int64),
             "orc_num_cores2": ([ctypes.c_int, _vp], ctypes.c_int64),
@@ -81,15 +94,20 @@ class Oracle:
         self.lib.orc_laplacian(ctypes.byref(p), _ptr(phi), _ptr(out))
         return out
 
-    def evolve(self, p, phi1, phi2, pi1, pi2, nsteps, tau=1.0, ker=None, form=0):
+    def evolve(self, p, phi1, phi2, pi1, pi2, nsteps, tau=1.0, ker=None, form=0, return_ker=False):
         """Reference-structured velocity-Verlet steps (form 0: vvsl_field_rescaled,
-        form 1: vvsl_hamiltonian_form); returns the new state."""
+        form 1: vvsl_hamiltonian_form); returns the new state. `ker` is the
+        pair (ker1_curr, ker2_curr) to continue from (zero, as after the
+        reference's calloc, when None); with return_ker the pair after the
+        last step is returned too."""
         f = [np.array(a, dtype=np.float64, copy=True, order="C") for a in (phi1, phi2, pi1, pi2)]
         k = [np.zeros_like(f[0]) for _ in range(4)] if ker is None else [np.array(a, copy=True) for a in ker] + [np.zeros_like(f[0]), np.zeros_like(f[0])]
         t = ctypes.c_double(tau)
         step = self.lib.orc_vvsl_hamiltonian_step if form == 1 else self.lib.orc_vvsl_step
         for _ in range(nsteps):
             step(ctypes.byref(p), *[_ptr(a) for a in f], _ptr(k[0]), _ptr(k[1]), _ptr(k[2]), _ptr(k[3]), ctypes.byref(t))
+        if return_ker:
+            return f[0], f[1], f[2], f[3], t.value, (k[0], k[1])
         return f[0], f[1], f[2], f[3], t.value
 
     def evolve_f32(self, p, phi1, phi2, pi1, pi2, nsteps, tau=1.0):

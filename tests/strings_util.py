@@ -46,6 +46,33 @@ def cell_sums3(n, z, y, x):
                      c(d000, d010) + c(d010, d011) + c(d011, d001)])
 
 
+def cell_sum2(n, j, i):
+    """The loop sum of cores2 (string_finding.cpp:3-33) for the cell with
+    corner (i, j) of the normalised angles n (array index [j, i])."""
+    N = n.shape[0]
+    ip, jp = (i + 1) % N, (j + 1) % N
+
+    def c(a, b):
+        return min(abs(b - a), 1 - abs(b - a))
+
+    n1, n2, n3, n4 = n[j, i], n[j, ip], n[jp, ip], n[jp, i]
+    return c(n1, n2) + c(n2, n3) + c(n3, n4)
+
+
+def threshold_only_mismatches(nd, theta, mask_a, mask_b, accept, margin=1e-12):
+    """Cells where two masks differ, and whether every one of them has a
+    plaquette sum within `margin` of the acceptance value (a cell that an
+    ulp of atan2 can move across the threshold)."""
+    n = (theta + np.pi) / (2 * np.pi)
+    cells = list(zip(*np.nonzero(mask_a != mask_b)))
+    ok = True
+    for c in cells:
+        s = np.atleast_1d(cell_sum2(n, *c) if nd == 2 else cell_sums3(n, *c))
+        if np.abs(s - accept).min() >= margin:
+            ok = False
+    return len(cells), ok
+
+
 def num_cores2_ascending(N, offsets):
     """s_run.cpp:101-109 over a list in ascending offset order."""
     offs = np.sort(np.asarray(offsets, dtype=np.int64))

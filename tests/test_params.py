@@ -88,8 +88,10 @@ def test_comments_and_gpu_tags_are_accepted(driver, tmp_path):
 
 
 def test_reference_default_param_parses(driver, tmp_path):
-    ref = "/root/reference/default.param"
-    if not os.path.exists(ref):
-        pytest.skip("reference checkout not present")
+    import oracle_lib
+    checkout = oracle_lib.reference_checkout()
+    if checkout is None:
+        pytest.skip("reference checkout not present (set AXS_REFERENCE_DIR)")
+    ref = os.path.join(checkout, "default.param")
     r = subprocess.run([driver, ref], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=120)
     assert "not allowed" not in r.stdout and "I miss a value" not in r.stdout
