@@ -8,6 +8,7 @@
 #include <mutex>
 
 #include "axs_internal.h"
+#include "axs_tma.cuh"
 
 namespace axs {
 
@@ -32,15 +33,37 @@ static int grid_cap(int64_t work, int threads, int per_sm) {
 //     which makes the decision bit-exact to the reference on a given theta.
 static constexpr float kMargin = 1e-5f;
 
-// atan2(y, x) in float within 5e-7 rad, for the float stage above: octant
-// reduction to a = min(|x|,|y|) / max(|x|,|y|) in [0, 1] (a fast division,
-// within 2 ulp), atan(a) = a P(a^2) with P of degree 7 fitted to atan on
-// [0, 1] (weighted least squares iterated to equal ripple, Lawson's method;
-// 1.4e-7 rad evaluated in float), then the octant undone. Exact zeros and
-// magnitudes outside [1e-30, 1e30] take atan2f (the signed results on the axes).
-__device__ constexpr float kAtanC[8] = {0.9999993443489075f,  -0.33329859375953674f, 0.19946566224098206f,
-                                    -0.1390862911939621f, 0.0964219719171524f,   -0.0559123270213604f,
-                                    0.021862957626581192f, -0.004054567310959101f};
+// atan2(y, x) in float within 5e-7 rad (the background means' float angle):
+// octant reduction to a = min(|x|,|y|) / max(|x|,|y|) in [0, 1] (a fast
+// division, within 2 ulp), atan(a) = a P(a^2) with P of degree 7 fitted to
+// atan on [0, 1] (weighted least squares iterated to equal ripple, Lawson's
+// method; tests/atan_fit.py regenerates the table), then the octant undone.
+// Exact zeros and magnitudes outside [1e-30, 1e30] take atan2f (the signed
+// results on the axes).
+__device__ constexpr float kAtanC[8] = {9.999993443e-01f, -3.332986236e-01f, 1.994658262e-01f, -1.390872002e-01f,
+                                        9.642439336e-02f, -5.591578037e-02f, 2.186544798e-02f, -4.055280238e-03f};
+// The string finder's angle in turns, atan2(y, x) / (2 pi): the same
+// reduction with P of degree 5 fitted to atan(a) / (2 pi) (tests/atan_fit.py),
+// within 2.8e-7 turns (1.7e-6 rad) evaluated in float, and the octant undone
+// in turns (1/4, 1/2). Only zeros on both axes, magnitudes outside
+// [1e-30, 1e30] and NaN take atan2f: with one zero component the reduced
+// argument is 0 and the fix-ups give atan2's signed axis values.
+__device__ constexpr float kTurnC[6] = {1.591513157e-01f, -5.293861777e-02f, 3.080324642e-02f,
+                                        -1.853073202e-02f, 8.380074054e-03f, -1.865555299e-03f};
+__device__ __forceinline__ float fast_turns(float y, float x) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+    if (!(mx >= 1e-30f && mx <= 1e30f)) return atan2f(y, x) * 0.15915494309189535f;
+    const float a = __fdividef(mn, mx);   // within 2 ulp for 2^-126 <= mx <= 2^126
+    const float s = a * a;
+    float p = kTurnC[5];
+#pragma unroll
+    for (int k = 4; k >= 0; --k) p = fmaf(p, s, kTurnC[k]);
+    float r = p * a;
+    if (ay > ax) r = 0.25f - r;
+    if (x < 0.0f) r = 0.5f - r;
+    return copysignf(r, y);
+}
 __device__ __forceinline__ float fast_atan2(float y, float x) {
     const float ax = fabsf(x), ay = fabsf(y);
     const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
@@ -155,22 +178,33 @@ __global__ void __launch_bounds__(256) k_cores(const typename Cplx<T>::type *__r
 }
 
 // 3D finder from psi, tiled: a block owns a CX x CY tile of cells and marches a
-// z-chunk; the normalised angles n = (theta+pi)/(2pi) of the tile's sites (one
-// site of halo in +x and +y) are computed once per site into a two-plane
-// shared ring (k_cores evaluates them once per corner, six times per site).
-// Each thread owns a run of four cells along x in one row and keeps the angles
-// of plane z (rows y, y+1, five sites each) and the circular distances of
-// their y-edges in registers, so per plane it reads ten angles of plane z+1
-// (two 16-byte and two 4-byte shared loads) and forms 21 edge distances for
-// its four cells instead of 32; the four mask bytes go out as one 32-bit store
-// when N is a multiple of 4. The edge sums keep k_cores' association order:
-// same float sums, same margin test, same double replay, same decisions.
+// z-chunk; the angles of the tile's sites (one site of halo in +x and +y), in
+// turns theta/(2 pi) (fast_turns; n of the reference minus 1/2, which no
+// difference sees), are computed once per site into a two-plane shared ring
+// (k_cores evaluates them once per corner, six times per site). Each thread
+// owns a run of four cells along x in one row and keeps the angles of plane z
+// (rows y, y+1, five sites each) and the edge values of their y-edges in
+// registers, so per plane it reads ten angles of plane z+1 (two 16-byte and
+// two 4-byte shared loads) and forms 21 edge values for its four cells; the
+// four mask bytes go out as one 32-bit store when N is a multiple of 4.
+// An edge is kept as t = 1/2 - |d| (d the difference of its angles, |d| < 1):
+// the reference's min(|d|, 1 - |d|) is 1/2 - |t|, so a plaquette's sum is
+// 3/2 - (|t1| + |t2| + |t3|) and the three sums of a cell exceed accept when
+// the least sum of |t| is below 3/2 - accept. The float stage decides at a
+// margin of kMargin from that bound (its error: angles within 3.2e-7 turns
+// with the division and the octant roundings, edges within 7e-7, a sum of
+// |t| within 2.3e-6); the other cells take the double replay after the march.
 static constexpr int kCX = 64, kCY = 16, kCZ = 32;   // cells per block tile; 256 threads x 4 cells
+
+// 1/2 - |b - a| for angles in turns (see above)
+__device__ __forceinline__ float half_gap(float a, float b) { return 0.5f - fabsf(b - a); }
 static_assert(kCZ * 4 <= 128, "two 64-bit words of margin bits per thread");
 static constexpr int kRS = kCX + 4;                   // shared row stride: 16-byte aligned rows, +x halo at kCX
 
 template <typename T>
-__global__ void __launch_bounds__(256, 3) k_cores3_tiled(const typename Cplx<T>::type *__restrict__ psi,
+// Four CTAs per SM (64 registers, a few bytes of spills): the march is
+// latency-bound, and 32 warps per SM ran 3.12 against 3.36 ms at 1024^3 for 24.
+__global__ void __launch_bounds__(256, 4) k_cores3_tiled(const typename Cplx<T>::type *__restrict__ psi,
                                                       uint8_t *__restrict__ mask, int N, double accept,
                                                       unsigned long long *count) {
     typedef typename Cplx<T>::type C;
@@ -179,6 +213,8 @@ __global__ void __launch_bounds__(256, 3) k_cores3_tiled(const typename Cplx<T>:
     __shared__ __align__(16) float nsm[2][kCY + 1][kRS];
     Corner<T, false> cn{psi, nullptr};
     const float acc_f = (float)accept;
+    // least sum of |t| of a certainly flagged cell, greatest of an undecided one
+    const float t_flag = 1.5f - acc_f - kMargin, t_undecided = 1.5f - acc_f + kMargin;
     const int64_t NN = (int64_t)N * N;
     const int x0 = blockIdx.x * kCX, y0 = blockIdx.y * kCY, z0 = blockIdx.z * kCZ;
     const int z1 = min(N, z0 + kCZ);
@@ -204,9 +240,13 @@ __global__ void __launch_bounds__(256, 3) k_cores3_tiled(const typename Cplx<T>:
     }
     const bool row_ok = gy < N;
     const bool packed = row_ok && (N & 3) == 0 && gx < N;   // then gx + 3 < N and the store is 4-byte aligned
-    int vmask = 0;   // bit j: cell (gx + j, gy) is in the lattice
+    unsigned vmask = 0, vbytes = 0;   // bit / byte j: cell (gx + j, gy) is in the lattice
 #pragma unroll
-    for (int j = 0; j < 4; ++j) vmask |= (row_ok && gx + j < N) ? 1 << j : 0;
+    for (int j = 0; j < 4; ++j)
+        if (row_ok && gx + j < N) {
+            vmask |= 1u << j;
+            vbytes |= 1u << (8 * j);
+        }
     unsigned long long unc0 = 0, unc1 = 0;   // bit 4 (z - z0) + j: cell within the float margin (kCZ = 32 planes)
     C pre[PER];   // psi of the next plane's tile, loaded one plane ahead
     auto load = [&](int z) {
@@ -219,7 +259,7 @@ __global__ void __launch_bounds__(256, 3) k_cores3_tiled(const typename Cplx<T>:
         float *dst = &nsm[buf][0][0];
 #pragma unroll
         for (int k = 0; k < PER; ++k)
-            if (si[k] >= 0) dst[si[k]] = fmaf(fast_atan2((float)pre[k].x, (float)pre[k].y), 0.15915494309189535f, 0.5f);
+            if (si[k] >= 0) dst[si[k]] = fast_turns((float)pre[k].x, (float)pre[k].y);
     };
     // angles of rows ly, ly+1 at x = lx .. lx+4 of a buffered plane
     auto read = [&](int buf, float (&r0)[5], float (&r1)[5]) {
@@ -228,14 +268,14 @@ __global__ void __launch_bounds__(256, 3) k_cores3_tiled(const typename Cplx<T>:
         r0[0] = u.x; r0[1] = u.y; r0[2] = u.z; r0[3] = u.w; r0[4] = nsm[buf][ly][lx + 4];
         r1[0] = v.x; r1[1] = v.y; r1[2] = v.z; r1[3] = v.w; r1[4] = nsm[buf][ly + 1][lx + 4];
     };
-    float a0[5], a1[5], ya[5];   // plane z: rows y, y+1 and their y-edge distances
+    float a0[5], a1[5], ya[5];   // plane z: rows y, y+1 and their y-edge values t
     load(z0);
     store(0);
     load(z0 + 1);
     __syncthreads();
     read(0, a0, a1);
 #pragma unroll
-    for (int i = 0; i < 5; ++i) ya[i] = circf(a0[i], a1[i]);
+    for (int i = 0; i < 5; ++i) ya[i] = half_gap(a0[i], a1[i]);
     // One plane: plane z+1 goes into buffer nb, the one last read two planes
     // ago (every thread is past the previous barrier, so done with it).
     auto plane_step = [&](const int z, const int nb) {
@@ -245,29 +285,28 @@ __global__ void __launch_bounds__(256, 3) k_cores3_tiled(const typename Cplx<T>:
         float b0[5], b1[5], yb[5];
         read(nb, b0, b1);
 #pragma unroll
-        for (int i = 0; i < 5; ++i) yb[i] = circf(b0[i], b1[i]);
-        unsigned word = 0;
-        int nflag = 0;
+        for (int i = 0; i < 5; ++i) yb[i] = half_gap(b0[i], b1[i]);
+        unsigned word = 0, und = 0;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             // f000 = a0[j], f001 = a0[j+1], f010 = a1[j], f011 = a1[j+1],
-            // f100 = b0[j], f110 = b1[j]
-            const float e_000_100 = circf(a0[j], b0[j]);
-            const float sa = e_000_100 + yb[j] + circf(b1[j], a1[j]);
-            const float sb = e_000_100 + circf(b0[j], a1[j + 1]) + ya[j + 1];   // plaquette b, string_finding.cpp:54-57
-            const float sc = ya[j] + circf(a1[j], a1[j + 1]) + ya[j + 1];
-            const float mx = fmaxf(sa, fmaxf(sb, sc));
-            int flag = 0;
-            if ((vmask >> j) & 1) {
-                if (mx > acc_f + kMargin) flag = 1;
-                else if (!(mx < acc_f - kMargin)) {   // within the margin: the double replay, after the march
-                    const int b = (z - z0) * 4 + j;
-                    if (b < 64) unc0 |= 1ull << b;
-                    else unc1 |= 1ull << (b - 64);
-                }
-            }
-            word |= (unsigned)flag << (8 * j);
-            nflag += flag;
+            // f100 = b0[j], f110 = b1[j]; plaquettes a, b, c of string_finding.cpp:49-82
+            const float e_000_100 = fabsf(half_gap(a0[j], b0[j]));
+            const float ta = e_000_100 + fabsf(yb[j]) + fabsf(half_gap(b1[j], a1[j]));
+            const float tb = e_000_100 + fabsf(half_gap(b0[j], a1[j + 1])) + fabsf(ya[j + 1]);   // the (i,j+1,k+1) corner
+            const float tc = fabsf(ya[j]) + fabsf(half_gap(a1[j], a1[j + 1])) + fabsf(ya[j + 1]);
+            const float tmin = fminf(ta, fminf(tb, tc));
+            const bool flag = tmin < t_flag;
+            word |= (flag ? 1u : 0u) << (8 * j);
+            und |= (!flag && tmin <= t_undecided ? 1u : 0u) << j;   // the double replay, after the march
+        }
+        word &= vbytes;   // cells past the lattice's edge (N not a multiple of 4)
+        und &= vmask;
+        const int nflag = __popc(word);
+        if (und) {
+            const int b = (z - z0) * 4;   // bits b .. b+3 of the 128-bit set; b is a multiple of 4
+            if (b < 64) unc0 |= (unsigned long long)und << b;
+            else unc1 |= (unsigned long long)und << (b - 64);
         }
         uint8_t *mz = mask + (int64_t)z * NN + (int64_t)gy * N + gx;
         if (packed) *reinterpret_cast<unsigned *>(mz) = word;
@@ -751,6 +790,69 @@ __device__ __forceinline__ void ff_acc(double *slot, FF x) {
     *s = make_float2(r.hi, r.lo);
 }
 
+// w * a for w = 1 or 2 (exact in float-float)
+__device__ __forceinline__ FF ff_scale(FF a, float w) { return FF{w * a.hi, w * a.lo}; }
+
+// |n| = sqrt(n2) as float-float. Below 2^24, n2 is exact in float: hi = sqrtf
+// (correctly rounded), the residual n2 - hi^2 is exact in float (that of a
+// correctly rounded square root always is) and lo = residual / (2 hi). Above
+// (large 2D lattices), from the double square root (used by a binning's first
+// call only).
+__device__ __forceinline__ FF mode_norm(int n2) {
+    if (n2 < (1 << 24)) {
+        const float n2f = (float)n2;
+        const float shi = sqrtf(n2f);
+        return FF{shi, shi > 0.0f ? __fdiv_rn(fmaf(-shi, shi, n2f), 2.0f * shi) : 0.0f};
+    }
+    const double rd = sqrt((double)n2);
+    const float shi = (float)rd;
+    return FF{shi, (float)(rd - (double)shi)};
+}
+
+// The least s >= 0 with s^2 >= m (0 < m < 2^31).
+__device__ __forceinline__ int ceil_isqrt(int m) {
+    int s = (int)sqrtf((float)m);
+    while ((int64_t)s * s < m) ++s;
+    while (s > 0 && (int64_t)(s - 1) * (s - 1) >= m) --s;
+    return s;
+}
+
+// Weighted power of the modes ix in [a, e) of one bin's run, added to v:
+// weight 2 (the mode and its conjugate of the half spectrum), 1 for the row's
+// first (ix = 0) and last (ix = N/2 = nh - 1) mode. Summed in FP32 in blocks
+// of at most 16 modes (relative error below 16 ulp of a block's sum, all terms
+// being non-negative), even and odd modes in two chains to shorten the
+// dependent FMA sequence, each block added to v in float-float. s: the staged
+// row segment that starts at mode s0.
+__device__ __forceinline__ FF run_power(const float2 *s, int s0, int a, int e, int nh, FF v) {
+    if (a == 0) {
+        const float2 f = s[-s0];
+        v = ff_add(v, FF{fmaf(f.x, f.x, f.y * f.y), 0.f});
+        a = 1;
+    }
+    const int eh = e == nh ? nh - 1 : e;
+    while (a < eh) {
+        const int ce = min(eh, a + 16);
+        float t0 = 0.f, t1 = 0.f;
+        for (; a + 1 < ce; a += 2) {
+            const float2 f = s[a - s0], g = s[a + 1 - s0];
+            t0 = fmaf(f.x, f.x, fmaf(f.y, f.y, t0));
+            t1 = fmaf(g.x, g.x, fmaf(g.y, g.y, t1));
+        }
+        if (a < ce) {
+            const float2 f = s[a - s0];
+            t0 = fmaf(f.x, f.x, fmaf(f.y, f.y, t0));
+            ++a;
+        }
+        v = ff_add(v, FF{2.f * (t0 + t1), 0.f});
+    }
+    if (e == nh) {
+        const float2 f = s[nh - 1 - s0];
+        v = ff_add(v, FF{fmaf(f.x, f.x, f.y * f.y), 0.f});
+    }
+    return v;
+}
+
 template <typename T> __device__ __forceinline__ FF mode_power(const typename Cplx<T>::type &f);
 template <> __device__ __forceinline__ FF mode_power<float>(const float2 &f) { return FF{fmaf(f.x, f.x, f.y * f.y), 0.0f}; }
 template <> __device__ __forceinline__ FF mode_power<double>(const double2 &f) {
@@ -778,19 +880,32 @@ template <> __device__ __forceinline__ FF mode_power<double>(const double2 &f) {
 // launch summing bins b0 .. b0+nbp-1 only (modes of other bins are skipped).
 // One segment per row and one pass is the common case.
 template <typename T, typename B, bool KS>
-__global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *__restrict__ F, int N, int ndims,
+__global__ void __launch_bounds__(128, 8) k_bin_runs(const typename Cplx<T>::type *__restrict__ F, int N, int ndims,
                                                   B binner, int nbins, int seg, int b0, int nbp,
-                                                  double *__restrict__ partials) {
+                                                  double *__restrict__ partials, int *derr) {
     typedef typename Cplx<T>::type C;
-    extern __shared__ double hist[];   // [4 warps][3][nbp], bin table, [4 warps][seg] staged row segments
+    constexpr bool kRuns = sizeof(T) == 4;   // FP32 modes: whole runs per bin lookup
+    // [4 warps][3][nbp] histograms, bin table, [4 warps][2][sbuf] staging buffers, [4 warps][2] mbarriers
+    extern __shared__ double hist[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nh = N / 2 + 1;
     const int nseg = (nh + seg - 1) / seg;
     const int b1 = b0 + nbp;
     for (int i = threadIdx.x; i < 4 * 3 * nbp; i += blockDim.x) hist[i] = 0.0;
     const B bins = binner.staged(hist + 4 * 3 * nbp);
-    // staged segments start 16-byte aligned (complex double modes are read as double2)
-    C *stage = reinterpret_cast<C *>(hist + ((4 * 3 * nbp + B::kSmemTable * nbins + 1) & ~1)) + (size_t)w * seg;
+    // Row segments arrive by bulk copies into two staging buffers per warp: the
+    // next unit's copy is in flight while this one is binned. A buffer holds a
+    // segment and up to one mode either side (the copy starts and ends on 16
+    // bytes); buffers start 16-byte aligned, the warp's two mbarriers follow.
+    const int sbuf = (seg + 3) & ~1;
+    C *stg = reinterpret_cast<C *>(hist + ((4 * 3 * nbp + B::kSmemTable * nbins + 1) & ~1)) + (size_t)w * 2 * sbuf;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(reinterpret_cast<C *>(hist + ((4 * 3 * nbp + B::kSmemTable * nbins + 1) & ~1)) +
+                                                  (size_t)4 * 2 * sbuf) + 2 * w;
+    if (lane == 0) {
+        mbar_init(smem_u32(&bars[0]), 1);
+        mbar_init(smem_u32(&bars[1]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     __syncthreads();
     double *hp = hist + (size_t)w * 3 * nbp;   // indexed by bin - b0
     double *hk = hp + nbp;
@@ -799,7 +914,36 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
     const int64_t rows = ndims == 2 ? (int64_t)N : (int64_t)N * N;
     const int64_t units = rows * nseg;
     const int64_t nwarps = (int64_t)gridDim.x * 4;
-    for (int64_t u = (int64_t)blockIdx.x * 4 + w; u < units; u += nwarps) {
+    // The mode offset of unit uu's copy below its first mode (FP32 modes are 8
+    // bytes; the array and every row-segment copy start on 16 bytes), and the
+    // copy itself (lane 0). The copy ends on 16 bytes too: at most one mode
+    // past the segment, which exists (the array holds an even number of modes,
+    // so the last segment's copy ends exactly at its end).
+    auto unit_off = [&](int64_t uu) -> int {
+        const int64_t rr = uu / nseg;
+        return sizeof(C) == 8 ? (int)((rr * nh + (uu - rr * nseg) * seg) & 1) : 0;
+    };
+    auto issue = [&](int64_t uu, int buf) {
+        const int64_t rr = uu / nseg;
+        const int ss0 = (int)(uu - rr * nseg) * seg, ssl = min(seg, nh - ss0);
+        const int off = unit_off(uu);
+        const uint32_t bytes = (uint32_t)(((size_t)(ssl + off) * sizeof(C) + 15) & ~(size_t)15);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // after this warp's reads of the buffer
+        mbar_expect_tx(smem_u32(&bars[buf]), bytes);
+        bulk_load(smem_u32(stg + (size_t)buf * sbuf), F + rr * nh + ss0 - off, bytes, smem_u32(&bars[buf]));
+    };
+    const int64_t ufirst = (int64_t)blockIdx.x * 4 + w;
+    if (lane == 0 && ufirst < units) issue(ufirst, 0);
+    int it = 0;
+    bool ok = true;
+    int64_t u = ufirst;
+    for (; u < units; u += nwarps, ++it) {
+        const int cur = it & 1;
+        __syncwarp();   // every lane is done with the other buffer (the previous unit)
+        if (lane == 0 && u + nwarps < units) issue(u + nwarps, cur ^ 1);
+        ok = __all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[cur]), (uint32_t)((it >> 1) & 1)));
+        if (!ok) break;
+        const C *stage = stg + (size_t)cur * sbuf + unit_off(u);
         const int64_t r = u / nseg;
         const int s0 = (int)(u - r * nseg) * seg, sl = min(seg, nh - s0);
         const int chunk = (sl + 31) / 32;
@@ -814,14 +958,48 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
             const int fz = iz < N / 2 ? iz : iz - N, fy = iy < N / 2 ? iy : iy - N;
             c2 = fy * fy + fz * fz;
         }
-        const C *row = F + r * nh + s0;
-        for (int ix = lane; ix < sl; ix += 32) stage[ix] = row[ix];
-        __syncwarp();
         int b = -1, fb = -1, lb = -1;
         int up = 0;          // the bin is looked up again once n2 reaches this
         bool inp = false;    // in_pass(b)
         FF v{0.f, 0.f}, kk{0.f, 0.f}, fv{0.f, 0.f}, fk{0.f, 0.f};
         int c = 0, fc = 0;
+        if constexpr (kRuns) {
+            // FP32: jump from run to run. A run ends where n2 reaches `up`, at
+            // ix = ceil(sqrt(up - c2)); its power is summed by run_power, so a
+            // binning's first call (KS: also |n| and the mode count, per mode)
+            // and its later calls give the same power sums.
+            for (int ix = lo; ix < hi;) {
+                const int n2 = ix * ix + c2;
+                if (n2 >= up) {
+                    const int nb = bins.next(b, n2);
+                    up = bins.upper(nb, n2);
+                    if (b >= 0) {   // nb != b: n2 reached the bound of b's run
+                        if (fb < 0) { fb = b; fv = v; fk = kk; fc = c; }
+                        else if (in_pass(b)) {   // a run inside the slice
+                            ff_acc(hp + (b - b0), v);
+                            if constexpr (KS) {
+                                ff_acc(hk + (b - b0), kk);
+                                ff_acc(hc + (b - b0), FF{(float)c, 0.f});
+                            }
+                        }
+                    }
+                    b = nb;
+                    v = kk = FF{0.f, 0.f};
+                    c = 0;
+                }
+                const int e = up == INT_MAX ? hi : min(hi, ceil_isqrt(up - c2));
+                if (b >= 0 && in_pass(b)) {
+                    v = run_power(reinterpret_cast<const float2 *>(stage), s0, ix, e, nh, v);
+                    if constexpr (KS)
+                        for (int a = ix; a < e; ++a) {
+                            const int wt = (a == 0 || 2 * a == N) ? 1 : 2;
+                            kk = ff_add(kk, ff_scale(mode_norm(a * a + c2), (float)wt));
+                            c += wt;
+                        }
+                }
+                ix = e;
+            }
+        } else
         for (int ix = lo; ix < hi; ++ix) {
             const int n2 = ix * ix + c2;
             int nb = b;
@@ -851,22 +1029,7 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
                 const FF p = mode_power<T>(stage[ix - s0]);
                 v = ff_add(v, FF{fw * p.hi, fw * p.lo});
                 if constexpr (KS) {
-                    // |n| = sqrt(n2) as float-float. Below 2^24, n2 is exact in float:
-                    // hi = sqrtf (correctly rounded), the residual n2 - hi^2 is exact
-                    // in float (that of a correctly rounded square root always is)
-                    // and lo = residual / (2 hi). Above (large 2D lattices), from the
-                    // double square root (this pass runs once per binning).
-                    float2 sq;
-                    if (n2 < (1 << 24)) {
-                        const float n2f = (float)n2;
-                        const float shi = sqrtf(n2f);
-                        sq = make_float2(shi, shi > 0.0f ? __fdiv_rn(fmaf(-shi, shi, n2f), 2.0f * shi) : 0.0f);
-                    } else {
-                        const double rd = sqrt((double)n2);
-                        const float shi = (float)rd;
-                        sq = make_float2(shi, (float)(rd - (double)shi));
-                    }
-                    kk = ff_add(kk, FF{fw * sq.x, fw * sq.y});
+                    kk = ff_add(kk, ff_scale(mode_norm(n2), fw));
                     c += wt;
                 }
             }
@@ -912,6 +1075,14 @@ __global__ void __launch_bounds__(128) k_bin_runs(const typename Cplx<T>::type *
                 ff_acc(hk + (lb - b0), lk);
                 ff_acc(hc + (lb - b0), FF{(float)lc, 0.f});
             }
+        }
+        __syncwarp();
+    }
+    if (!ok) {   // a copy never completed: flag it, then wait (bounded) for this warp's copies in flight
+        if (lane == 0) {
+            atomicOr(derr, DEVERR_TIMEOUT);
+            mbar_wait_bounded(smem_u32(&bars[it & 1]), (uint32_t)((it >> 1) & 1));
+            if (u + nwarps < units) mbar_wait_bounded(smem_u32(&bars[(it + 1) & 1]), (uint32_t)(((it + 1) >> 1) & 1));
         }
         __syncwarp();
     }
@@ -1060,11 +1231,12 @@ static BinPending bin_spectrum_enqueue(Lattice *L, const B &binner, int kind, co
     const int N = L->p.N;
     const int nh = N / 2 + 1;
     // shared memory of one block: 4 warp histograms of nbp bins x 3 rows, the
-    // bin table, 4 staged segments of seg modes. Whole rows and every bin in
-    // one pass when they fit (up to N ~ 3000); else segments of 2048 modes,
-    // then passes over the bins.
-    auto smem_of = [&](int nbp, int seg) {
-        return (size_t)((4 * 3 * nbp + B::kSmemTable * nbins + 1) & ~1) * sizeof(double) + (size_t)4 * seg * 2 * L->esz;
+    // bin table, two staging buffers of a segment of seg modes per warp. Whole
+    // rows and every bin in one pass when they fit (up to N ~ 1500); else
+    // segments of 2048 modes, then passes over the bins.
+    auto smem_of = [&](int nbp, int seg) {   // k_bin_runs' layout: histograms, table, 4 x 2 buffers, 8 mbarriers
+        return (size_t)((4 * 3 * nbp + B::kSmemTable * nbins + 1) & ~1) * sizeof(double) +
+               (size_t)4 * 2 * ((seg + 3) & ~1) * 2 * L->esz + 8 * sizeof(uint64_t);
     };
     const size_t cap = 200 * 1024;
     int nbp = nbins, seg = nh;
@@ -1089,11 +1261,11 @@ static BinPending bin_spectrum_enqueue(Lattice *L, const B &binner, int kind, co
     for (int b0 = 0; b0 < nbins; b0 += nbp) {
         const int nb = std::min(nbp, nbins - b0);
         if (L->esz == 4) {
-            if (ks) k_bin_runs<float, B, true><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, seg, b0, nb, part);
-            else k_bin_runs<float, B, false><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, seg, b0, nb, part);
+            if (ks) k_bin_runs<float, B, true><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, seg, b0, nb, part, L->derr);
+            else k_bin_runs<float, B, false><<<nblk, 128, sm, L->stream>>>((const float2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, seg, b0, nb, part, L->derr);
         } else {
-            if (ks) k_bin_runs<double, B, true><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, seg, b0, nb, part);
-            else k_bin_runs<double, B, false><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, seg, b0, nb, part);
+            if (ks) k_bin_runs<double, B, true><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, seg, b0, nb, part, L->derr);
+            else k_bin_runs<double, B, false><<<nblk, 128, sm, L->stream>>>((const double2 *)L->fft_out, N, L->p.NDIMS, binner, nbins, seg, b0, nb, part, L->derr);
         }
         AXS_CUDA(cudaGetLastError());
         k_bin_final3<<<nb, 256, 0, L->stream>>>(part, nblk, nb, out);
@@ -1104,6 +1276,8 @@ static BinPending bin_spectrum_enqueue(Lattice *L, const B &binner, int kind, co
         AXS_CUDA(cudaMemcpyAsync(host + 3 * (size_t)b0, out, 3 * (size_t)nb * sizeof(double), cudaMemcpyDeviceToHost,
                                  L->stream));
     }
+    // the lattice's error flag into the slot after the rows (host holds 3 nbins + 1 doubles)
+    AXS_CUDA(cudaMemcpyAsync(host + 3 * (size_t)nbins, L->derr, sizeof(int), cudaMemcpyDeviceToHost, L->stream));
     BinPending pd;
     pd.nbins = nbins;
     pd.nbp = nbp;
@@ -1120,6 +1294,12 @@ static BinPending bin_spectrum_enqueue(Lattice *L, const B &binner, int kind, co
 static void bin_spectrum_finish(Lattice *L, const BinPending &pd, std::vector<double> &psum, std::vector<double> &nsum,
                                 std::vector<unsigned long long> &cnt) {
     const int nbins = pd.nbins;
+    int flag = 0;   // the error flag copied after the rows (k_bin_runs' row copies complete on bounded waits)
+    memcpy(&flag, pd.host + 3 * (size_t)nbins, sizeof(int));
+    if (flag & DEVERR_TIMEOUT) {
+        AXS_CUDA(cudaMemsetAsync(L->derr, 0, sizeof(int), L->stream));
+        fail(AXS_ERR_TIMEOUT, "the spectrum binner gave up waiting for a row copy; the spectrum was not computed");
+    }
     psum.assign(nbins, 0.0);
     std::vector<double> nk(pd.ks ? nbins : 0, 0.0), cc(pd.ks ? nbins : 0, 0.0);
     for (int b0 = 0; b0 < nbins; b0 += pd.nbp) {
@@ -1157,7 +1337,7 @@ static void bin_spectrum_finish(Lattice *L, const BinPending &pd, std::vector<do
 template <typename B>
 static void bin_spectrum(Lattice *L, const B &binner, int kind, const std::vector<int> &edges, int nbins,
                          std::vector<double> &psum, std::vector<double> &nsum, std::vector<unsigned long long> &cnt) {
-    std::vector<double> h(3 * (size_t)nbins);
+    std::vector<double> h(3 * (size_t)nbins + 1);   // rows, then the error flag
     const BinPending pd = bin_spectrum_enqueue(L, binner, kind, edges, nbins, h.data());
     AXS_CUDA(cudaStreamSynchronize(L->stream));
     bin_spectrum_finish(L, pd, psum, nsum, cnt);
@@ -1271,7 +1451,7 @@ static void axion_spectrum_finish(Lattice *L, const AxionPending &pd, double *km
 }
 
 void axion_spectrum(Lattice *L, int nbins, double *kmean, double *pk, int64_t *count) {
-    std::vector<double> h(3 * (size_t)std::max(nbins, 1));
+    std::vector<double> h(3 * (size_t)std::max(nbins, 1) + 1);   // rows, then the error flag
     const AxionPending pd = axion_spectrum_enqueue(L, nbins, h.data(), nullptr);
     AXS_CUDA(cudaStreamSynchronize(L->stream));
     axion_spectrum_finish(L, pd, kmean, pk, count);
@@ -1372,12 +1552,13 @@ void ensemble_find_strings(Ensemble *E, int64_t *nplaq, int64_t *ncores) {
 void ensemble_axion_spectrum(Ensemble *E, int nbins, double *kmean, double *pk, int64_t *count) {
     if (nbins < 1) fail(AXS_ERR_ARG, "nbins must be >= 1");
     const size_t n = E->members.size();
-    const size_t per = 3 * (size_t)nbins * sizeof(double) + (((size_t)nbins * sizeof(int) + 15) & ~(size_t)15);
+    // per member: the rows and the error flag (3 nbins + 1 doubles), then the bin thresholds
+    const size_t per = (3 * (size_t)nbins + 2) * sizeof(double) + (((size_t)nbins * sizeof(int) + 15) & ~(size_t)15);
     char *base = (char *)ensemble_pinned(E, n * per);
     std::vector<AxionPending> pend(n);
     ensemble_fan_out(E, [&](Lattice *L, size_t i) {
         double *h = (double *)(base + i * per);
-        int *t = (int *)(base + i * per + 3 * (size_t)nbins * sizeof(double));
+        int *t = (int *)(base + i * per + (3 * (size_t)nbins + 2) * sizeof(double));
         pend[i] = axion_spectrum_enqueue(L, nbins, h, t);
     });
     AXS_CUDA(cudaStreamSynchronize(E->stream));

@@ -762,7 +762,8 @@ int axs_inject_wait_timeout(axs_lattice *h) {
     API_BEGIN
     CHECK_HANDLE(h);
     Lattice *L = &h->L;
-    if (L->in_ensemble) fail(AXS_ERR_STATE, "inject on a lattice that is not an ensemble member");
+    if (L->in_ensemble)
+        fail(AXS_ERR_STATE, "timeout injection on an ensemble member is not supported; use a standalone lattice");
     if (!L->tuned) lattice_evolve(L, 0);   // the configuration the next step will use (tuned unless AXS_AUTOTUNE=0)
     if (L->cfg.kind != 1 || L->p.laplacian != 0)
         fail(AXS_ERR_STATE, "the step kernel in use (%s) has no device-side waits",

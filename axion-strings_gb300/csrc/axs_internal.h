@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <stdint.h>
+#include <atomic>
 #include <map>
 #include <string>
 #include <vector>
@@ -249,7 +250,30 @@ inline int64_t lattice_length(const axs_params &p) {
     int64_t N = p.N;
     return p.NDIMS == 3 ? N * N * N : N * N;
 }
-int num_sms();
+int num_sms();                  // of the current device
+int current_device();
+// A value set up once per device (its SM count or shared-memory limit, a
+// kernel's attribute and occupancy there): one process may drive several
+// GPUs (axs_set_device), and their values may differ. make() runs with the
+// device current; concurrent first calls may both run it (same result).
+constexpr int kMaxDevices = 128;
+struct PerDevice {
+    std::atomic<int> v[kMaxDevices];
+    PerDevice() {
+        for (auto &x : v) x = -1;
+    }
+    template <class F>
+    int get(F make) {
+        const int d = current_device();
+        if (d < 0 || d >= kMaxDevices) return make();
+        int r = v[d].load();
+        if (r < 0) {
+            r = make();
+            v[d] = r;
+        }
+        return r;
+    }
+};
 int reduce_grid(int64_t len);   // fixed grid size of the deterministic reductions
 // Sum per-block partials (nblocks x K, device) in block order on the host.
 void sum_partials(const double *dpart, int nblocks, int K, double *out, cudaStream_t s);

@@ -802,6 +802,21 @@ __device__ __forceinline__ float2 update_site(float2 c, float2 xm, float2 xp, fl
     return o;
 }
 
+// The x neighbours of a thread's two-site vector are 8-byte loads 16 bytes
+// apart across the lanes: left neighbours touch only the banks 2, 3 mod 4 and
+// right neighbours only 0, 1 mod 4, so each load takes twice the wavefronts it
+// needs. Lanes 8-15 of each half-warp therefore load their right neighbour in
+// the first of the two loads and their left one in the second (offsets
+// swapped once per work item), which spreads both loads over all 32 banks;
+// the values are put back in place with selects.
+__device__ __forceinline__ bool swap_lane() { return (threadIdx.x & 8) != 0; }
+__device__ __forceinline__ void x_neighbours(const unsigned char *base, int oa, int ob, bool sw, float2 &left,
+                                             float2 &right) {
+    const float2 a = ldb2(base, oa), b = ldb2(base, ob);
+    left = sw ? b : a;
+    right = sw ? a : b;
+}
+
 // LEAN: the centre psi_n of the in-plane slot and psi_{n+1} of planes m-1 and
 // m-2 are read back from shared memory (a three-plane psi_{n+1} ring) instead
 // of being carried in registers, so the thread fits 128 registers and three
@@ -954,7 +969,9 @@ __device__ __forceinline__ void zmarch_2step_body(const ZLat *__restrict__ lats,
             // Tile vectors: byte offsets of the centre, left and right neighbours
             // in an input slot (psi_n band rows y0-2 .. : centre row 2+yy; the
             // pih band starts one row later) and in a psi_{n+1} plane (row 1+yy),
-            // and the global site offset at plane za.
+            // and the global site offset at plane za. With sw, the left and
+            // right offsets are stored swapped (x_neighbours puts them back).
+            const bool sw = swap_lane();
             int t_c[K::MAXV], t_l[K::MAXV], t_r[K::MAXV], m_l[K::MAXV], m_r[K::MAXV];
             int64_t g_off[K::MAXV];
 #pragma unroll
@@ -969,6 +986,11 @@ __device__ __forceinline__ void zmarch_2step_body(const ZLat *__restrict__ lats,
                 m_l[j] = xx > 0 ? mrow + (xx - 1) * K::CS : (xhalo ? K::MB + yy * K::CS : mrow + (tx - 1) * K::CS);
                 m_r[j] = xx + 2 < tx ? mrow + (xx + 2) * K::CS : (xhalo ? K::MB + (TY + yy) * K::CS : mrow);
                 g_off[j] = (int64_t)za * NN + (int64_t)(y0 + yy) * N + (x0 + xx);
+                if (sw) {   // first load: the right neighbour (see x_neighbours)
+                    const int a = t_l[j], b = m_l[j];
+                    t_l[j] = t_r[j]; t_r[j] = a;
+                    m_l[j] = m_r[j]; m_r[j] = b;
+                }
             }
             // Ring-row vectors (rows y0-1 and y0+TY: band rows 1 and TY+2).
             int r_c[K::MAXR], r_l[K::MAXR], r_r[K::MAXR];
@@ -982,6 +1004,10 @@ __device__ __forceinline__ void zmarch_2step_body(const ZLat *__restrict__ lats,
                 r_l[j] = xx > 0 ? r_c[j] - K::CS
                                 : (xhalo ? K::SL_OFF + strip_off<TY, K::ST_M>(br) + K::CS : rowb + (tx - 1) * K::CS);
                 r_r[j] = xx + 2 < tx ? r_c[j] + 2 * K::CS : (xhalo ? K::SR_OFF + strip_off<TY, K::ST_M>(br) : rowb);
+                if (sw) {
+                    const int a = r_l[j];
+                    r_l[j] = r_r[j]; r_r[j] = a;
+                }
             }
             // Ring-column site: x0-1 (column 1 of the left strips) or x0+tx
             // (column 0 of the right strips), row y0+cyy; it goes to the
@@ -1075,7 +1101,9 @@ __device__ __forceinline__ void zmarch_2step_body(const ZLat *__restrict__ lats,
                     const float4 ac = LEAN ? ldb4(Sc, t_c[j]) : a_c[j];
                     const float4 up = ldb4(Sc, t_c[j] - txb), dn = ldb4(Sc, t_c[j] + txb);
                     float4 p = ldb4(Sc, K::QB_OFF + t_c[j] - txb);
-                    const float4 o = update_vec2(ac, a_zm[j], zp, up, dn, ldb2(Sc, t_l[j]), ldb2(Sc, t_r[j]), p, cf1);
+                    float2 xl, xr;
+                    x_neighbours(Sc, t_l[j], t_r[j], sw, xl, xr);
+                    const float4 o = update_vec2(ac, a_zm[j], zp, up, dn, xl, xr, p, cf1);
                     *reinterpret_cast<float4 *>(Mw + t_c[j] - txb) = o;
                     b_new[j] = o;
                     p_new[j] = p;
@@ -1089,7 +1117,9 @@ __device__ __forceinline__ void zmarch_2step_body(const ZLat *__restrict__ lats,
                     const float4 rc = LEAN ? ldb4(Sc, r_c[j]) : r_cv[j];
                     const float4 up = ldb4(Sc, r_c[j] - txb), dn = ldb4(Sc, r_c[j] + txb);
                     float4 p = ldb4(Sc, K::QB_OFF + r_c[j] - txb);
-                    const float4 o = update_vec2(rc, r_zm[j], zp, up, dn, ldb2(Sc, r_l[j]), ldb2(Sc, r_r[j]), p, cf1);
+                    float2 xl, xr;
+                    x_neighbours(Sc, r_l[j], r_r[j], sw, xl, xr);
+                    const float4 o = update_vec2(rc, r_zm[j], zp, up, dn, xl, xr, p, cf1);
                     *reinterpret_cast<float4 *>(Mw + r_c[j] - txb) = o;
                     r_zm[j] = rc;
                     if constexpr (!LEAN) r_cv[j] = zp;
@@ -1121,7 +1151,9 @@ __device__ __forceinline__ void zmarch_2step_body(const ZLat *__restrict__ lats,
                         const float4 up = ldb4(Mr, mc - txb), dn = ldb4(Mr, mc + txb);
                         const float4 bc = LEAN ? ldb4(Mr, mc) : b_m1[j], bz = LEAN ? ldb4(Mrr, mc) : b_m2[j];
                         float4 p = p_m1[j];
-                        const float4 o = update_vec2(bc, bz, b_new[j], up, dn, ldb2(Mr, m_l[j]), ldb2(Mr, m_r[j]), p, cf2);
+                        float2 xl, xr;
+                        x_neighbours(Mr, m_l[j], m_r[j], sw, xl, xr);
+                        const float4 o = update_vec2(bc, bz, b_new[j], up, dn, xl, xr, p, cf2);
                         st4(&pih_out[g_off[j]], p);
                         st4(&psi_out[g_off[j]], o);
                         g_off[j] += NN;
@@ -1197,15 +1229,19 @@ static void (*zm3_kernel())(const ZLat *, int, int64_t, int *, int, int *) {
 
 // ============================================================== host side
 
-static std::atomic<int> g_num_sms{0};
+int current_device() {
+    int dev = 0;
+    AXS_CUDA(cudaGetDevice(&dev));
+    return dev;
+}
+
 int num_sms() {
-    if (!g_num_sms) {
-        int dev = 0, n = 0;
-        AXS_CUDA(cudaGetDevice(&dev));
-        AXS_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
-        g_num_sms = n;
-    }
-    return g_num_sms;
+    static PerDevice sms;
+    return sms.get([] {
+        int n = 0;
+        AXS_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, current_device()));
+        return n;
+    });
 }
 
 static int grid_for(int64_t len, int threads = 256) {
@@ -1268,15 +1304,14 @@ std::string StepConfig::describe() const {
 template <typename T, int TY, int TXMAX, int S>
 static int prepare_zmarch_t() {
     typedef ZCfg<T, TY, TXMAX, S> K;
-    static std::atomic<int> occ{-1};   // first calls may race: same value
-    if (occ < 0) {
+    static PerDevice occ;   // the attribute and occupancy belong to the device
+    return occ.get([] {
         AXS_CUDA(cudaFuncSetAttribute(k_zmarch<T, TY, TXMAX, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
         int o = 0;
         AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_zmarch<T, TY, TXMAX, S>, K::NT, K::SMEM));
         if (o < 1) fail(AXS_ERR_CUDA, "z-march kernel does not fit on an SM");
-        occ = o;
-    }
-    return occ;
+        return o;
+    });
 }
 
 template <typename T, int TY, int TXMAX, int S>
@@ -1294,15 +1329,14 @@ static void launch_zmarch_t(const ZLat *d, int nlat, int64_t items, int *counter
 template <typename T, int TY, int TXMAX, int S>
 static int prepare_zmarch2_t() {
     typedef Z2Cfg<T, TY, TXMAX, S> K;
-    static std::atomic<int> occ{-1};   // first calls may race: same value
-    if (occ < 0) {
+    static PerDevice occ;   // the attribute and occupancy belong to the device
+    return occ.get([] {
         AXS_CUDA(cudaFuncSetAttribute(k_zmarch2<T, TY, TXMAX, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
         int o = 0;
         AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_zmarch2<T, TY, TXMAX, S>, K::NT, K::SMEM));
         if (o < 1) fail(AXS_ERR_CUDA, "z-march kernel does not fit on an SM");
-        occ = o;
-    }
-    return occ;
+        return o;
+    });
 }
 
 template <typename T, int TY, int TXMAX, int S>
@@ -1320,8 +1354,8 @@ static void launch_zmarch2_t(const ZLat *d, int nlat, int64_t items, int *counte
 template <int TY, int TXMAX, int S, int NCW, int UNR, bool LEAN>
 static int prepare_zmarch3_t() {
     typedef Z3Cfg<TY, TXMAX, S, NCW, LEAN ? 3 : 2> K;
-    static std::atomic<int> occ{-1};   // first calls may race: same value
-    if (occ < 0) {
+    static PerDevice occ;   // the attribute and occupancy belong to the device
+    return occ.get([] {
         const auto kern = zm3_kernel<TY, TXMAX, S, NCW, UNR, LEAN>();
         AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
         int o = 0;
@@ -1335,9 +1369,8 @@ static int prepare_zmarch3_t() {
                  TY, TXMAX, S, NCW, UNR, (int)LEAN, K::NT, fa.numRegs, K::SMEM, fa.maxDynamicSharedSizeBytes,
                  (int)fa.sharedSizeBytes, fa.maxThreadsPerBlock);
         }
-        occ = o;
-    }
-    return occ;
+        return o;
+    });
 }
 
 template <int TY, int TXMAX, int S, int NCW, int UNR, bool LEAN>
@@ -1524,14 +1557,12 @@ static int variant_smem(const ZVariant &v, int esz) {
 }
 
 static int max_smem_optin() {
-    static std::atomic<int> m{0};
-    if (!m) {
-        int dev = 0, v = 0;
-        AXS_CUDA(cudaGetDevice(&dev));
-        AXS_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-        m = v;
-    }
-    return m;
+    static PerDevice m;
+    return m.get([] {
+        int v = 0;
+        AXS_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, current_device()));
+        return v;
+    });
 }
 
 // The tx a variant would use for an N (largest admissible divisor), or 0.
@@ -1963,12 +1994,14 @@ void lattice_evolve(Lattice *L, int nsteps) {
 }
 
 // ---------------------------------------------------------------- autotune
-// Everything that decides which kernels can run: the shape, the precision,
-// the stencil radius and the Laplacian (a spectral lattice never takes a
-// finite-difference configuration tuned for the same shape).
+// Everything that decides which kernels can run and how fast: the device,
+// the shape, the precision, the stencil radius and the Laplacian (a spectral
+// lattice never takes a finite-difference configuration tuned for the same
+// shape).
 struct TuneKey {
-    int n, ndims, esz, stencil, laplacian;
+    int dev, n, ndims, esz, stencil, laplacian;
     bool operator<(const TuneKey &o) const {
+        if (dev != o.dev) return dev < o.dev;
         if (n != o.n) return n < o.n;
         if (ndims != o.ndims) return ndims < o.ndims;
         if (esz != o.esz) return esz < o.esz;
@@ -1995,8 +2028,13 @@ static double time_launches(cudaStream_t st, int reps, const std::function<void(
     return ms / reps;
 }
 
-// Candidate steps run with dt = 0: psi_out = psi + 0*pih and pih + 0*K are
-// bit-identical copies, so the state (and tau) is unchanged. Candidates are
+// Candidate steps run with dt = 0 on the lattice's own buffers:
+// psi_out = psi + 0*pih and pih + 0*K are bit-identical copies for finite
+// values (a -0.0 comes back as +0.0, which compares equal and gives the same
+// decisions and sums), so the state (and tau) is unchanged. An infinite
+// value would come back as NaN, so a state that is not finite is not timed
+// on: the lattice keeps its untuned configuration, which is not cached.
+// Candidates are
 // the generic kernel and every z-march variant that tiles N (one-step
 // variants, and two-step variants with halo depth 2). Every variant is first
 // screened with one launch at one z-chunk; the three fastest are then timed
@@ -2021,7 +2059,7 @@ void lattice_autotune(Lattice *L) {
             return;
         }
     }
-    TuneKey key{L->p.N, L->p.NDIMS, L->esz, L->p.stencil_setting, L->p.laplacian};
+    TuneKey key{current_device(), L->p.N, L->p.NDIMS, L->esz, L->p.stencil_setting, L->p.laplacian};
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto hit = g_tune_cache.find(key);
@@ -2039,6 +2077,7 @@ void lattice_autotune(Lattice *L) {
             return;
         }
     }
+    if (!check_finite(L)) return;
     float dt_save = L->p.time_step;
     L->p.time_step = 0.0f;
     int reps = L->length >= (1 << 27) ? 4 : 10;
@@ -2104,10 +2143,10 @@ void lattice_autotune(Lattice *L) {
                                  L->stream));
         L->cur = cur_save;
     }
-    check_device_errors(L);
     L->cfg = best;
     L->zlat_variant = -1;   // rebuild the table with the real dt before the next step
     clear_graphs(L->graphs);
+    check_device_errors(L);   // a trial that timed out: fail here, with nothing cached
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune_cache[key] = best;
@@ -2228,6 +2267,10 @@ void ensemble_autotune(Ensemble *E) {
             return;
         }
     }
+    // dt = 0 trials on the members' own buffers, as in lattice_autotune: not
+    // on a state that is not finite (it would come back as NaN)
+    for (Lattice *m : E->members)
+        if (!check_finite(m)) return;
     std::vector<int> cur_save;
     for (Lattice *m : E->members) cur_save.push_back(m->cur);
     int reps = 6;
@@ -2269,10 +2312,10 @@ void ensemble_autotune(Ensemble *E) {
             m->cur = cur_save[i];
         }
     }
-    check_device_error_flag(E->derr, E->stream);
     E->cfg = best;
     ensemble_table(E, 0.f, false);
     clear_graphs(E->graphs);
+    check_device_error_flag(E->derr, E->stream);   // a trial that timed out fails here
 }
 
 std::string ensemble_describe(const Ensemble *E) {

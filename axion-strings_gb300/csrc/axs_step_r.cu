@@ -339,16 +339,15 @@ static void (*zr_kernel())(const ZLat *, int, int64_t, int *, int, int *) {
 template <typename T, int TY, int TXMAX, int S, int R>
 static int prepare_r_t() {
     typedef ZRCfg<T, TY, TXMAX, S, R> K;
-    static std::atomic<int> occ{-1};   // first calls may race: same value
-    if (occ < 0) {
+    static PerDevice occ;   // the attribute and occupancy belong to the device
+    return occ.get([] {
         const auto kern = zr_kernel<T, TY, TXMAX, S, R>();
         AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
         int o = 0;
         AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, K::NT, K::SMEM));
         if (o < 1) fail(AXS_ERR_CUDA, "radius-%d z-march kernel does not fit on an SM", R);
-        occ = o;
-    }
-    return occ;
+        return o;
+    });
 }
 
 template <typename T, int TY, int TXMAX, int S, int R>

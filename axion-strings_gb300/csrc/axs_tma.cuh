@@ -42,6 +42,14 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
+// Untiled bulk copy of `bytes` (a multiple of 16) from global to shared
+// memory, both addresses 16-byte aligned, completing on the mbarrier.
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"((uint64_t)src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
 template <typename T> struct Vec16;
 template <> struct Vec16<float> { typedef float4 type; };
 template <> struct Vec16<double> { typedef double2 type; };

@@ -152,9 +152,20 @@ class Dist:
 
 
 # --------------------------------------------------------------------- CPU baseline
+# What the CPU legs time, and how it compares with the reference's own code
+# (oracle/cpu_calibration.py on an 8-core x86 host, 256^3: 1.6-1.9x the
+# reference's FP64 step compiled from its sources with the project's COO SpMV
+# in place of MKL; the direct-stencil port was 0.73-0.81x).
+CPU_KIND = ("oracle port of vvsl_field_rescaled in the reference's six passes, Laplacian as a sparse "
+            "matrix-vector product over build_coefficient_matrix's matrix (CSR), float data_t, OpenMP")
+CPU_CALIBRATION = ("1.6-1.9x the reference's own FP64 step built from its sources with the project's SpMV shim "
+                   "(8-core x86, 256^3; profiles/cpu_baseline_calibration.md)")
+
+
 def cpu_port_rate(n=256, target_s=10.0, max_steps=200, min_steps=2):
-    """The oracle port of vvsl_field_rescaled (reference loop structure, FP32
-    data_t, OpenMP on all host cores) on an n^3 sample; site-updates/s."""
+    """The oracle's timing port of vvsl_field_rescaled (the reference's six
+    passes, its Laplacian as a sparse matrix-vector product, FP32 data_t,
+    OpenMP on all host cores) on an n^3 sample; site-updates/s."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
     orc = oracle_lib.load()
@@ -165,16 +176,22 @@ def cpu_port_rate(n=256, target_s=10.0, max_steps=200, min_steps=2):
     k = [np.zeros((n, n, n), dtype=np.float32) for _ in range(4)]
     t = ctypes.c_float(1.0)
     ptr = [a.ctypes.data for a in f + k]
-    step = lambda: orc.lib.orc_vvsl_step_f32(ctypes.byref(p), *ptr, ctypes.byref(t))
-    step()
-    t0 = time.perf_counter()
-    step()
-    one = time.perf_counter() - t0
-    steps = int(max(min_steps, min(max_steps, target_s / max(one, 1e-6))))
-    t0 = time.perf_counter()
-    for _ in range(steps):
+    A = orc.lib.orc_csr_build(ctypes.byref(p))     # build_coefficient_matrix: once, not timed
+    if not A:
+        raise MemoryError("CPU leg: no memory for the %d^3 sparse matrix" % n)
+    step = lambda: orc.lib.orc_ref_step_f32(ctypes.byref(p), A, *ptr, ctypes.byref(t))
+    try:
         step()
-    dt = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        step()
+        one = time.perf_counter() - t0
+        steps = int(max(min_steps, min(max_steps, target_s / max(one, 1e-6))))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            step()
+        dt = time.perf_counter() - t0
+    finally:
+        orc.lib.orc_csr_free(A)
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return n ** 3 * steps / dt, steps, dt, threads
 
@@ -325,14 +342,16 @@ def workload_name(n, precision, stencil=0):
 
 
 def reference_arm(args, dist):
-    """The reference's CPU path: the oracle port of vvsl_field_rescaled
-    (reference loop structure) on the host cores; oracle/_ref is x86-only."""
+    """The reference's CPU path on the host cores: the oracle's port of
+    vvsl_field_rescaled in the reference's structure (the reference's own
+    sources are not on the GPU machines, so oracle/_ref cannot be built
+    there)."""
     if dist.rank != 0:
         return
     n = 256
     sys.path.insert(0, os.path.join(ROOT, "tests"))
-    rate, steps_done, secs, threads = cpu_port_rate(n=n, target_s=max(5.0, 0.5 * (args.steps + args.warmup)),
-                                                    max_steps=args.steps + args.warmup)
+    # about 10 s of CPU work (up to 600 steps of the 256^3 sample)
+    rate, steps_done, secs, threads = cpu_port_rate(n=n, target_s=10.0, max_steps=600)
     line = {"metric": "site-updates/s", "value": rate, "unit": "site-updates/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n ** 3 / rate,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -340,8 +359,8 @@ def reference_arm(args, dist):
             "config": {"workload": workload_name(args.n, 32), "N": args.n, "precision": "fp32 fields",
                        "sample": "%d^3 lattice, %d steps" % (n, steps_done)},
             "cpu_baseline": {"value": rate, "unit": "site-updates/s", "cores": threads, "kind": "port",
-                             "sample": "%d^3 FP32, %d steps of the reference-structured step (oracle port; "
-                                       "the reference's own build needs MKL/FFTW and x86)" % (n, steps_done)},
+                             "sample": "%d^3 FP32, %d steps (%.1f s)" % (n, steps_done, secs),
+                             "code": CPU_KIND, "calibration": CPU_CALIBRATION},
             "e2e": {"value": rate, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -385,10 +404,10 @@ def gpu_arm(args, dist):
                "analysis_ms": e["analysis_ms"]}
     cpu = None
     if dist.rank == 0 and not args.no_cpu:
-        rate, steps_done, secs, threads = cpu_port_rate(n=256, target_s=10.0)
+        rate, steps_done, secs, threads = cpu_port_rate(n=256, target_s=10.0, max_steps=600)
         cpu = {"value": rate, "unit": "site-updates/s", "cores": threads, "kind": "port",
-               "sample": "256^3 FP32, %d steps (%.1f s) of the reference-structured step (oracle port)"
-                         % (steps_done, secs)}
+               "sample": "256^3 FP32, %d steps (%.1f s)" % (steps_done, secs),
+               "code": CPU_KIND, "calibration": CPU_CALIBRATION}
     e2e = main.get("e2e")
     e2e_line = None
     if e2e:
@@ -398,6 +417,16 @@ def gpu_arm(args, dist):
                     "steps": E2E_STEPS}
     if dist.rank != 0:
         return
+    # state held on the device: two psi buffers, pi and the spare (complex)
+    state_bytes = 4 * 2 * (args.precision // 8) * main["sites"]
+    big = state_bytes > 129e6
+    l2_note = ("state %.3g GB %s 129 MB L2: %s" %
+               (state_bytes / 1e9, ">" if big else "<=",
+                "every pass streams from HBM, no flush needed" if big else
+                "the state fits in L2; figures are L2-resident, not HBM"))
+    # 32 B (FP32) per site-update is the algorithmic minimum of one step per
+    # pass; a two-step pass moves those bytes once for two site-updates
+    per_step_achieved = BYTES_PER_SITE[args.precision] * value / dist.world / 1e9
     line = {
         "metric": "site-updates/s", "value": value, "unit": "site-updates/s", "n_gpus": dist.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": main["ms"] / args.steps,
@@ -406,9 +435,19 @@ def gpu_arm(args, dist):
         "config": {"workload": workload_name(args.n, args.precision, args.stencil),
                    "N": args.n, "precision": "fp32 fields, fp64 tau",
                    "parallelism": "replicas" if dist.world > 1 else "single",
-                   "l2": "state 25.8 GB >> 129 MB L2; no flush needed", "kernel": main["desc"]},
+                   "l2": l2_note, "kernel": main["desc"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "frac_per_pass": achieved / hbm,
+                     "effective_bytes_per_step_frac": per_step_achieved / hbm,
+                     "effective_note": ("%d B per site-update (one step per pass) x site-updates/s over the peak; "
+                                        "above 1 because the kernel takes %g steps per pass (temporal blocking), "
+                                        "bit-identical to one-step passes" % (BYTES_PER_SITE[args.precision],
+                                                                               steps_per_launch))
+                                       if steps_per_launch > 1 else "one step per pass: equals frac_per_pass",
                      "traffic": traffic, "traffic_unit": "GB per launch (ncu dram read+write)",
+                     "traffic_source": ("profiles/k_zmarch_traffic.txt: dram__bytes_read.sum + dram__bytes_write.sum "
+                                        "of this kernel in an ncu launch list of this bench command")
+                                       if traffic else None,
                      "algorithmic_gb_per_launch": BYTES_PER_SITE[args.precision] * main["sites"] / 1e9,
                      "peak_source": peak_note,
                      "algorithmic_bytes_per_site_update": BYTES_PER_SITE[args.precision] / steps_per_launch,

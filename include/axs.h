@@ -128,8 +128,10 @@ int axs_set_time(axs_lattice *h, double tau, int64_t steps);
 /* gaussian_thermal (src/common/init.cpp:33-200): Bose-Einstein amplitudes at
  * T_initial for phi and phidot, inverse FFT, checkerboard shift, 1/N^d.
  * The deviates are the project's Philox-4x32-10 + Box-Muller stream, not MKL
- * SFMT19937. The 3D k=0 phidot amplitude (uninitialised in init.cpp:377-378)
- * is 0. Resets tau to tau_initial and the step counter to 0. */
+ * SFMT19937. The 3D k=0 phidot amplitude (never set by init.cpp:163-164,
+ * which assign the phi amplitude twice) is 0; the reference as compiled keeps
+ * the previous mode's value there, a constant offset of its phidot. Resets
+ * tau to tau_initial and the step counter to 0. */
 int axs_init_gaussian_thermal(axs_lattice *h, uint64_t seed);
 /* Flat spectrum for 0 < |k| < kcut (k = 2 pi n / L), zero elsewhere, scaled
  * to <|phi|^2> = 1 at tau_initial, phidot = 0 (no reference counterpart). */

@@ -209,3 +209,59 @@ def test_fast_atan2_error_bound():
         r = np.copysign(r, y)
         err = np.abs(r.astype(np.float64) - np.arctan2(y.astype(np.float64), x.astype(np.float64)))
         assert err.max() <= 5e-7, (shift, err.max())
+
+
+def _table(name, n):
+    import re
+    src = open(os.path.join(oracle_lib.ROOT, "axion-strings_gb300", "csrc", "axs_analysis.cu")).read()
+    body = re.search(name + r"\[%d\] = \{([^}]*)\}" % n, src).group(1)
+    c = np.array([float(t.strip().rstrip("f")) for t in body.split(",")], dtype=np.float32)
+    assert c.size == n
+    return c
+
+
+def test_fast_turns_error_bound():
+    """The string finder's float angle in turns (fast_turns, re-evaluated here
+    in float32 step by step) stays within 3.3e-7 turns of atan2/(2 pi) in all
+    four quadrants and on the axes, with the division anywhere within its 2
+    ulp: the finder's 1e-5 decision margin rests on it (edge values within
+    7e-7, a plaquette's sum of three within 2.3e-6)."""
+    c = _table("kTurnC", 6)
+    rng = np.random.default_rng(6)
+    ang = np.concatenate([rng.uniform(-np.pi, np.pi, 400000), np.arange(-4, 5) * np.pi / 4])
+    rad = np.concatenate([rng.uniform(1e-3, 10.0, 400000), np.full(9, 2.5)])
+    y = (rad * np.sin(ang)).astype(np.float32)
+    x = (rad * np.cos(ang)).astype(np.float32)
+    y[-9:][[0, 4, 8]] = 0.0   # exact axes: y = 0 at x < 0 (both signs of zero) and x > 0
+    y[-9] = -0.0
+    x[-9:][[2, 6]] = 0.0
+    ax, ay = np.abs(x), np.abs(y)
+    mx, mn = np.maximum(ax, ay), np.minimum(ax, ay)
+    a0 = (mn / mx).astype(np.float32)
+    up = np.float32(np.inf)
+    for shift in (-2, -1, 0, 1, 2):   # __fdividef: within 2 ulp of the rounded quotient
+        a = a0.copy()
+        for _ in range(abs(shift)):
+            a = np.where(a > 0, np.nextafter(a, up if shift > 0 else -up), a).astype(np.float32)
+        s = (a * a).astype(np.float32)
+        p = np.full_like(a, c[5])
+        for k in range(4, -1, -1):
+            p = (p.astype(np.float64) * s + c[k]).astype(np.float32)   # fmaf: one rounding
+        r = (p * a).astype(np.float32)
+        r = np.where(ay > ax, (np.float32(0.25) - r).astype(np.float32), r)
+        r = np.where(x < 0, (np.float32(0.5) - r).astype(np.float32), r)
+        r = np.copysign(r, y)
+        want = np.arctan2(y.astype(np.float64), x.astype(np.float64)) / (2 * np.pi)
+        err = np.abs(r.astype(np.float64) - want)
+        assert err.max() <= 3.3e-7, (shift, err.max())
+
+
+def test_atan_tables_match_their_generator():
+    """Both float atan tables are the output of tests/atan_fit.py (to the last
+    float32 ulp, for BLAS rounding differences between machines)."""
+    import atan_fit
+    for name, gen in atan_fit.tables().items():
+        c = _table(name, len(gen))
+        g = gen.astype(np.float32)
+        ulp = np.spacing(np.abs(g))
+        assert np.all(np.abs(c - g) <= ulp), (name, c, g)

@@ -1,5 +1,5 @@
 """The allocation-free spectrum binner (axs_powerspec_noalloc) against the
-allocating entry point (axs_powerspec) on the same field.
+allocating entry point (axs_powerspec) and the oracle on the same field.
 
 axs_powerspec_noalloc is for callers that own every byte of device memory
 and cannot have this library call cudaMalloc/cudaFree: they bring the R2C
@@ -14,13 +14,13 @@ every other test before it. It also passes on its own in a fresh process
 import numpy as np
 import pytest
 
-from gpu_util import params
+from gpu_util import orc, params
 
 pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("nd,N,precision,tol", [(3, 32, 64, 1e-11), (2, 64, 64, 1e-11), (3, 48, 32, 1e-5)])
-def test_noalloc_binner_matches_powerspec_twice(axs, nd, N, precision, tol):
+def test_noalloc_binner_matches_powerspec_twice(axs, oracle, nd, N, precision, tol):
     torch = pytest.importorskip("torch")
     p = params(axs, nd, N, precision)
     rdt = torch.float64 if precision == 64 else torch.float32
@@ -50,6 +50,11 @@ def test_noalloc_binner_matches_powerspec_twice(axs, nd, N, precision, tol):
         assert np.abs(pk_h[ok] - pk_w[ok]).max() <= tol * np.abs(pk_w[ok]).max()
         assert np.abs(ks_h[ok] - ks_w[ok]).max() <= tol * np.abs(ks_w[ok]).max()
         assert np.all(np.isnan(pk_h[~ok])) and np.all(np.isnan(pk_w[~ok]))
+        # and directly against the oracle's output_powerspec of the same field
+        pk_o, ks_o, cnt_o = oracle.powerspec(orc(p), field)
+        assert np.array_equal(cnt_h, cnt_o)
+        assert np.abs(pk_h[ok] - pk_o[ok]).max() <= tol * np.abs(pk_o[ok]).max()
+        assert np.abs(ks_h[ok] - ks_o[ok]).max() <= tol * np.abs(ks_o[ok]).max()
 
 
 def test_noalloc_binner_rejects_sizes_beyond_its_scratch(axs):
