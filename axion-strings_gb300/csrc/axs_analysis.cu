@@ -733,20 +733,21 @@ struct RefBinsI {
 struct LogBinsI {
     const int *thr;   // thr[b] for b = 1..nbins-1 (thr[0] = 0)
     int nbins;
+    float lscale;     // nbins / log2(ratio^2): thr[b] ~ ratio^(2b/nbins), so b ~ log2(n2) * lscale
     __device__ __forceinline__ LogBinsI staged(double *s) const {
         int *t = reinterpret_cast<int *>(s);
         for (int i = threadIdx.x; i < nbins; i += blockDim.x) t[i] = thr[i];
-        return LogBinsI{t, nbins};
+        return LogBinsI{t, nbins, lscale};
     }
     static constexpr int kSmemTable = 1;   // nbins ints fit in nbins doubles
+    // The bin from the logarithm's estimate (off by at most a step or two),
+    // then moved to the largest b with thr[b] <= n2: the table decides.
     __device__ __forceinline__ int bin(int n2) const {
         if (n2 == 0) return -1;
-        int lo = 0, hi = nbins - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (thr[mid] <= n2) lo = mid; else hi = mid - 1;
-        }
-        return lo;
+        int b = min(nbins - 1, max(0, (int)(__log2f((float)n2) * lscale)));
+        while (b + 1 < nbins && thr[b + 1] <= n2) ++b;
+        while (b > 0 && thr[b] > n2) --b;
+        return b;
     }
     // bin of n2 >= the n2 that gave b (bins only grow along a row)
     __device__ __forceinline__ int next(int b, int n2) const {
@@ -919,45 +920,59 @@ __global__ void __launch_bounds__(128, 8) k_bin_runs(const typename Cplx<T>::typ
     // copy itself (lane 0). The copy ends on 16 bytes too: at most one mode
     // past the segment, which exists (the array holds an even number of modes,
     // so the last segment's copy ends exactly at its end).
-    auto unit_off = [&](int64_t uu) -> int {
-        const int64_t rr = uu / nseg;
-        return sizeof(C) == 8 ? (int)((rr * nh + (uu - rr * nseg) * seg) & 1) : 0;
+    auto unit_off = [&](int rr, int ssi) -> int {
+        return sizeof(C) == 8 ? (int)(((unsigned)rr * (unsigned)nh + (unsigned)(ssi * seg)) & 1u) : 0;
     };
-    auto issue = [&](int64_t uu, int buf) {
-        const int64_t rr = uu / nseg;
-        const int ss0 = (int)(uu - rr * nseg) * seg, ssl = min(seg, nh - ss0);
-        const int off = unit_off(uu);
+    auto issue = [&](int rr, int ssi, int buf) {
+        const int ss0 = ssi * seg, ssl = min(seg, nh - ss0);
+        const int off = unit_off(rr, ssi);
         const uint32_t bytes = (uint32_t)(((size_t)(ssl + off) * sizeof(C) + 15) & ~(size_t)15);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // after this warp's reads of the buffer
         mbar_expect_tx(smem_u32(&bars[buf]), bytes);
-        bulk_load(smem_u32(stg + (size_t)buf * sbuf), F + rr * nh + ss0 - off, bytes, smem_u32(&bars[buf]));
+        bulk_load(smem_u32(stg + (size_t)buf * sbuf), F + (int64_t)rr * nh + ss0 - off, bytes, smem_u32(&bars[buf]));
     };
+    // A unit is (row r, segment si); in 3D row r = iz N + iy (rows < N^2 <=
+    // 2^24). A warp advances nwarps units at a time: dr rows and ds segments,
+    // carried incrementally, so no unit costs a 64-bit division.
     const int64_t ufirst = (int64_t)blockIdx.x * 4 + w;
-    if (lane == 0 && ufirst < units) issue(ufirst, 0);
+    const int dr = (int)(nwarps / nseg), ds = (int)(nwarps - (int64_t)dr * nseg);
+    const int dz = ndims == 3 ? dr / N : 0, dy = ndims == 3 ? dr - dz * N : 0;
+    int r = (int)(ufirst / nseg), si = (int)(ufirst - (int64_t)r * nseg);
+    int iz = ndims == 3 ? r / N : 0, iy = ndims == 3 ? r - iz * N : 0;
+    if (lane == 0 && ufirst < units) issue(r, si, 0);
     int it = 0;
     bool ok = true;
     int64_t u = ufirst;
     for (; u < units; u += nwarps, ++it) {
         const int cur = it & 1;
+        // the next unit's position (a carry from the segments into the rows, and
+        // in 3D from y into z; dy + 1 < 2N, so one wrap suffices)
+        int si_n = si + ds, carry = 0;
+        if (si_n >= nseg) { si_n -= nseg; carry = 1; }
+        const int r_n = r + dr + carry;
+        int iy_n = iy + dy + carry, iz_n = iz + dz;
+        if (iy_n >= N) { iy_n -= N; ++iz_n; }
         __syncwarp();   // every lane is done with the other buffer (the previous unit)
-        if (lane == 0 && u + nwarps < units) issue(u + nwarps, cur ^ 1);
+        if (lane == 0 && u + nwarps < units) issue(r_n, si_n, cur ^ 1);
         ok = __all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[cur]), (uint32_t)((it >> 1) & 1)));
         if (!ok) break;
-        const C *stage = stg + (size_t)cur * sbuf + unit_off(u);
-        const int64_t r = u / nseg;
-        const int s0 = (int)(u - r * nseg) * seg, sl = min(seg, nh - s0);
+        const C *stage = stg + (size_t)cur * sbuf + unit_off(r, si);
+        const int s0 = si * seg, sl = min(seg, nh - s0);
         const int chunk = (sl + 31) / 32;
         const int lo = s0 + min(sl, lane * chunk), hi = s0 + min(sl, lane * chunk + chunk);
         // |n|^2 = ix^2 + fy^2 (+ fz^2) <= 2 (N/2)^2 < 2^31 in 2D (N <= 32768), 3 (N/2)^2 in 3D (N <= 4096): int
         int c2;
         if (ndims == 2) {
-            const int fy = r < N / 2 ? (int)r : (int)r - N;
+            const int fy = r < N / 2 ? r : r - N;
             c2 = fy * fy;
         } else {
-            const int iz = (int)r / N, iy = (int)r - iz * N;   // r < N^2
             const int fz = iz < N / 2 ? iz : iz - N, fy = iy < N / 2 ? iy : iy - N;
             c2 = fy * fy + fz * fz;
         }
+        r = r_n;   // the rest of the body uses s0, sl, lo, hi and c2
+        si = si_n;
+        iz = iz_n;
+        iy = iy_n;
         int b = -1, fb = -1, lb = -1;
         int up = 0;          // the bin is looked up again once n2 reaches this
         bool inp = false;    // in_pass(b)
@@ -1427,7 +1442,8 @@ static AxionPending axion_spectrum_enqueue(Lattice *L, int nbins, double *host, 
         src = thr_host;
     }
     AXS_CUDA(cudaMemcpyAsync(de2, src, nbins * sizeof(int), cudaMemcpyHostToDevice, L->stream));
-    pd.bin = bin_spectrum_enqueue(L, LogBinsI{de2, nbins}, 1, pd.thr, nbins, host);
+    pd.bin = bin_spectrum_enqueue(L, LogBinsI{de2, nbins, (float)((double)nbins / log2(ratio * ratio))}, 1, pd.thr,
+                                  nbins, host);
     return pd;
 }
 
