@@ -45,15 +45,18 @@ __device__ constexpr float kAtanC[8] = {9.999993443e-01f, -3.332986236e-01f, 1.9
 // The string finder's angle in turns, atan2(y, x) / (2 pi): the same
 // reduction with P of degree 5 fitted to atan(a) / (2 pi) (tests/atan_fit.py),
 // within 2.8e-7 turns (1.7e-6 rad) evaluated in float, and the octant undone
-// in turns (1/4, 1/2). Only zeros on both axes, magnitudes outside
-// [1e-30, 1e30] and NaN take atan2f: with one zero component the reduced
-// argument is 0 and the fix-ups give atan2's signed axis values.
+// in turns (1/4, 1/2). Only |x| + |y| outside [2e-30, 1e30] (so max(|x|, |y|)
+// within [1e-30, 1e30] otherwise) and a NaN component take atan2f: with one
+// zero component the reduced argument is 0 and the fix-ups give atan2's
+// signed axis values. turns_core is the polynomial path; it clears `ok` when
+// the pair needs atan2f, so a caller can test several angles at once.
 __device__ constexpr float kTurnC[6] = {1.591513157e-01f, -5.293861777e-02f, 3.080324642e-02f,
                                         -1.853073202e-02f, 8.380074054e-03f, -1.865555299e-03f};
-__device__ __forceinline__ float fast_turns(float y, float x) {
+__device__ __forceinline__ float turns_core(float y, float x, bool &ok) {
     const float ax = fabsf(x), ay = fabsf(y);
     const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
-    if (!(mx >= 1e-30f && mx <= 1e30f)) return atan2f(y, x) * 0.15915494309189535f;
+    const float sum = ax + ay;   // NaN when either component is
+    ok = ok && sum >= 2e-30f && sum <= 1e30f;
     const float a = __fdividef(mn, mx);   // within 2 ulp for 2^-126 <= mx <= 2^126
     const float s = a * a;
     float p = kTurnC[5];
@@ -63,6 +66,11 @@ __device__ __forceinline__ float fast_turns(float y, float x) {
     if (ay > ax) r = 0.25f - r;
     if (x < 0.0f) r = 0.5f - r;
     return copysignf(r, y);
+}
+__device__ __forceinline__ float fast_turns(float y, float x) {
+    bool ok = true;
+    const float r = turns_core(y, x, ok);
+    return ok ? r : atan2f(y, x) * 0.15915494309189535f;
 }
 __device__ __forceinline__ float fast_atan2(float y, float x) {
     const float ax = fabsf(x), ay = fabsf(y);
@@ -178,38 +186,47 @@ __global__ void __launch_bounds__(256) k_cores(const typename Cplx<T>::type *__r
 }
 
 // 3D finder from psi, tiled: a block owns a CX x CY tile of cells and marches a
-// z-chunk; the angles of the tile's sites (one site of halo in +x and +y), in
-// turns theta/(2 pi) (fast_turns; n of the reference minus 1/2, which no
-// difference sees), are computed once per site into a two-plane shared ring
-// (k_cores evaluates them once per corner, six times per site). Each thread
-// owns a run of four cells along x in one row and keeps the angles of plane z
-// (rows y, y+1, five sites each) and the edge values of their y-edges in
-// registers, so per plane it reads ten angles of plane z+1 (two 16-byte and
-// two 4-byte shared loads) and forms 21 edge values for its four cells; the
-// four mask bytes go out as one 32-bit store when N is a multiple of 4.
+// z-chunk. Each thread owns a run of four cells along x in one row and loads
+// the four sites at their (i,j,k) corners (in FP32 two 16-byte loads when N is
+// a multiple of 4); threads 0-80 load one more site each, the tile's +y row
+// and +x column. The angles, in turns theta/(2 pi) (fast_turns; n of the
+// reference minus 1/2, which no difference sees), are computed once per site
+// into a two-plane shared ring (k_cores evaluates them once per corner, six
+// times per site), one range test for a thread's four. A thread keeps its own
+// four angles in registers and per plane reads six of plane z+1 from the ring
+// (one 16-byte and two 4-byte shared loads: row y+1 and the +x neighbours);
+// it carries the angles of plane z and the edge values of their y-edges, and
+// forms 21 edge values for its four cells. The four mask bytes go out as one
+// 32-bit store when N is a multiple of 4.
 // An edge is kept as t = 1/2 - |d| (d the difference of its angles, |d| < 1):
 // the reference's min(|d|, 1 - |d|) is 1/2 - |t|, so a plaquette's sum is
 // 3/2 - (|t1| + |t2| + |t3|) and the three sums of a cell exceed accept when
-// the least sum of |t| is below 3/2 - accept. The float stage decides at a
-// margin of kMargin from that bound (its error: angles within 3.2e-7 turns
-// with the division and the octant roundings, edges within 7e-7, a sum of
-// |t| within 2.3e-6); the other cells take the double replay after the march.
+// the least sum of |t| is below 3/2 - accept. Plaquettes a and b share their
+// z-edge e, so the cell's least sum is min(e + min(sa', sb'), sc) with sa',
+// sb' the sums of their other two edges. The float stage decides at a margin
+// of kMargin from that bound (its error: angles within 3.2e-7 turns with the
+// division and the octant roundings, edges within 7e-7, a sum of |t| within
+// 2.3e-6); the other cells take the double replay after the march. A thread
+// whose twelve sums all lie above the margin (nearly every thread: flagged
+// cells are rare) writes four zero bytes without forming the flag bits.
 static constexpr int kCX = 64, kCY = 16, kCZ = 32;   // cells per block tile; 256 threads x 4 cells
+static constexpr int kHalo = kCX + kCY + 1;          // the tile's +y row and +x column (with the corner)
 
 // 1/2 - |b - a| for angles in turns (see above)
 __device__ __forceinline__ float half_gap(float a, float b) { return 0.5f - fabsf(b - a); }
 static_assert(kCZ * 4 <= 128, "two 64-bit words of margin bits per thread");
 static constexpr int kRS = kCX + 4;                   // shared row stride: 16-byte aligned rows, +x halo at kCX
 
-template <typename T>
-// Four CTAs per SM (64 registers, a few bytes of spills): the march is
-// latency-bound, and 32 warps per SM ran 3.12 against 3.36 ms at 1024^3 for 24.
-__global__ void __launch_bounds__(256, 4) k_cores3_tiled(const typename Cplx<T>::type *__restrict__ psi,
-                                                      uint8_t *__restrict__ mask, int N, double accept,
-                                                      unsigned long long *count) {
+// VEC: N is a multiple of 4, so a thread's four cells are all in the lattice
+// or all outside it and its four sites are contiguous and 16-byte aligned.
+// FP32: four CTAs per SM (64 registers); the march is issue-bound, and 32
+// warps per SM ran 3.12 against 3.36 ms at 1024^3 for 24. FP64 holds twice
+// the prefetched field in registers: three CTAs.
+template <typename T, bool VEC>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3)
+    k_cores3_tiled(const typename Cplx<T>::type *__restrict__ psi, uint8_t *__restrict__ mask, int N, double accept,
+                   unsigned long long *count) {
     typedef typename Cplx<T>::type C;
-    constexpr int NS = (kCX + 1) * (kCY + 1);   // sites of a plane tile with its +x/+y halo
-    constexpr int PER = (NS + 255) / 256;
     __shared__ __align__(16) float nsm[2][kCY + 1][kRS];
     Corner<T, false> cn{psi, nullptr};
     const float acc_f = (float)accept;
@@ -221,25 +238,37 @@ __global__ void __launch_bounds__(256, 4) k_cores3_tiled(const typename Cplx<T>:
     const int tid = threadIdx.x;
     const int lx = 4 * (tid & 15), ly = tid >> 4;   // the thread's cells: (lx .. lx+3, ly) of the tile
     const int gx = x0 + lx, gy = y0 + ly;
-    unsigned long long local = 0;
-    // Per-thread offsets do not depend on z: the tile sites this thread loads
-    // (in-plane offset, shared index; -1 when outside).
-    int so[PER], si[PER];
+    unsigned local = 0;   // flagged cells of this thread (at most 4 kCZ)
+    // bit 4 (z - z0 - 8 w) + j of unc[w][tid]: cell (gx + j, gy, z) lies within
+    // the float margin (in shared memory: set rarely, read once at the end)
+    __shared__ unsigned unc[kCZ / 8][256];
 #pragma unroll
-    for (int k = 0; k < PER; ++k) {
-        const int s = tid + k * 256;
-        const int sx = s % (kCX + 1), sy = s / (kCX + 1);
-        int sgx = x0 + sx, sgy = y0 + sy;
-        si[k] = -1;
-        so[k] = 0;
-        if (s >= NS || sgx > N || sgy > N) continue;
-        sgx = sgx >= N ? sgx - N : sgx;
-        sgy = sgy >= N ? sgy - N : sgy;
-        so[k] = sgy * N + sgx;
-        si[k] = sy * kRS + sx;
+    for (int w = 0; w < kCZ / 8; ++w) unc[w][tid] = 0;
+    // The sites this thread loads, as in-plane offsets that do not depend on z.
+    // A site at x = N or y = N is site 0 of that axis (periodic); sites past
+    // that are corners of no cell in the lattice and are not loaded.
+    const int wy = gy < N ? gy : (gy == N ? 0 : -1);
+    int own = -1;   // VEC: the first of the four sites
+    int xs[4];      // general N: each site's x, -1 when not loaded
+    if (VEC) {
+        const int wx = gx < N ? gx : (gx == N ? 0 : -1);   // gx < N: gx + 3 < N
+        if (wy >= 0 && wx >= 0) own = wy * N + wx;
+    } else {
+        own = wy >= 0 ? wy * N : -1;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int x = gx + j;
+            xs[j] = (wy < 0 || x > N) ? -1 : (x == N ? 0 : x);
+        }
+    }
+    int hso = -1, hsi = 0;   // threads 0-80: the +y row (x0 .. x0+63), then the +x column (y0 .. y0+16)
+    if (tid < kHalo) {
+        const bool row = tid < kCX;
+        const int hx = row ? x0 + tid : x0 + kCX, hy = row ? y0 + kCY : y0 + (tid - kCX);
+        hsi = row ? kCY * kRS + tid : (tid - kCX) * kRS + kCX;
+        if (hx <= N && hy <= N) hso = (hy == N ? 0 : hy) * N + (hx == N ? 0 : hx);
     }
     const bool row_ok = gy < N;
-    const bool packed = row_ok && (N & 3) == 0 && gx < N;   // then gx + 3 < N and the store is 4-byte aligned
     unsigned vmask = 0, vbytes = 0;   // bit / byte j: cell (gx + j, gy) is in the lattice
 #pragma unroll
     for (int j = 0; j < 4; ++j)
@@ -247,30 +276,57 @@ __global__ void __launch_bounds__(256, 4) k_cores3_tiled(const typename Cplx<T>:
             vmask |= 1u << j;
             vbytes |= 1u << (8 * j);
         }
-    unsigned long long unc0 = 0, unc1 = 0;   // bit 4 (z - z0) + j: cell within the float margin (kCZ = 32 planes)
-    C pre[PER];   // psi of the next plane's tile, loaded one plane ahead
+    // psi of the next plane's sites, loaded one plane ahead; sites not loaded
+    // keep (0, 1), a valid angle that only cells outside the lattice see
+    C pre[4], ph;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) pre[j] = C{T(0), T(1)};
+    ph = C{T(0), T(1)};
     auto load = [&](int z) {
         const C *pl = psi + (int64_t)(z >= N ? z - N : z) * NN;
+        if (VEC) {
+            if (own >= 0) {
+                if constexpr (sizeof(T) == 4) {
+                    const float4 *q = reinterpret_cast<const float4 *>(pl + own);
+                    const float4 u = q[0], v = q[1];
+                    pre[0] = C{u.x, u.y};
+                    pre[1] = C{u.z, u.w};
+                    pre[2] = C{v.x, v.y};
+                    pre[3] = C{v.z, v.w};
+                } else {
 #pragma unroll
-        for (int k = 0; k < PER; ++k)
-            if (si[k] >= 0) pre[k] = pl[so[k]];
-    };
-    auto store = [&](int buf) {
-        float *dst = &nsm[buf][0][0];
+                    for (int j = 0; j < 4; ++j) pre[j] = pl[own + j];
+                }
+            }
+        } else {
 #pragma unroll
-        for (int k = 0; k < PER; ++k)
-            if (si[k] >= 0) dst[si[k]] = fast_turns((float)pre[k].x, (float)pre[k].y);
+            for (int j = 0; j < 4; ++j)
+                if (xs[j] >= 0) pre[j] = pl[own + xs[j]];
+        }
+        if (hso >= 0) ph = pl[hso];
     };
-    // angles of rows ly, ly+1 at x = lx .. lx+4 of a buffered plane
+    // the angles of the prefetched plane: the thread's four into c[0..3] and
+    // the ring's row ly, the halo site into the ring
+    auto angles = [&](int buf, float (&c)[5]) {
+        bool ok = true;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) c[j] = turns_core((float)pre[j].x, (float)pre[j].y, ok);
+        if (!ok) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) c[j] = fast_turns((float)pre[j].x, (float)pre[j].y);
+        }
+        *reinterpret_cast<float4 *>(&nsm[buf][ly][lx]) = make_float4(c[0], c[1], c[2], c[3]);
+        if (hso >= 0) (&nsm[buf][0][0])[hsi] = fast_turns((float)ph.x, (float)ph.y);
+    };
+    // after the barrier: the +x neighbour of row ly and row ly+1 at x = lx .. lx+4
     auto read = [&](int buf, float (&r0)[5], float (&r1)[5]) {
-        const float4 u = *reinterpret_cast<const float4 *>(&nsm[buf][ly][lx]);
         const float4 v = *reinterpret_cast<const float4 *>(&nsm[buf][ly + 1][lx]);
-        r0[0] = u.x; r0[1] = u.y; r0[2] = u.z; r0[3] = u.w; r0[4] = nsm[buf][ly][lx + 4];
+        r0[4] = nsm[buf][ly][lx + 4];
         r1[0] = v.x; r1[1] = v.y; r1[2] = v.z; r1[3] = v.w; r1[4] = nsm[buf][ly + 1][lx + 4];
     };
     float a0[5], a1[5], ya[5];   // plane z: rows y, y+1 and their y-edge values t
     load(z0);
-    store(0);
+    angles(0, a0);
     load(z0 + 1);
     __syncthreads();
     read(0, a0, a1);
@@ -278,44 +334,48 @@ __global__ void __launch_bounds__(256, 4) k_cores3_tiled(const typename Cplx<T>:
     for (int i = 0; i < 5; ++i) ya[i] = half_gap(a0[i], a1[i]);
     // One plane: plane z+1 goes into buffer nb, the one last read two planes
     // ago (every thread is past the previous barrier, so done with it).
+    int64_t mo = (int64_t)z0 * NN + (int64_t)gy * N + gx;   // mask offset of cell (gx, gy, z)
     auto plane_step = [&](const int z, const int nb) {
-        store(nb);
+        float b0[5], b1[5], yb[5];
+        angles(nb, b0);
         if (z + 2 <= z1) load(z + 2);   // in flight while plane z is evaluated
         __syncthreads();
-        float b0[5], b1[5], yb[5];
         read(nb, b0, b1);
 #pragma unroll
         for (int i = 0; i < 5; ++i) yb[i] = half_gap(b0[i], b1[i]);
-        unsigned word = 0, und = 0;
+        float tm[4];   // each cell's least sum of |t|
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             // f000 = a0[j], f001 = a0[j+1], f010 = a1[j], f011 = a1[j+1],
             // f100 = b0[j], f110 = b1[j]; plaquettes a, b, c of string_finding.cpp:49-82
             const float e_000_100 = fabsf(half_gap(a0[j], b0[j]));
-            const float ta = e_000_100 + fabsf(yb[j]) + fabsf(half_gap(b1[j], a1[j]));
-            const float tb = e_000_100 + fabsf(half_gap(b0[j], a1[j + 1])) + fabsf(ya[j + 1]);   // the (i,j+1,k+1) corner
+            const float sa = fabsf(yb[j]) + fabsf(half_gap(b1[j], a1[j]));
+            const float sb = fabsf(half_gap(b0[j], a1[j + 1])) + fabsf(ya[j + 1]);   // the (i,j+1,k+1) corner
             const float tc = fabsf(ya[j]) + fabsf(half_gap(a1[j], a1[j + 1])) + fabsf(ya[j + 1]);
-            const float tmin = fminf(ta, fminf(tb, tc));
-            const bool flag = tmin < t_flag;
-            word |= (flag ? 1u : 0u) << (8 * j);
-            und |= (!flag && tmin <= t_undecided ? 1u : 0u) << j;   // the double replay, after the march
+            tm[j] = fminf(e_000_100 + fminf(sa, sb), tc);
         }
-        word &= vbytes;   // cells past the lattice's edge (N not a multiple of 4)
-        und &= vmask;
-        const int nflag = __popc(word);
-        if (und) {
-            const int b = (z - z0) * 4;   // bits b .. b+3 of the 128-bit set; b is a multiple of 4
-            if (b < 64) unc0 |= (unsigned long long)und << b;
-            else unc1 |= (unsigned long long)und << (b - 64);
+        unsigned word = 0;
+        if (fminf(fminf(tm[0], tm[1]), fminf(tm[2], tm[3])) <= t_undecided) {
+            unsigned und = 0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const bool flag = tm[j] < t_flag;
+                word |= (flag ? 1u : 0u) << (8 * j);
+                und |= (!flag && tm[j] <= t_undecided ? 1u : 0u) << j;   // the double replay, after the march
+            }
+            word &= vbytes;   // cells past the lattice's edge
+            und &= vmask;
+            local += __popc(word);
+            if (und) unc[(z - z0) >> 3][tid] |= und << (4 * ((z - z0) & 7));
         }
-        uint8_t *mz = mask + (int64_t)z * NN + (int64_t)gy * N + gx;
-        if (packed) *reinterpret_cast<unsigned *>(mz) = word;
-        else if (row_ok) {
+        if (VEC) {
+            if (vbytes) *reinterpret_cast<unsigned *>(mask + mo) = word;   // 4-byte aligned: N, gx multiples of 4
+        } else if (row_ok) {
 #pragma unroll
             for (int j = 0; j < 4; ++j)
-                if (gx + j < N) mz[j] = (uint8_t)(word >> (8 * j));
+                if (gx + j < N) mask[mo + j] = (uint8_t)(word >> (8 * j));
         }
-        local += nflag;
+        mo += NN;
 #pragma unroll
         for (int i = 0; i < 5; ++i) {
             a0[i] = b0[i];
@@ -333,10 +393,10 @@ __global__ void __launch_bounds__(256, 4) k_cores3_tiled(const typename Cplx<T>:
     // The cells within the float margin (written 0 above) take the exact
     // double decision here, where little else is live across the call.
 #pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
-        unsigned long long u = h ? unc1 : unc0;
+    for (int w = 0; w < kCZ / 8; ++w) {
+        unsigned u = unc[w][tid];
         while (u) {
-            const int b = __ffsll((long long)u) - 1 + 64 * h;
+            const int b = __ffs((int)u) - 1 + 32 * w;
             u &= u - 1;
             const int zz = z0 + (b >> 2), j = b & 3;
             if (cell3_exact<T, false>(cn, gx + j, gy, zz, N, accept)) {
@@ -346,7 +406,7 @@ __global__ void __launch_bounds__(256, 4) k_cores3_tiled(const typename Cplx<T>:
         }
     }
     for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
-    if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, (unsigned long long)local);
 }
 
 // ---- ordered compaction of the mask: chunk counts, scan, ordered write
@@ -490,7 +550,8 @@ static void launch_cores(Lattice *L, bool from_theta, double accept, unsigned lo
         if (from_theta) k_cores<T, 3, true><<<g, 256, 0, L->stream>>>(psi, L->dtheta, L->dmask, N, L->length, accept, cnt);
         else {
             dim3 grid((N + kCX - 1) / kCX, (N + kCY - 1) / kCY, (N + kCZ - 1) / kCZ);
-            k_cores3_tiled<T><<<grid, 256, 0, L->stream>>>(psi, L->dmask, N, accept, cnt);
+            if ((N & 3) == 0) k_cores3_tiled<T, true><<<grid, 256, 0, L->stream>>>(psi, L->dmask, N, accept, cnt);
+            else k_cores3_tiled<T, false><<<grid, 256, 0, L->stream>>>(psi, L->dmask, N, accept, cnt);
         }
     }
     AXS_CUDA(cudaGetLastError());

@@ -367,6 +367,7 @@ static void launch_r_t(const ZLat *d, int nlat, int64_t items, int *counters, in
 #define AXS_ZR_SHAPES(X) \
     X(8, 128, 6, 2)      \
     X(4, 128, 6, 2)      \
+    X(16, 64, 6, 2)      \
     X(8, 64, 8, 3)       \
     X(4, 128, 8, 3)      \
     X(4, 128, 10, 4)     \
