@@ -774,7 +774,8 @@ struct RefBinsI {
     static constexpr int kSmemTable = 0;
     __device__ __forceinline__ int bin(int n2) const {
         if (n2 == 0 || n2 >= half * half) return -1;
-        int s = (int)sqrtf((float)n2);
+        const float fn = (float)n2;
+        int s = (int)(fn * rsqrtf(fn));   // within 0.02 of sqrt(n2), as in ceil_isqrt
         while (s * s > n2) --s;
         while ((s + 1) * (s + 1) <= n2) ++s;
         return s - 1;
@@ -871,21 +872,28 @@ __device__ __forceinline__ FF mode_norm(int n2) {
     return FF{shi, (float)(rd - (double)shi)};
 }
 
-// The least s >= 0 with s^2 >= m (0 < m < 2^31).
+// The least s >= 0 with s^2 >= m (m < 2^31). The estimate m * rsqrt(m) is
+// within a few 1e-7 of sqrt(m) relatively (the approximate reciprocal square
+// root and the rounding of m to float), so within 0.02 of it for m < 2^31; the
+// corrections are exact in 32-bit unsigned arithmetic (s <= 46341).
 __device__ __forceinline__ int ceil_isqrt(int m) {
-    int s = (int)sqrtf((float)m);
-    while ((int64_t)s * s < m) ++s;
-    while (s > 0 && (int64_t)(s - 1) * (s - 1) >= m) --s;
-    return s;
+    if (m <= 0) return 0;
+    const float fm = (float)m;
+    unsigned s = (unsigned)(fm * rsqrtf(fm));
+    const unsigned um = (unsigned)m;
+    while (s * s < um) ++s;
+    while (s > 0 && (s - 1) * (s - 1) >= um) --s;
+    return (int)s;
 }
 
 // Weighted power of the modes ix in [a, e) of one bin's run, added to v:
 // weight 2 (the mode and its conjugate of the half spectrum), 1 for the row's
 // first (ix = 0) and last (ix = N/2 = nh - 1) mode. Summed in FP32 in blocks
 // of at most 16 modes (relative error below 16 ulp of a block's sum, all terms
-// being non-negative), even and odd modes in two chains to shorten the
-// dependent FMA sequence, each block added to v in float-float. s: the staged
-// row segment that starts at mode s0.
+// being non-negative), a full block of 16 unrolled in four chains (modes k
+// mod 4, then chains 0+2 and 1+3), a shorter one in two (even and odd modes),
+// each block added to v in float-float. s: the staged row segment that starts
+// at mode s0.
 __device__ __forceinline__ FF run_power(const float2 *s, int s0, int a, int e, int nh, FF v) {
     if (a == 0) {
         const float2 f = s[-s0];
@@ -896,15 +904,31 @@ __device__ __forceinline__ FF run_power(const float2 *s, int s0, int a, int e, i
     while (a < eh) {
         const int ce = min(eh, a + 16);
         float t0 = 0.f, t1 = 0.f;
-        for (; a + 1 < ce; a += 2) {
-            const float2 f = s[a - s0], g = s[a + 1 - s0];
-            t0 = fmaf(f.x, f.x, fmaf(f.y, f.y, t0));
-            t1 = fmaf(g.x, g.x, fmaf(g.y, g.y, t1));
-        }
-        if (a < ce) {
-            const float2 f = s[a - s0];
-            t0 = fmaf(f.x, f.x, fmaf(f.y, f.y, t0));
-            ++a;
+        if (ce - a == 16) {
+            const float2 *q = s + (a - s0);
+            float t2 = 0.f, t3 = 0.f;
+#pragma unroll
+            for (int k = 0; k < 16; k += 4) {
+                const float2 f0 = q[k], f1 = q[k + 1], f2 = q[k + 2], f3 = q[k + 3];
+                t0 = fmaf(f0.x, f0.x, fmaf(f0.y, f0.y, t0));
+                t1 = fmaf(f1.x, f1.x, fmaf(f1.y, f1.y, t1));
+                t2 = fmaf(f2.x, f2.x, fmaf(f2.y, f2.y, t2));
+                t3 = fmaf(f3.x, f3.x, fmaf(f3.y, f3.y, t3));
+            }
+            t0 += t2;
+            t1 += t3;
+            a = ce;
+        } else {
+            for (; a + 1 < ce; a += 2) {
+                const float2 f = s[a - s0], g = s[a + 1 - s0];
+                t0 = fmaf(f.x, f.x, fmaf(f.y, f.y, t0));
+                t1 = fmaf(g.x, g.x, fmaf(g.y, g.y, t1));
+            }
+            if (a < ce) {
+                const float2 f = s[a - s0];
+                t0 = fmaf(f.x, f.x, fmaf(f.y, f.y, t0));
+                ++a;
+            }
         }
         v = ff_add(v, FF{2.f * (t0 + t1), 0.f});
     }
@@ -1019,7 +1043,10 @@ __global__ void __launch_bounds__(128, 8) k_bin_runs(const typename Cplx<T>::typ
         if (!ok) break;
         const C *stage = stg + (size_t)cur * sbuf + unit_off(r, si);
         const int s0 = si * seg, sl = min(seg, nh - s0);
-        const int chunk = (sl + 31) / 32;
+        // Lane slices of an odd number of modes: lanes reading mode k of their
+        // slices at once are 2 * chunk words apart, which spreads them over the
+        // 32 banks (an even chunk such as 16 put every lane on one bank).
+        const int chunk = ((sl + 31) / 32) | 1;
         const int lo = s0 + min(sl, lane * chunk), hi = s0 + min(sl, lane * chunk + chunk);
         // |n|^2 = ix^2 + fy^2 (+ fz^2) <= 2 (N/2)^2 < 2^31 in 2D (N <= 32768), 3 (N/2)^2 in 3D (N <= 4096): int
         int c2;

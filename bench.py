@@ -267,11 +267,20 @@ def e2e_leg(axs, L, dist, steps):
         b.array[...] = a
     del f
 
+    split = {}
+
     def interval():
+        # upload, find_strings and download return after their stream has
+        # synchronised, so the split points cost no extra synchronisation
+        t = time.perf_counter()
         L.upload(*[b.array for b in ins], dtype=np.float32)
+        t1 = time.perf_counter()
         L.evolve(steps)
         n, _, _ = L.find_strings()
+        t2 = time.perf_counter()
         axs._check(axs._lib.axs_download_f32(L._h, outs[0].array.ctypes.data, outs[1].array.ctypes.data, None, None))
+        t3 = time.perf_counter()
+        split.update(upload_s=t1 - t, evolve_and_strings_s=t2 - t1, download_s=t3 - t2)
         return n
 
     for _ in range(2):
@@ -288,7 +297,9 @@ def e2e_leg(axs, L, dist, steps):
     h2d = 4 * 4 * sites
     d2h = 2 * 4 * sites + 16
     return {"wall_s": wall, "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
-            "string_count": int(n), "site_updates_per_s": sites * steps / wall}
+            "string_count": int(n), "site_updates_per_s": sites * steps / wall,
+            "split_s": {k: round(v, 6) for k, v in split.items()},
+            "h2d_gbs": h2d / split["upload_s"] / 1e9, "d2h_gbs": d2h / split["download_s"] / 1e9}
 
 
 def ensemble_shard(n_total, rank, world):
@@ -414,7 +425,8 @@ def gpu_arm(args, dist):
         e2e_line = {"value": sites_all * E2E_STEPS / e2e["wall_s"],      # wall_s is already the max over ranks
                     "unit": "site-updates/s", "h2d_bytes_per_step": e2e["h2d_bytes_per_step"],
                     "d2h_bytes_per_step": e2e["d2h_bytes_per_step"], "wall_s": e2e["wall_s"],
-                    "steps": E2E_STEPS}
+                    "steps": E2E_STEPS, "split_s": e2e["split_s"],   # rank 0's upload / evolve + strings / download
+                    "h2d_gbs": e2e["h2d_gbs"], "d2h_gbs": e2e["d2h_gbs"]}
     if dist.rank != 0:
         return
     # state held on the device: two psi buffers, pi and the spare (complex)

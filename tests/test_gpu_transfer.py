@@ -45,6 +45,31 @@ def test_round_trip_page_locked(axs, precision):
         o.free()
 
 
+@pytest.mark.parametrize("precision", [32, 64])
+def test_round_trip_page_locked_unaligned(axs, precision):
+    """Page-locked arrays that start off a 16-byte boundary take the packing
+    kernels' one-site-per-thread form instead of the 16-byte one."""
+    N = 32
+    n = N ** 3
+    p = params(axs, 3, N, precision)
+    dt = np.float32 if precision == 32 else np.float64
+    bufs = [axs.PinnedBuffer((n + 1,), dt) for _ in range(4)]
+    outs = [axs.PinnedBuffer((n + 1,), dt) for _ in range(4)]
+    ins = [b.array[1:] for b in bufs]
+    got = [o.array[1:] for o in outs]
+    rng = np.random.default_rng(9)
+    for v in ins:
+        v[...] = rng.standard_normal(n)
+    with axs.Lattice(p) as L:
+        L.upload(*ins, dtype=dt)
+        fn = axs._lib.axs_download_f32 if precision == 32 else axs._lib.axs_download
+        axs._check(fn(L._h, *[v.ctypes.data for v in got]))
+    for v, o in zip(ins, got):
+        assert np.array_equal(v, o)
+    for b in bufs + outs:
+        b.free()
+
+
 def test_single_field_transfers(axs):
     N = 32
     p = params(axs, 3, N, 64)
