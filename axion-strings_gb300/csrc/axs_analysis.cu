@@ -997,9 +997,16 @@ __global__ void __launch_bounds__(128, 8) k_bin_runs(const typename Cplx<T>::typ
     double *hk = hp + nbp;
     double *hc = hk + nbp;
     auto in_pass = [&](int bb) { return bb >= b0 && bb < b1; };
-    const int64_t rows = ndims == 2 ? (int64_t)N : (int64_t)N * N;
-    const int64_t units = rows * nseg;
-    const int64_t nwarps = (int64_t)gridDim.x * 4;
+    // A unit is (group, segment si). A group holds the rows whose frequencies
+    // are (+-gz, +-gy), gz and gy in 0 .. N/2 (2D: +-gy): up to four rows with
+    // the same c = fy^2 + fz^2, hence the same bin at every x. A lane's slice
+    // has the same runs in each of them, so its first and last runs are summed
+    // over the group's rows in registers, and the segmented scan and the
+    // histogram updates run once per group instead of once per row. There are
+    // (N/2 + 1)^2 nseg < 2^31 units (3D N <= 4096; 2D far fewer): int.
+    const int gh = N / 2 + 1;
+    const int units = (ndims == 3 ? gh * gh : gh) * nseg;
+    const int nwarps = gridDim.x * 4;
     // The mode offset of unit uu's copy below its first mode (FP32 modes are 8
     // bytes; the array and every row-segment copy start on 16 bytes), and the
     // copy itself (lane 0). The copy ends on 16 bytes too: at most one mode
@@ -1016,69 +1023,132 @@ __global__ void __launch_bounds__(128, 8) k_bin_runs(const typename Cplx<T>::typ
         mbar_expect_tx(smem_u32(&bars[buf]), bytes);
         bulk_load(smem_u32(stg + (size_t)buf * sbuf), F + (int64_t)rr * nh + ss0 - off, bytes, smem_u32(&bars[buf]));
     };
-    // A unit is (row r, segment si); in 3D row r = iz N + iy (rows < N^2 <=
-    // 2^24). A warp advances nwarps units at a time: dr rows and ds segments,
-    // carried incrementally, so no unit costs a 64-bit division.
-    const int64_t ufirst = (int64_t)blockIdx.x * 4 + w;
-    const int dr = (int)(nwarps / nseg), ds = (int)(nwarps - (int64_t)dr * nseg);
-    const int dz = ndims == 3 ? dr / N : 0, dy = ndims == 3 ? dr - dz * N : 0;
-    int r = (int)(ufirst / nseg), si = (int)(ufirst - (int64_t)r * nseg);
-    int iz = ndims == 3 ? r / N : 0, iy = ndims == 3 ? r - iz * N : 0;
-    if (lane == 0 && ufirst < units) issue(r, si, 0);
-    int it = 0;
+    struct Unit {
+        int gz, gy, si, ny, cnt;   // ny: 1 or 2 values of y; cnt: rows in the group
+    };
+    auto unit_at = [&](int uu) {
+        const int g = uu / nseg;
+        Unit q;
+        q.si = uu - g * nseg;
+        q.gz = ndims == 3 ? g / gh : 0;
+        q.gy = ndims == 3 ? g - q.gz * gh : g;
+        q.ny = (q.gy == 0 || 2 * q.gy == N) ? 1 : 2;
+        q.cnt = q.ny * ((ndims == 2 || q.gz == 0 || 2 * q.gz == N) ? 1 : 2);
+        return q;
+    };
+    // row m of a group: y = gy, then N - gy; z = gz, then N - gz
+    auto row_of = [&](const Unit &q, int m) {
+        const int jz = m >= q.ny ? 1 : 0, jy = m - jz * q.ny;
+        const int iy = jy ? N - q.gy : q.gy;
+        return ndims == 2 ? iy : (jz ? N - q.gz : q.gz) * N + iy;
+    };
+    const int ufirst = blockIdx.x * 4 + w;
+    if (lane == 0 && ufirst < units) {
+        const Unit q0 = unit_at(ufirst);
+        issue(row_of(q0, 0), q0.si, 0);
+    }
+    int it = 0;            // row copies taken by this warp: buffer it & 1, phase (it >> 1) & 1
     bool ok = true;
-    int64_t u = ufirst;
-    for (; u < units; u += nwarps, ++it) {
-        const int cur = it & 1;
-        // the next unit's position (a carry from the segments into the rows, and
-        // in 3D from y into z; dy + 1 < 2N, so one wrap suffices)
-        int si_n = si + ds, carry = 0;
-        if (si_n >= nseg) { si_n -= nseg; carry = 1; }
-        const int r_n = r + dr + carry;
-        int iy_n = iy + dy + carry, iz_n = iz + dz;
-        if (iy_n >= N) { iy_n -= N; ++iz_n; }
-        __syncwarp();   // every lane is done with the other buffer (the previous unit)
-        if (lane == 0 && u + nwarps < units) issue(r_n, si_n, cur ^ 1);
-        ok = __all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[cur]), (uint32_t)((it >> 1) & 1)));
-        if (!ok) break;
-        const C *stage = stg + (size_t)cur * sbuf + unit_off(r, si);
-        const int s0 = si * seg, sl = min(seg, nh - s0);
+    bool more = false;     // a copy after the current one is in flight
+    for (int u = ufirst; u < units; u += nwarps) {
+        const Unit q = unit_at(u);
+        const int s0 = q.si * seg, sl = min(seg, nh - s0);
         // Lane slices of an odd number of modes: lanes reading mode k of their
         // slices at once are 2 * chunk words apart, which spreads them over the
         // 32 banks (an even chunk such as 16 put every lane on one bank).
         const int chunk = ((sl + 31) / 32) | 1;
         const int lo = s0 + min(sl, lane * chunk), hi = s0 + min(sl, lane * chunk + chunk);
         // |n|^2 = ix^2 + fy^2 (+ fz^2) <= 2 (N/2)^2 < 2^31 in 2D (N <= 32768), 3 (N/2)^2 in 3D (N <= 4096): int
-        int c2;
-        if (ndims == 2) {
-            const int fy = r < N / 2 ? r : r - N;
-            c2 = fy * fy;
-        } else {
-            const int fz = iz < N / 2 ? iz : iz - N, fy = iy < N / 2 ? iy : iy - N;
-            c2 = fy * fy + fz * fz;
-        }
-        r = r_n;   // the rest of the body uses s0, sl, lo, hi and c2
-        si = si_n;
-        iz = iz_n;
-        iy = iy_n;
-        int b = -1, fb = -1, lb = -1;
-        int up = 0;          // the bin is looked up again once n2 reaches this
-        bool inp = false;    // in_pass(b)
-        FF v{0.f, 0.f}, kk{0.f, 0.f}, fv{0.f, 0.f}, fk{0.f, 0.f};
-        int c = 0, fc = 0;
-        if constexpr (kRuns) {
-            // FP32: jump from run to run. A run ends where n2 reaches `up`, at
-            // ix = ceil(sqrt(up - c2)); its power is summed by run_power, so a
-            // binning's first call (KS: also |n| and the mode count, per mode)
-            // and its later calls give the same power sums.
-            for (int ix = lo; ix < hi;) {
+        const int c2 = q.gy * q.gy + q.gz * q.gz;
+        int fb = -1, lb = -1;   // the slice's first and last runs' bins, the same in every row of the group
+        FF fv{0.f, 0.f}, fk{0.f, 0.f}, lv{0.f, 0.f}, lk{0.f, 0.f};
+        int fc = 0, lc = 0;
+        for (int m = 0; m < q.cnt; ++m, ++it) {
+            const int cur = it & 1;
+            __syncwarp();   // every lane is done with the other buffer (the previous row)
+            more = m + 1 < q.cnt || u + nwarps < units;
+            if (lane == 0 && more) {
+                if (m + 1 < q.cnt) {
+                    issue(row_of(q, m + 1), q.si, cur ^ 1);
+                } else {
+                    const Unit qn = unit_at(u + nwarps);
+                    issue(row_of(qn, 0), qn.si, cur ^ 1);
+                }
+            }
+            ok = __all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[cur]), (uint32_t)((it >> 1) & 1)));
+            if (!ok) break;
+            const C *stage = stg + (size_t)cur * sbuf + unit_off(row_of(q, m), q.si);
+            int b = -1;
+            int up = 0;          // the bin is looked up again once n2 reaches this
+            bool inp = false;    // in_pass(b)
+            bool first = true;   // no run of this row has ended yet
+            FF v{0.f, 0.f}, kk{0.f, 0.f};
+            int c = 0;
+            if constexpr (kRuns) {
+                // FP32: jump from run to run. A run ends where n2 reaches `up`, at
+                // ix = ceil(sqrt(up - c2)); its power is summed by run_power, so a
+                // binning's first call (KS: also |n| and the mode count, per mode)
+                // and its later calls give the same power sums.
+                for (int ix = lo; ix < hi;) {
+                    const int n2 = ix * ix + c2;
+                    if (n2 >= up) {
+                        const int nb = bins.next(b, n2);
+                        up = bins.upper(nb, n2);
+                        if (b >= 0) {   // nb != b: n2 reached the bound of b's run
+                            if (first) {   // the row's first run: summed over the group's rows
+                                fb = b;
+                                fv = ff_add(fv, v);
+                                if constexpr (KS) {
+                                    fk = ff_add(fk, kk);
+                                    fc += c;
+                                }
+                                first = false;
+                            } else if (in_pass(b)) {   // a run inside the slice
+                                ff_acc(hp + (b - b0), v);
+                                if constexpr (KS) {
+                                    ff_acc(hk + (b - b0), kk);
+                                    ff_acc(hc + (b - b0), FF{(float)c, 0.f});
+                                }
+                            }
+                        }
+                        b = nb;
+                        v = kk = FF{0.f, 0.f};
+                        c = 0;
+                    }
+                    const int e = up == INT_MAX ? hi : min(hi, ceil_isqrt(up - c2));
+                    if (b >= 0 && in_pass(b)) {
+                        v = run_power(reinterpret_cast<const float2 *>(stage), s0, ix, e, nh, v);
+                        // the |n| sums and mode counts are the same in every row of
+                        // the group: the first row's, times the rows (1, 2 or 4: exact)
+                        if constexpr (KS)
+                            if (m == 0)
+                                for (int a = ix; a < e; ++a) {
+                                    const int wt = ((a == 0 || 2 * a == N) ? 1 : 2) * q.cnt;
+                                    kk = ff_add(kk, ff_scale(mode_norm(a * a + c2), (float)wt));
+                                    c += wt;
+                                }
+                    }
+                    ix = e;
+                }
+            } else
+            for (int ix = lo; ix < hi; ++ix) {
                 const int n2 = ix * ix + c2;
+                int nb = b;
                 if (n2 >= up) {
-                    const int nb = bins.next(b, n2);
+                    nb = bins.next(b, n2);
                     up = bins.upper(nb, n2);
-                    if (b >= 0) {   // nb != b: n2 reached the bound of b's run
-                        if (fb < 0) { fb = b; fv = v; fk = kk; fc = c; }
-                        else if (in_pass(b)) {   // a run inside the slice
+                }
+                if (nb != b) {
+                    if (b >= 0) {
+                        if (first) {
+                            fb = b;
+                            fv = ff_add(fv, v);
+                            if constexpr (KS) {
+                                fk = ff_add(fk, kk);
+                                fc += c;
+                            }
+                            first = false;
+                        } else if (in_pass(b)) {   // a run inside the slice: no other lane has this bin in this segment
                             ff_acc(hp + (b - b0), v);
                             if constexpr (KS) {
                                 ff_acc(hk + (b - b0), kk);
@@ -1087,63 +1157,43 @@ __global__ void __launch_bounds__(128, 8) k_bin_runs(const typename Cplx<T>::typ
                         }
                     }
                     b = nb;
+                    inp = in_pass(b);
                     v = kk = FF{0.f, 0.f};
                     c = 0;
                 }
-                const int e = up == INT_MAX ? hi : min(hi, ceil_isqrt(up - c2));
-                if (b >= 0 && in_pass(b)) {
-                    v = run_power(reinterpret_cast<const float2 *>(stage), s0, ix, e, nh, v);
-                    if constexpr (KS)
-                        for (int a = ix; a < e; ++a) {
-                            const int wt = (a == 0 || 2 * a == N) ? 1 : 2;
-                            kk = ff_add(kk, ff_scale(mode_norm(a * a + c2), (float)wt));
-                            c += wt;
-                        }
-                }
-                ix = e;
-            }
-        } else
-        for (int ix = lo; ix < hi; ++ix) {
-            const int n2 = ix * ix + c2;
-            int nb = b;
-            if (n2 >= up) {
-                nb = bins.next(b, n2);
-                up = bins.upper(nb, n2);
-            }
-            if (nb != b) {
-                if (b >= 0) {
-                    if (fb < 0) { fb = b; fv = v; fk = kk; fc = c; }
-                    else if (in_pass(b)) {   // a run inside the slice: no other lane has this bin in this segment
-                        ff_acc(hp + (b - b0), v);
-                        if constexpr (KS) {
-                            ff_acc(hk + (b - b0), kk);
-                            ff_acc(hc + (b - b0), FF{(float)c, 0.f});
+                if (inp) {
+                    const int wt = (ix == 0 || 2 * ix == N) ? 1 : 2;
+                    const float fw = (float)wt;   // x1 or x2: exact in float-float
+                    const FF p = mode_power<T>(stage[ix - s0]);
+                    v = ff_add(v, FF{fw * p.hi, fw * p.lo});
+                    if constexpr (KS) {
+                        if (m == 0) {   // as above: the first row's |n| and count, times the rows
+                            kk = ff_add(kk, ff_scale(mode_norm(n2), fw * (float)q.cnt));
+                            c += wt * q.cnt;
                         }
                     }
                 }
-                b = nb;
-                inp = in_pass(b);
-                v = kk = FF{0.f, 0.f};
-                c = 0;
             }
-            if (inp) {
-                const int wt = (ix == 0 || 2 * ix == N) ? 1 : 2;
-                const float fw = (float)wt;   // x1 or x2: exact in float-float
-                const FF p = mode_power<T>(stage[ix - s0]);
-                v = ff_add(v, FF{fw * p.hi, fw * p.lo});
-                if constexpr (KS) {
-                    kk = ff_add(kk, ff_scale(mode_norm(n2), fw));
-                    c += wt;
+            if (b >= 0) {   // the open run: the row's first if none ended, else the slice's last
+                if (first) {
+                    fb = b;
+                    fv = ff_add(fv, v);
+                    if constexpr (KS) {
+                        fk = ff_add(fk, kk);
+                        fc += c;
+                    }
+                } else {
+                    lb = b;
+                    lv = ff_add(lv, v);
+                    if constexpr (KS) {
+                        lk = ff_add(lk, kk);
+                        lc += c;
+                    }
                 }
             }
         }
-        FF lv{0.f, 0.f}, lk{0.f, 0.f};
-        int lc = 0;
-        if (b >= 0) {   // the open run: the lane's first if it has none yet, else its last
-            if (fb < 0) { fb = b; fv = v; fk = kk; fc = c; }
-            else { lb = b; lv = v; lk = kk; lc = c; }
-        }
-        __syncwarp();   // inside runs are in; the staged row is no longer read
+        if (!ok) break;
+        __syncwarp();   // inside runs are in; the staged rows are no longer read
         // first runs: inclusive segmented scan over lanes with equal bins
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -1185,7 +1235,7 @@ __global__ void __launch_bounds__(128, 8) k_bin_runs(const typename Cplx<T>::typ
         if (lane == 0) {
             atomicOr(derr, DEVERR_TIMEOUT);
             mbar_wait_bounded(smem_u32(&bars[it & 1]), (uint32_t)((it >> 1) & 1));
-            if (u + nwarps < units) mbar_wait_bounded(smem_u32(&bars[(it + 1) & 1]), (uint32_t)(((it + 1) >> 1) & 1));
+            if (more) mbar_wait_bounded(smem_u32(&bars[(it + 1) & 1]), (uint32_t)(((it + 1) >> 1) & 1));
         }
         __syncwarp();
     }
@@ -1353,9 +1403,11 @@ static BinPending bin_spectrum_enqueue(Lattice *L, const B &binner, int kind, co
     // as many 4-warp blocks as fit on the SMs (up to 16 per SM): the per-warp
     // histograms leave this kernel latency-bound at low occupancy
     int per_sm = (int)std::max<size_t>(1, std::min<size_t>(16, (size_t)(200 * 1024) / std::max<size_t>(sm, 1)));
-    const int64_t rows = L->p.NDIMS == 2 ? (int64_t)N : (int64_t)N * N;
-    const int64_t units = rows * ((nh + seg - 1) / seg);
-    int nblk = (int)std::min<int64_t>((int64_t)num_sms() * per_sm, (units + 3) / 4);   // whole segments per warp
+    // k_bin_runs' units: groups of up to four rows (+-gz, +-gy) times segments
+    const int64_t groups = L->p.NDIMS == 2 ? (int64_t)nh : (int64_t)nh * nh;
+    const int64_t units = groups * ((nh + seg - 1) / seg);
+    if (units >= ((int64_t)1 << 31)) fail(AXS_ERR_ARG, "spectrum of N = %d: too many row groups", N);
+    int nblk = (int)std::min<int64_t>((int64_t)num_sms() * per_sm, (units + 3) / 4);   // whole units per warp
     double *part = (double *)lattice_tmp(L, 1, (size_t)nblk * 3 * nbp * sizeof(double) + (size_t)3 * nbp * sizeof(double));
     double *out = part + (size_t)nblk * 3 * nbp;
     auto kern = L->esz == 4 ? (ks ? (const void *)k_bin_runs<float, B, true> : (const void *)k_bin_runs<float, B, false>)
