@@ -956,10 +956,12 @@ template <> __device__ __forceinline__ FF mode_power<double>(const double2 &f) {
 // one segmented scan of 5 shuffle steps), and its last run has a bin no other
 // lane's last run has. Every bin thus receives its sums in an order fixed by
 // the data: results are the same run to run and for an ensemble member alone.
+// Rows are taken in groups that share every bin boundary (see the unit loop).
 // Per-warp histograms (float-float slots), block partial rows in double and
-// k_bin_final3 as before (three rows: power, |n|, count). With KS false only the power row is summed (the
-// |n| and count rows, which depend on N and the bin edges alone, stay zero;
-// the power sums are the same bits either way).
+// k_bin_final3 (three rows: power, |n|, count). With KS false only the power
+// row is summed and held (the |n| and count rows, which depend on N and the
+// bin edges alone, come out zero; the power sums are the same bits either
+// way: the host gives both kinds of call the same segments, passes and grid).
 // Large spectra run in pieces that fit shared memory: a row of the half
 // spectrum is taken in segments of `seg` modes (each segment is binned like a
 // row: bins still only grow along it), and the bins in passes of `nbp`, this
@@ -971,21 +973,22 @@ __global__ void __launch_bounds__(128, 8) k_bin_runs(const typename Cplx<T>::typ
                                                   double *__restrict__ partials, int *derr) {
     typedef typename Cplx<T>::type C;
     constexpr bool kRuns = sizeof(T) == 4;   // FP32 modes: whole runs per bin lookup
-    // [4 warps][3][nbp] histograms, bin table, [4 warps][2][sbuf] staging buffers, [4 warps][2] mbarriers
+    // [4 warps][HR][nbp] histograms, bin table, [4 warps][2][sbuf] staging buffers, [4 warps][2] mbarriers
     extern __shared__ double hist[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nh = N / 2 + 1;
     const int nseg = (nh + seg - 1) / seg;
     const int b1 = b0 + nbp;
-    for (int i = threadIdx.x; i < 4 * 3 * nbp; i += blockDim.x) hist[i] = 0.0;
-    const B bins = binner.staged(hist + 4 * 3 * nbp);
+    constexpr int HR = KS ? 3 : 1;   // histogram rows: power (and |n|, count on a binning's first call)
+    for (int i = threadIdx.x; i < 4 * HR * nbp; i += blockDim.x) hist[i] = 0.0;
+    const B bins = binner.staged(hist + 4 * HR * nbp);
     // Row segments arrive by bulk copies into two staging buffers per warp: the
     // next unit's copy is in flight while this one is binned. A buffer holds a
     // segment and up to one mode either side (the copy starts and ends on 16
     // bytes); buffers start 16-byte aligned, the warp's two mbarriers follow.
     const int sbuf = (seg + 3) & ~1;
-    C *stg = reinterpret_cast<C *>(hist + ((4 * 3 * nbp + B::kSmemTable * nbins + 1) & ~1)) + (size_t)w * 2 * sbuf;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(reinterpret_cast<C *>(hist + ((4 * 3 * nbp + B::kSmemTable * nbins + 1) & ~1)) +
+    C *stg = reinterpret_cast<C *>(hist + ((4 * HR * nbp + B::kSmemTable * nbins + 1) & ~1)) + (size_t)w * 2 * sbuf;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(reinterpret_cast<C *>(hist + ((4 * HR * nbp + B::kSmemTable * nbins + 1) & ~1)) +
                                                   (size_t)4 * 2 * sbuf) + 2 * w;
     if (lane == 0) {
         mbar_init(smem_u32(&bars[0]), 1);
@@ -993,7 +996,7 @@ __global__ void __launch_bounds__(128, 8) k_bin_runs(const typename Cplx<T>::typ
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    double *hp = hist + (size_t)w * 3 * nbp;   // indexed by bin - b0
+    double *hp = hist + (size_t)w * HR * nbp;   // indexed by bin - b0
     double *hk = hp + nbp;
     double *hc = hk + nbp;
     auto in_pass = [&](int bb) { return bb >= b0 && bb < b1; };
@@ -1061,6 +1064,7 @@ __global__ void __launch_bounds__(128, 8) k_bin_runs(const typename Cplx<T>::typ
         // |n|^2 = ix^2 + fy^2 (+ fz^2) <= 2 (N/2)^2 < 2^31 in 2D (N <= 32768), 3 (N/2)^2 in 3D (N <= 4096): int
         const int c2 = q.gy * q.gy + q.gz * q.gz;
         int fb = -1, lb = -1;   // the slice's first and last runs' bins, the same in every row of the group
+        int nr = 0, r1b = -1, r1e = 0, r2b = -1;   // FP32: the slice's runs in the group's first row (count, bins, first end)
         FF fv{0.f, 0.f}, fk{0.f, 0.f}, lv{0.f, 0.f}, lk{0.f, 0.f};
         int fc = 0, lc = 0;
         for (int m = 0; m < q.cnt; ++m, ++it) {
@@ -1084,40 +1088,68 @@ __global__ void __launch_bounds__(128, 8) k_bin_runs(const typename Cplx<T>::typ
             bool first = true;   // no run of this row has ended yet
             FF v{0.f, 0.f}, kk{0.f, 0.f};
             int c = 0;
+            // a run of bin b ended inside the slice: the row's first (summed over
+            // the group's rows), or one strictly inside, straight to the histogram
+            auto close_run = [&]() {
+                if (b < 0) return;
+                if (first) {
+                    fb = b;
+                    fv = ff_add(fv, v);
+                    if constexpr (KS) {
+                        fk = ff_add(fk, kk);
+                        fc += c;
+                    }
+                    first = false;
+                } else if (in_pass(b)) {
+                    ff_acc(hp + (b - b0), v);
+                    if constexpr (KS) {
+                        ff_acc(hk + (b - b0), kk);
+                        ff_acc(hc + (b - b0), FF{(float)c, 0.f});
+                    }
+                }
+            };
             if constexpr (kRuns) {
                 // FP32: jump from run to run. A run ends where n2 reaches `up`, at
                 // ix = ceil(sqrt(up - c2)); its power is summed by run_power, so a
                 // binning's first call (KS: also |n| and the mode count, per mode)
-                // and its later calls give the same power sums.
+                // and its later calls give the same power sums. The group's later
+                // rows have the first row's runs: a slice of one or two runs
+                // replays them without the bin lookups.
+                const float2 *sf = reinterpret_cast<const float2 *>(stage);
+                if (m > 0 && nr <= 2) {
+                    if (nr > 0) {
+                        b = r1b;
+                        if (b >= 0 && in_pass(b)) v = run_power(sf, s0, lo, r1e, nh, v);
+                    }
+                    if (nr == 2) {
+                        close_run();
+                        b = r2b;
+                        v = FF{0.f, 0.f};
+                        if (b >= 0 && in_pass(b)) v = run_power(sf, s0, r1e, hi, nh, v);
+                    }
+                } else
                 for (int ix = lo; ix < hi;) {
                     const int n2 = ix * ix + c2;
-                    if (n2 >= up) {
+                    if (n2 >= up) {   // every pass but the first: n2 reached the bound of b's run
                         const int nb = bins.next(b, n2);
                         up = bins.upper(nb, n2);
-                        if (b >= 0) {   // nb != b: n2 reached the bound of b's run
-                            if (first) {   // the row's first run: summed over the group's rows
-                                fb = b;
-                                fv = ff_add(fv, v);
-                                if constexpr (KS) {
-                                    fk = ff_add(fk, kk);
-                                    fc += c;
-                                }
-                                first = false;
-                            } else if (in_pass(b)) {   // a run inside the slice
-                                ff_acc(hp + (b - b0), v);
-                                if constexpr (KS) {
-                                    ff_acc(hk + (b - b0), kk);
-                                    ff_acc(hc + (b - b0), FF{(float)c, 0.f});
-                                }
-                            }
-                        }
+                        close_run();
                         b = nb;
                         v = kk = FF{0.f, 0.f};
                         c = 0;
                     }
                     const int e = up == INT_MAX ? hi : min(hi, ceil_isqrt(up - c2));
+                    if (m == 0) {   // the slice's runs, for the group's later rows
+                        if (nr == 0) {
+                            r1b = b;
+                            r1e = e;
+                        } else if (nr == 1) {
+                            r2b = b;
+                        }
+                        ++nr;
+                    }
                     if (b >= 0 && in_pass(b)) {
-                        v = run_power(reinterpret_cast<const float2 *>(stage), s0, ix, e, nh, v);
+                        v = run_power(sf, s0, ix, e, nh, v);
                         // the |n| sums and mode counts are the same in every row of
                         // the group: the first row's, times the rows (1, 2 or 4: exact)
                         if constexpr (KS)
@@ -1139,23 +1171,7 @@ __global__ void __launch_bounds__(128, 8) k_bin_runs(const typename Cplx<T>::typ
                     up = bins.upper(nb, n2);
                 }
                 if (nb != b) {
-                    if (b >= 0) {
-                        if (first) {
-                            fb = b;
-                            fv = ff_add(fv, v);
-                            if constexpr (KS) {
-                                fk = ff_add(fk, kk);
-                                fc += c;
-                            }
-                            first = false;
-                        } else if (in_pass(b)) {   // a run inside the slice: no other lane has this bin in this segment
-                            ff_acc(hp + (b - b0), v);
-                            if constexpr (KS) {
-                                ff_acc(hk + (b - b0), kk);
-                                ff_acc(hc + (b - b0), FF{(float)c, 0.f});
-                            }
-                        }
-                    }
+                    close_run();
                     b = nb;
                     inp = in_pass(b);
                     v = kk = FF{0.f, 0.f};
@@ -1244,8 +1260,8 @@ __global__ void __launch_bounds__(128, 8) k_bin_runs(const typename Cplx<T>::typ
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             double acc = 0.0;
-            for (int ww = 0; ww < 4; ++ww) {
-                const float2 h = reinterpret_cast<const float2 *>(hist)[(size_t)ww * 3 * nbp + (size_t)q * nbp + bn];
+            for (int ww = 0; ww < 4 && q < HR; ++ww) {
+                const float2 h = reinterpret_cast<const float2 *>(hist)[(size_t)ww * HR * nbp + (size_t)q * nbp + bn];
                 acc += (double)h.x + (double)h.y;
             }
             partials[((int64_t)blockIdx.x * 3 + q) * nbp + bn] = acc;
@@ -1383,26 +1399,33 @@ static BinPending bin_spectrum_enqueue(Lattice *L, const B &binner, int kind, co
     const bool ks = geom == nullptr;
     const int N = L->p.N;
     const int nh = N / 2 + 1;
-    // shared memory of one block: 4 warp histograms of nbp bins x 3 rows, the
-    // bin table, two staging buffers of a segment of seg modes per warp. Whole
-    // rows and every bin in one pass when they fit (up to N ~ 1500); else
-    // segments of 2048 modes, then passes over the bins.
-    auto smem_of = [&](int nbp, int seg) {   // k_bin_runs' layout: histograms, table, 4 x 2 buffers, 8 mbarriers
-        return (size_t)((4 * 3 * nbp + B::kSmemTable * nbins + 1) & ~1) * sizeof(double) +
+    // shared memory of one block: 4 warp histograms of nbp bins x 3 rows (1 row
+    // when only the power is summed), the bin table, two staging buffers of a
+    // segment of seg modes per warp. Whole rows and every bin in one pass when
+    // they fit (up to N ~ 1500); else segments of 2048 modes, then passes over
+    // the bins.
+    // k_bin_runs' layout: histograms (hr rows), table, 4 x 2 buffers, 8 mbarriers
+    auto smem_of = [&](int nbp, int seg, int hr) {
+        return (size_t)((4 * hr * nbp + B::kSmemTable * nbins + 1) & ~1) * sizeof(double) +
                (size_t)4 * 2 * ((seg + 3) & ~1) * 2 * L->esz + 8 * sizeof(uint64_t);
     };
+    // The segments, the bin passes and the grid fix which modes each lane and
+    // each warp sums, hence the bits: they follow from the first call's layout
+    // (three histogram rows) for every call, so later calls (one row) give the
+    // first call's power sums exactly.
     const size_t cap = 200 * 1024;
     int nbp = nbins, seg = nh;
-    while (smem_of(nbp, seg) > cap) {
+    while (smem_of(nbp, seg, 3) > cap) {
         if (seg > 2048) seg = 2048;
         else if (nbp > 512) nbp = (nbp + 1) / 2;
         else if (seg > 256) seg /= 2;
         else fail(AXS_ERR_ARG, "spectrum binning with %d bins does not fit shared memory", nbins);
     }
-    const size_t sm = smem_of(nbp, seg);
-    // as many 4-warp blocks as fit on the SMs (up to 16 per SM): the per-warp
-    // histograms leave this kernel latency-bound at low occupancy
-    int per_sm = (int)std::max<size_t>(1, std::min<size_t>(16, (size_t)(200 * 1024) / std::max<size_t>(sm, 1)));
+    const size_t sm = smem_of(nbp, seg, ks ? 3 : 1);
+    // as many 4-warp blocks as the later calls' layout fits on the SMs (up to 16
+    // per SM): the per-warp histograms leave this kernel latency-bound at low
+    // occupancy; the first call runs the same grid in more waves
+    int per_sm = (int)std::max<size_t>(1, std::min<size_t>(16, cap / std::max<size_t>(smem_of(nbp, seg, 1), 1)));
     // k_bin_runs' units: groups of up to four rows (+-gz, +-gy) times segments
     const int64_t groups = L->p.NDIMS == 2 ? (int64_t)nh : (int64_t)nh * nh;
     const int64_t units = groups * ((nh + seg - 1) / seg);
