@@ -1332,6 +1332,10 @@ static const ZVariant kZVariants[] = {
     // instead of per 4 or 8; 6.25 against 6.79 ms/step for variant 21 at 1024^3;
     // 8 x 64 tiles measured 7.07)
     {4, 16, 64, 6, 8, -1, 2},
+    // 42-45: the z-neighbours in registers with deeper rings: a register ring
+    // holds the R + 1 planes still to be centres, so S = R + 2 keeps one plane
+    // load in flight per CTA; these keep three (radius 2: two), at two CTAs per SM
+    {4, 4, 128, 7, 8, -1, 3},  {4, 8, 64, 7, 8, -1, 3},  {4, 8, 64, 8, 8, -1, 4},  {4, 4, 128, 5, 8, -1, 2},
 };
 static const int kNumZVariants = sizeof(kZVariants) / sizeof(kZVariants[0]);
 

@@ -380,7 +380,11 @@ static void launch_r_t(const ZLat *d, int nlat, int64_t items, int *counters, in
     X(4, 128, 5, 3)        \
     X(8, 64, 5, 3)         \
     X(4, 128, 6, 4)        \
-    X(8, 64, 6, 4)
+    X(8, 64, 6, 4)         \
+    X(4, 128, 7, 3)        \
+    X(8, 64, 7, 3)         \
+    X(8, 64, 8, 4)         \
+    X(4, 128, 5, 2)
 
 void launch_zmarch_r(int esz, int ty, int txmax, int slots, int r, const ZLat *d, int nlat, int64_t items,
                      int *counters, int parity, int *derr, cudaStream_t st, int ctas_per_sm) {
