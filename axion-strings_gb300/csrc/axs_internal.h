@@ -65,6 +65,12 @@ struct ZLat {
     CUtensorMap t2_str2[2];  // box {16-byte halo, 2, 1} over psi[b]
     CUtensorMap t2_prow[2];  // box {tx, 1, 1} over pih[b]
     CUtensorMap t2_pstr[2];  // box {16-byte halo, TY, 1} over pih[b]
+    // three-step (halo depth 3) kernel only
+    CUtensorMap t3_row3[2];  // box {tx, 3, 1} over psi[b]
+    CUtensorMap t3_strm[2];  // box {4 sites, TY, 1} over psi[b]
+    CUtensorMap t3_str2[2];  // box {4 sites, 2, 1} over psi[b]
+    CUtensorMap t3_prow2[2]; // box {tx, 2, 1} over pih[b]
+    CUtensorMap t3_pst1[2];  // box {16-byte halo, 1, 1} over pih[b]
     void *psi[2];
     // pih[b]: the half-step momentum that goes with psi[b] as current field.
     // A launch reads pih[bin] and writes pih[bin ^ 1]; both are the same

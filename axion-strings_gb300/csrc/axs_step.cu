@@ -1275,6 +1275,523 @@ static void (*zm3_kernel())(const ZLat *, int, int64_t, int *, int, int *) {
     else return k_zmarch_2step<TY, TXMAX, S, NCW, UNR>;
 }
 
+// ============================================================== three steps per pass
+//
+// Three leapfrog steps per pass (halo depth 3), complex float, x-tiled
+// lattices (tx < N). A work item is a tx x TY tile marching a z-chunk, as in
+// the two-step kernel. Per plane m:
+//  stage 1: psi_{n+1}, pih_{n+1} at plane m over the tile, the two rows above
+//           and the two below it (tile width), and the 2-site side vectors
+//           [x0-2, x0-1], [x0+tx, x0+tx+1] of rows y0-1 .. y0+TY, from psi_n
+//           of planes m-1, m, m+1 (a band of rows y0-3 .. y0+TY+2 and 4-site
+//           x strips of rows y0-2 .. y0+TY+1) and pih_n; psi_{n+1} goes into a
+//           three-plane ring;
+//  stage 2: psi_{n+2}, pih_{n+2} at plane m-1 over the tile, the rows y0-1 and
+//           y0+TY and the sites x0-1, x0+tx of the tile rows, psi_{n+2} into a
+//           second three-plane ring;
+//  stage 3: psi_{n+3}, pih_{n+3} of the tile at plane m-2, to global memory.
+// A thread computes the same sites in every stage it takes part in: the z+1
+// neighbour of stages 2 and 3 (written by the stage before in the same
+// iteration) and the momentum handed from stage to stage stay in its
+// registers, and the rings are read only at planes finished in earlier
+// iterations, so one barrier per plane suffices, as in the two-step kernel.
+// Centres and z-1 planes are read back from the rings (the two-step kernel's
+// LEAN form). DRAM: 32 B per site per pass, 10.7 B per site-update.
+template <int TY, int TXMAX, int S, int NCW>
+struct Z5Cfg {
+    static constexpr int CS = 8;                                   // bytes per complex float site
+    static constexpr int NC = NCW * 32;                            // consumer threads
+    static constexpr int NT = NC + 32;
+    static constexpr int NVX = TXMAX / 2;                          // 2-site vectors per row
+    static constexpr int MAXT = (TY * NVX + NC - 1) / NC;          // tile vectors per thread
+    static constexpr int MAXE = (4 * NVX + 2 * (TY + 2) + NC - 1) / NC;   // other stage-1 vectors per thread
+    // input slot
+    static constexpr int PB = (TY + 6) * TXMAX * CS;               // psi_n band, rows y0-3 .. y0+TY+2
+    static constexpr int SMID = (TY * 32 + 127) / 128 * 128;
+    static constexpr int STRIP = 128 + SMID + 128;                 // 4-site psi strip: rows 0-1 | 2..TY+1 | TY+2..TY+3
+    static constexpr int SL_OFF = PB, SR_OFF = PB + STRIP;
+    static constexpr int QB_OFF = PB + 2 * STRIP;                  // pih_n band, rows y0-2 .. y0+TY+1
+    static constexpr int QMID = (TY * 16 + 127) / 128 * 128;
+    static constexpr int PSTRIP = 128 + QMID + 128;                // 2-site pih strip: row 0 | 1..TY | TY+1
+    static constexpr int QL_OFF = QB_OFF + (TY + 4) * TXMAX * CS;
+    static constexpr int QR_OFF = QL_OFF + PSTRIP;
+    static constexpr int SLOT = QR_OFF + PSTRIP;
+    // psi_{n+1} ring plane: band rows y0-2 .. y0+TY+1, then the left and the
+    // right side vectors of rows y0-1 .. y0+TY
+    static constexpr int M1B = (TY + 4) * TXMAX * CS;
+    static constexpr int M1 = (M1B + 2 * (TY + 2) * 16 + 127) / 128 * 128;
+    // psi_{n+2} ring plane: band rows y0-1 .. y0+TY, then the sites x0-1 and
+    // x0+tx of the tile rows
+    static constexpr int M2B = (TY + 2) * TXMAX * CS;
+    static constexpr int M2 = (M2B + 2 * TY * CS + 127) / 128 * 128;
+    static constexpr int M1_OFF = S * SLOT;
+    static constexpr int M2_OFF = M1_OFF + 3 * M1;
+    static constexpr int BAR_OFF = M2_OFF + 3 * M2;
+    static constexpr int SMEM = BAR_OFF + 256;
+};
+
+// Byte offset of row r within a 4-site psi strip (r = 0 .. TY+3 for rows
+// y0-2 .. y0+TY+1; the boxes of rows 0-1, 2..TY+1 and TY+2..TY+3 start on
+// 128 bytes) and within a 2-site pih strip (r = 0 .. TY+1 for y0-1 .. y0+TY).
+template <int TY, int SMID>
+__device__ __forceinline__ int strip4_off(int r) {
+    return r < 2 ? r * 32 : (r < TY + 2 ? 128 + (r - 2) * 32 : 128 + SMID + (r - TY - 2) * 32);
+}
+template <int TY, int QMID>
+__device__ __forceinline__ int pstrip_off(int r) {
+    return r < 1 ? 0 : (r < TY + 1 ? 128 + (r - 1) * 16 : 128 + QMID);
+}
+
+__device__ __forceinline__ void dswap(int &a, int &b) {
+    const int t = a;
+    a = b;
+    b = t;
+}
+
+template <int TY, int TXMAX, int S, int NCW>
+__device__ __forceinline__ void zmarch_3step_body(const ZLat *__restrict__ lats, int nlat, int64_t total_items,
+                                                  int *counters, int parity, int *derr) {
+    typedef Z5Cfg<TY, TXMAX, S, NCW> K;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + K::BAR_OFF);
+    uint64_t *empty = full + S;
+    uint64_t *ifull = empty + S;                                 // [2]
+    uint64_t *iempty = ifull + 2;                                // [2]
+    uint64_t *midbar = iempty + 2;                               // consumer barrier of the rings
+    volatile int64_t *items = reinterpret_cast<volatile int64_t *>(midbar + 1);   // [2]
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(items + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), NCW);
+        }
+        for (int k = 0; k < 2; ++k) {
+            mbar_init(smem_u32(&ifull[k]), 1);
+            mbar_init(smem_u32(&iempty[k]), NCW);
+        }
+        mbar_init(smem_u32(midbar), NCW);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp == NCW) {
+        // ------------------------------------------------------------ producer
+        if (lane == 0) {
+            int64_t q = 0;
+            bool ok = true;
+            for (int64_t k = 0; ok; ++k) {
+                if (k >= 2) ok = mbar_wait_bounded(smem_u32(&iempty[k & 1]), (uint32_t)(((k >> 1) - 1) & 1));
+                if (!ok || *abort_flag) break;
+                const int64_t item = (int64_t)atomicAdd(&counters[0], 1);
+                items[k & 1] = item;
+                mbar_arrive(smem_u32(&ifull[k & 1]));
+                if (item >= total_items) break;
+                const int li = find_lat(lats, nlat, item);
+                const ZLat &Lt = lats[li];
+                const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
+                const int64_t local = item - Lt.item_base;
+                const int ncols = ntx * nty;
+                const int zq = (int)(local / ncols), col = (int)(local % ncols);
+                const int x0 = (col % ntx) * tx, y0 = (col / ntx) * TY;
+                const int za = (int)((int64_t)zq * N / nzc), zb = (int)((int64_t)(zq + 1) * N / nzc);
+                const int nload = zb - za + 6;   // psi_n planes za-3 .. zb+2
+                const int bin = Lt.a_index ^ parity;
+                const uint32_t psi_bytes = (uint32_t)((TY + 6) * tx * K::CS + 2 * (TY + 4) * 32);
+                const uint32_t pih_bytes = (uint32_t)((TY + 4) * tx * K::CS + 2 * (TY + 2) * 16);
+                // halo rows and columns with the periodic wrap (x0, y0 are
+                // multiples of tx, TY >= 3, so no box wraps inside itself;
+                // every x coordinate is even: 16-byte aligned)
+                const int ym3 = y0 >= 3 ? y0 - 3 : y0 - 3 + N;
+                const int ym2 = y0 >= 2 ? y0 - 2 : y0 - 2 + N;
+                const int ym1 = y0 >= 1 ? y0 - 1 : N - 1;
+                const int yp = (y0 + TY == N) ? 0 : y0 + TY;
+                const int xl4 = x0 >= 4 ? x0 - 4 : x0 - 4 + N;
+                const int xl2 = x0 >= 2 ? x0 - 2 : x0 - 2 + N;
+                const int xr = (x0 + tx == N) ? 0 : x0 + tx;
+                for (int i = 0; i < nload; ++i, ++q) {
+                    const int s = (int)(q % S);
+                    if (q >= S) {
+                        ok = mbar_wait_bounded(smem_u32(&empty[s]), (uint32_t)(((q / S) - 1) & 1));
+                        if (!ok || *abort_flag) break;
+                    }
+                    int z = za - 3 + i;
+                    z = z < 0 ? z + N : (z >= N ? z - N : z);
+                    unsigned char *slot = smem + s * K::SLOT;
+                    const uint32_t bar = smem_u32(&full[s]);
+                    const bool with_pih = i >= 1 && i <= nload - 2;   // stage-1 planes za-2 .. zb+1
+                    mbar_expect_tx(bar, psi_bytes + (with_pih ? pih_bytes : 0u) +
+                                            (i == 0 ? (uint32_t)Lt.debug_tx_excess : 0u));
+                    tma_load_3d(smem_u32(slot), &Lt.t3_row3[bin], x0, ym3, z, bar);
+                    tma_load_3d(smem_u32(slot + 3 * tx * K::CS), &Lt.tm_main[bin], x0, y0, z, bar);
+                    tma_load_3d(smem_u32(slot + (TY + 3) * tx * K::CS), &Lt.t3_row3[bin], x0, yp, z, bar);
+                    tma_load_3d(smem_u32(slot + K::SL_OFF), &Lt.t3_str2[bin], xl4, ym2, z, bar);
+                    tma_load_3d(smem_u32(slot + K::SL_OFF + 128), &Lt.t3_strm[bin], xl4, y0, z, bar);
+                    tma_load_3d(smem_u32(slot + K::SL_OFF + 128 + K::SMID), &Lt.t3_str2[bin], xl4, yp, z, bar);
+                    tma_load_3d(smem_u32(slot + K::SR_OFF), &Lt.t3_str2[bin], xr, ym2, z, bar);
+                    tma_load_3d(smem_u32(slot + K::SR_OFF + 128), &Lt.t3_strm[bin], xr, y0, z, bar);
+                    tma_load_3d(smem_u32(slot + K::SR_OFF + 128 + K::SMID), &Lt.t3_str2[bin], xr, yp, z, bar);
+                    if (with_pih) {
+                        tma_load_3d(smem_u32(slot + K::QB_OFF), &Lt.t3_prow2[bin], x0, ym2, z, bar);
+                        tma_load_3d(smem_u32(slot + K::QB_OFF + 2 * tx * K::CS), &Lt.tm_pih[bin], x0, y0, z, bar);
+                        tma_load_3d(smem_u32(slot + K::QB_OFF + (TY + 2) * tx * K::CS), &Lt.t3_prow2[bin], x0, yp, z,
+                                    bar);
+                        tma_load_3d(smem_u32(slot + K::QL_OFF), &Lt.t3_pst1[bin], xl2, ym1, z, bar);
+                        tma_load_3d(smem_u32(slot + K::QL_OFF + 128), &Lt.t2_pstr[bin], xl2, y0, z, bar);
+                        tma_load_3d(smem_u32(slot + K::QL_OFF + 128 + K::QMID), &Lt.t3_pst1[bin], xl2, yp, z, bar);
+                        tma_load_3d(smem_u32(slot + K::QR_OFF), &Lt.t3_pst1[bin], xr, ym1, z, bar);
+                        tma_load_3d(smem_u32(slot + K::QR_OFF + 128), &Lt.t2_pstr[bin], xr, y0, z, bar);
+                        tma_load_3d(smem_u32(slot + K::QR_OFF + 128 + K::QMID), &Lt.t3_pst1[bin], xr, yp, z, bar);
+                    }
+                }
+            }
+            if (!ok) {
+                atomicOr(derr, DEVERR_TIMEOUT);
+                *abort_flag = 1;
+            }
+            // Drain: wait (bounded) for this CTA's last loads still in flight.
+            for (int64_t d = q > S ? q - S : 0; d < q; ++d)
+                mbar_wait_bounded(smem_u32(&full[d % S]), (uint32_t)((d / S) & 1));
+        }
+    } else {
+        // ------------------------------------------------------------ consumers
+        const int cid = tid;   // 0 .. NC-1
+        int64_t q0 = 0;        // loads of the items before the current one
+        int64_t g = 0;         // iterations done (completed phases of midbar)
+        int gm = 0;            // g mod 3: the ring plane written next
+        for (int64_t k = 0;; ++k) {
+            int w = warp_wait(smem_u32(&ifull[k & 1]), (uint32_t)((k >> 1) & 1), abort_flag);
+            if (w) {
+                if (w == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
+                break;
+            }
+            const int64_t item = items[k & 1];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&iempty[k & 1]));
+            if (item >= total_items) break;
+            const int li = find_lat(lats, nlat, item);
+            const ZLat &Lt = lats[li];
+            const int N = Lt.N, tx = Lt.tx, ntx = Lt.ntx, nty = Lt.nty, nzc = Lt.nzc;
+            const int64_t local = item - Lt.item_base;
+            const int ncols = ntx * nty;
+            const int zq = (int)(local / ncols), col = (int)(local % ncols);
+            const int x0 = (col % ntx) * tx, y0 = (col / ntx) * TY;
+            const int za = (int)((int64_t)zq * N / nzc), zb = (int)((int64_t)(zq + 1) * N / nzc);
+            const int T_steps = zb - za;
+            const int bin = Lt.a_index ^ parity;
+            float2 *psi_out = reinterpret_cast<float2 *>(Lt.psi[bin ^ 1]);
+            float2 *pih_out = reinterpret_cast<float2 *>(Lt.pih[bin ^ 1]);
+            const double tau = Lt.clock[bin];
+            const double tau1 = tau + Lt.dt, tau2 = tau1 + Lt.dt;
+            const StepCoefs<float> cf1 = make_coefs<float>(tau, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs, Lt.form);
+            const StepCoefs<float> cf2 = make_coefs<float>(tau1, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs, Lt.form);
+            const StepCoefs<float> cf3 = make_coefs<float>(tau2, Lt.dt, Lt.dt, Lt.inv_dx2, Lt.lambda, Lt.T0sq3, Lt.prs, Lt.form);
+            if (local == 0 && cid == 0) Lt.clock[bin ^ 1] = tau2 + Lt.dt;   // tau += dt three times, s_integrate.cpp:317
+            const int nvx = tx / 2;
+            const int nvec = nvx * TY;
+            const int next = 4 * nvx + 2 * (TY + 2);
+            const int txb = tx * K::CS;   // bytes per band row
+            const int64_t NN = (int64_t)N * N;
+
+            // Tile vectors: offsets in an input slot (psi_n band row 3+yy,
+            // 4-site strip row 2+yy, pih_n band row 2+yy), in a psi_{n+1}
+            // plane (band row 2+yy, side-vector row 1+yy), in a psi_{n+2}
+            // plane (band row 1+yy, side sites of row yy), and the global
+            // offset at plane za.
+            int t_c[K::MAXT], t_l[K::MAXT], t_r[K::MAXT], t_q[K::MAXT];
+            int u_c[K::MAXT], u_l[K::MAXT], u_r[K::MAXT];   // psi_{n+1} plane
+            int w_c[K::MAXT], w_l[K::MAXT], w_r[K::MAXT];   // psi_{n+2} plane
+            int64_t g_off[K::MAXT];
+            // With sw, every vector's left and right x-neighbour offsets are
+            // stored swapped (x_neighbours puts the values back): the loads of a
+            // half-warp then cover all 32 banks.
+            const bool sw = swap_lane();
+#pragma unroll
+            for (int j = 0; j < K::MAXT; ++j) {
+                const int v = cid + j * K::NC;
+                const int yy = v < nvec ? v / nvx : 0, xx = v < nvec ? (v % nvx) * 2 : 0;
+                t_c[j] = (3 + yy) * txb + xx * K::CS;
+                t_l[j] = xx > 0 ? t_c[j] - K::CS : K::SL_OFF + strip4_off<TY, K::SMID>(2 + yy) + 24;
+                t_r[j] = xx + 2 < tx ? t_c[j] + 2 * K::CS : K::SR_OFF + strip4_off<TY, K::SMID>(2 + yy);
+                t_q[j] = K::QB_OFF + (2 + yy) * txb + xx * K::CS;
+                u_c[j] = (2 + yy) * txb + xx * K::CS;
+                u_l[j] = xx > 0 ? u_c[j] - K::CS : K::M1B + (1 + yy) * 16 + 8;
+                u_r[j] = xx + 2 < tx ? u_c[j] + 2 * K::CS : K::M1B + (TY + 2) * 16 + (1 + yy) * 16;
+                w_c[j] = (1 + yy) * txb + xx * K::CS;
+                w_l[j] = xx > 0 ? w_c[j] - K::CS : K::M2B + yy * K::CS;
+                w_r[j] = xx + 2 < tx ? w_c[j] + 2 * K::CS : K::M2B + (TY + yy) * K::CS;
+                g_off[j] = (int64_t)za * NN + (int64_t)(y0 + yy) * N + (x0 + xx);
+                if (sw) {
+                    dswap(t_l[j], t_r[j]);
+                    dswap(u_l[j], u_r[j]);
+                    dswap(w_l[j], w_r[j]);
+                }
+            }
+            // Other stage-1 vectors: kind 0 the rows y0-1 and y0+TY (stages 1
+            // and 2), kind 1 the rows y0-2 and y0+TY+1 (stage 1), kind 2 the
+            // side vectors of rows y0-1 .. y0+TY (stage 1; stage 2 on the site
+            // next to the tile, x0-1 or x0+tx, for the tile rows).
+            int e_kind[K::MAXE], e_c[K::MAXE], e_l[K::MAXE], e_r[K::MAXE], e_u[K::MAXE], e_d[K::MAXE], e_q[K::MAXE];
+            int e_m1[K::MAXE];                                            // psi_{n+1} offset (the vector)
+            int f_c[K::MAXE], f_l[K::MAXE], f_r[K::MAXE], f_u[K::MAXE], f_d[K::MAXE], f_w[K::MAXE];   // stage 2
+            bool e_s2[K::MAXE], e_hi[K::MAXE];   // takes part in stage 2; its stage-2 site is the vector's second
+#pragma unroll
+            for (int j = 0; j < K::MAXE; ++j) {
+                const int u = cid + j * K::NC;
+                e_kind[j] = -1;
+                e_c[j] = e_l[j] = e_r[j] = e_u[j] = e_d[j] = e_q[j] = e_m1[j] = 0;
+                f_c[j] = f_l[j] = f_r[j] = f_u[j] = f_d[j] = f_w[j] = 0;
+                e_s2[j] = e_hi[j] = false;
+                if (u >= next) continue;
+                if (u < 4 * nvx) {
+                    const bool outer = u >= 2 * nvx;
+                    const int uu = outer ? u - 2 * nvx : u;
+                    const bool below = uu >= nvx;
+                    const int xx = (uu % nvx) * 2;
+                    // rows: psi_n band b, strip s, pih band p, psi_{n+1} band m
+                    const int b = outer ? (below ? TY + 4 : 1) : (below ? TY + 3 : 2);
+                    const int s = b - 1, p = b - 1, m = b - 1;
+                    e_kind[j] = outer ? 1 : 0;
+                    e_c[j] = b * txb + xx * K::CS;
+                    e_u[j] = e_c[j] - txb;
+                    e_d[j] = e_c[j] + txb;
+                    e_l[j] = xx > 0 ? e_c[j] - K::CS : K::SL_OFF + strip4_off<TY, K::SMID>(s) + 24;
+                    e_r[j] = xx + 2 < tx ? e_c[j] + 2 * K::CS : K::SR_OFF + strip4_off<TY, K::SMID>(s);
+                    e_q[j] = K::QB_OFF + p * txb + xx * K::CS;
+                    e_m1[j] = m * txb + xx * K::CS;
+                    if (!outer) {   // stage 2 on the same vector: psi_{n+1} row m, side-vector row m-1
+                        e_s2[j] = true;
+                        f_c[j] = e_m1[j];
+                        f_u[j] = f_c[j] - txb;
+                        f_d[j] = f_c[j] + txb;
+                        f_l[j] = xx > 0 ? f_c[j] - K::CS : K::M1B + (m - 1) * 16 + 8;
+                        f_r[j] = xx + 2 < tx ? f_c[j] + 2 * K::CS : K::M1B + (TY + 2) * 16 + (m - 1) * 16;
+                        f_w[j] = (below ? TY + 1 : 0) * txb + xx * K::CS;
+                    }
+                } else {
+                    const int kk = u - 4 * nvx;
+                    const int side = kk / (TY + 2), r = kk % (TY + 2);   // row y0-1+r
+                    const int so = side ? K::SR_OFF : K::SL_OFF;
+                    const int vo = side ? 0 : 16;                        // the vector within the strip row
+                    e_kind[j] = 2;
+                    e_c[j] = so + strip4_off<TY, K::SMID>(r + 1) + vo;
+                    e_u[j] = so + strip4_off<TY, K::SMID>(r) + vo;
+                    e_d[j] = so + strip4_off<TY, K::SMID>(r + 2) + vo;
+                    // x neighbours: left vector x0-3 (strip) and x0 (band);
+                    // right vector x0+tx-1 (band) and x0+tx+2 (strip)
+                    e_l[j] = side ? (r + 2) * txb + (tx - 1) * K::CS : so + strip4_off<TY, K::SMID>(r + 1) + 8;
+                    e_r[j] = side ? so + strip4_off<TY, K::SMID>(r + 1) + 16 : (r + 2) * txb;
+                    e_q[j] = (side ? K::QR_OFF : K::QL_OFF) + pstrip_off<TY, K::QMID>(r);
+                    e_m1[j] = K::M1B + (side * (TY + 2) + r) * 16;
+                    if (r >= 1 && r <= TY) {   // the site next to the tile, row y0-1+r of the tile rows
+                        e_s2[j] = true;
+                        e_hi[j] = side == 0;   // x0-1 is the left vector's second site, x0+tx the right's first
+                        const int own = side ? 0 : 8;
+                        f_c[j] = e_m1[j] + own;
+                        f_u[j] = e_m1[j] - 16 + own;
+                        f_d[j] = e_m1[j] + 16 + own;
+                        f_l[j] = side ? (r + 1) * txb + (tx - 1) * K::CS : e_m1[j];
+                        f_r[j] = side ? e_m1[j] + 8 : (r + 1) * txb;
+                        f_w[j] = K::M2B + (side * TY + r - 1) * K::CS;
+                    }
+                }
+                if (sw) {   // the vectors' x neighbours (a side vector's stage-2 site reads them plainly)
+                    dswap(e_l[j], e_r[j]);
+                    if (e_kind[j] == 0) dswap(f_l[j], f_r[j]);
+                }
+            }
+
+            float4 a_zm[K::MAXT], e_zm[K::MAXE];   // psi_n of plane m-1 (stage 1's z-1 neighbour)
+            float4 p1_t[K::MAXT], p1_e[K::MAXE];   // pih_{n+1} of plane m-1 (stage 2)
+            float4 p2_t[K::MAXT];                  // pih_{n+2} of plane m-2 (stage 3)
+            const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < K::MAXT; ++j) a_zm[j] = p1_t[j] = p2_t[j] = zero4;
+#pragma unroll
+            for (int j = 0; j < K::MAXE; ++j) e_zm[j] = p1_e[j] = zero4;
+
+            // load q sits in slot q % S and completes phase (q / S) & 1 of full[slot]
+            int s0 = (int)(q0 % S);
+            uint32_t ph0 = (uint32_t)((q0 / S) & 1);
+            int s1 = s0 + 1;
+            uint32_t ph1 = ph0;
+            if (s1 == S) { s1 = 0; ph1 ^= 1u; }
+            // plane za-3 (load 0) primes the z-1 registers; load 1 is the first centre
+            w = warp_wait(smem_u32(&full[s0]), ph0, abort_flag);
+            if (!w) w = warp_wait(smem_u32(&full[s1]), ph1, abort_flag);
+            if (w) {
+                if (w == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
+                break;
+            }
+            {
+                const unsigned char *B0 = smem + s0 * K::SLOT;
+#pragma unroll
+                for (int j = 0; j < K::MAXT; ++j)
+                    if (cid + j * K::NC < nvec) a_zm[j] = ldb4(B0, t_c[j]);
+#pragma unroll
+                for (int j = 0; j < K::MAXE; ++j)
+                    if (e_kind[j] >= 0) e_zm[j] = ldb4(B0, e_c[j]);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&empty[s0]));
+
+            int sc = s1, sn = s1 + 1;
+            uint32_t phn = ph1;
+            if (sn == S) { sn = 0; phn ^= 1u; }
+            bool ok = true;
+            for (int i = 0; i <= T_steps + 3; ++i) {
+                w = warp_wait(smem_u32(&full[sn]), phn, abort_flag);
+                if (w) {
+                    if (w == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
+                    ok = false;
+                    break;
+                }
+                const unsigned char *Sc = smem + sc * K::SLOT, *Sn = smem + sn * K::SLOT;
+                const int g1 = gm, g0 = gm == 0 ? 2 : gm - 1, gz = g0 == 0 ? 2 : g0 - 1;   // planes m, m-1, m-2 of a ring
+                unsigned char *R1w = smem + K::M1_OFF + g1 * K::M1;
+                const unsigned char *R1c = smem + K::M1_OFF + g0 * K::M1, *R1z = smem + K::M1_OFF + gz * K::M1;
+                unsigned char *R2w = smem + K::M2_OFF + g1 * K::M2;
+                const unsigned char *R2c = smem + K::M2_OFF + g0 * K::M2, *R2z = smem + K::M2_OFF + gz * K::M2;
+                // ---- stage 1 at plane m (load i+1), z+1 from load i+2
+                float4 b1_t[K::MAXT], q1_t[K::MAXT], b1_e[K::MAXE], q1_e[K::MAXE];
+#pragma unroll
+                for (int j = 0; j < K::MAXT; ++j) {
+                    b1_t[j] = q1_t[j] = zero4;
+                    if (cid + j * K::NC >= nvec) continue;
+                    const float4 ac = ldb4(Sc, t_c[j]);
+                    float4 p = ldb4(Sc, t_q[j]);
+                    float2 xl, xr;
+                    x_neighbours(Sc, t_l[j], t_r[j], sw, xl, xr);
+                    const float4 o = update_vec2(ac, a_zm[j], ldb4(Sn, t_c[j]), ldb4(Sc, t_c[j] - txb),
+                                                 ldb4(Sc, t_c[j] + txb), xl, xr, p, cf1);
+                    *reinterpret_cast<float4 *>(R1w + u_c[j]) = o;
+                    b1_t[j] = o;
+                    q1_t[j] = p;
+                    a_zm[j] = ac;
+                }
+#pragma unroll
+                for (int j = 0; j < K::MAXE; ++j) {
+                    b1_e[j] = q1_e[j] = zero4;
+                    if (e_kind[j] < 0) continue;
+                    const float4 ac = ldb4(Sc, e_c[j]);
+                    float4 p = ldb4(Sc, e_q[j]);
+                    float2 xl, xr;
+                    x_neighbours(Sc, e_l[j], e_r[j], sw, xl, xr);
+                    const float4 o = update_vec2(ac, e_zm[j], ldb4(Sn, e_c[j]), ldb4(Sc, e_u[j]), ldb4(Sc, e_d[j]),
+                                                 xl, xr, p, cf1);
+                    *reinterpret_cast<float4 *>(R1w + e_m1[j]) = o;
+                    b1_e[j] = o;
+                    q1_e[j] = p;
+                    e_zm[j] = ac;
+                }
+                // this warp is done with load i+1; at the last plane also with load i+2
+                __syncwarp();
+                if (lane == 0) {
+                    mbar_arrive(smem_u32(&empty[sc]));
+                    if (i == T_steps + 3) mbar_arrive(smem_u32(&empty[sn]));
+                }
+                // ---- stage 2 at plane m-1 (planes za-1 .. zb)
+                float4 b2_t[K::MAXT], q2_t[K::MAXT];
+#pragma unroll
+                for (int j = 0; j < K::MAXT; ++j) b2_t[j] = q2_t[j] = zero4;
+                if (i >= 2) {
+#pragma unroll
+                    for (int j = 0; j < K::MAXT; ++j) {
+                        if (cid + j * K::NC >= nvec) continue;
+                        float4 p = p1_t[j];
+                        float2 xl, xr;
+                        x_neighbours(R1c, u_l[j], u_r[j], sw, xl, xr);
+                        const float4 o = update_vec2(ldb4(R1c, u_c[j]), ldb4(R1z, u_c[j]), b1_t[j], ldb4(R1c, u_c[j] - txb),
+                                                     ldb4(R1c, u_c[j] + txb), xl, xr, p, cf2);
+                        *reinterpret_cast<float4 *>(R2w + w_c[j]) = o;
+                        b2_t[j] = o;
+                        q2_t[j] = p;
+                    }
+#pragma unroll
+                    for (int j = 0; j < K::MAXE; ++j) {
+                        if (!e_s2[j]) continue;
+                        if (e_kind[j] == 0) {
+                            float4 p = p1_e[j];
+                            float2 xl, xr;
+                            x_neighbours(R1c, f_l[j], f_r[j], sw, xl, xr);
+                            const float4 o = update_vec2(ldb4(R1c, f_c[j]), ldb4(R1z, f_c[j]), b1_e[j], ldb4(R1c, f_u[j]),
+                                                         ldb4(R1c, f_d[j]), xl, xr, p, cf2);
+                            *reinterpret_cast<float4 *>(R2w + f_w[j]) = o;
+                        } else {   // one site of a side vector
+                            const bool hi = e_hi[j];
+                            float2 p = hi ? make_float2(p1_e[j].z, p1_e[j].w) : make_float2(p1_e[j].x, p1_e[j].y);
+                            const float2 zp = hi ? make_float2(b1_e[j].z, b1_e[j].w) : make_float2(b1_e[j].x, b1_e[j].y);
+                            *reinterpret_cast<float2 *>(R2w + f_w[j]) =
+                                update_site(ldb2(R1c, f_c[j]), ldb2(R1c, f_l[j]), ldb2(R1c, f_r[j]), ldb2(R1c, f_u[j]),
+                                            ldb2(R1c, f_d[j]), ldb2(R1z, f_c[j]), zp, p, cf2);
+                        }
+                    }
+                }
+                // ---- stage 3 at plane m-2 (planes za .. zb-1)
+                if (i >= 4) {
+#pragma unroll
+                    for (int j = 0; j < K::MAXT; ++j) {
+                        if (cid + j * K::NC >= nvec) continue;
+                        float4 p = p2_t[j];
+                        float2 xl, xr;
+                        x_neighbours(R2c, w_l[j], w_r[j], sw, xl, xr);
+                        const float4 o = update_vec2(ldb4(R2c, w_c[j]), ldb4(R2z, w_c[j]), b2_t[j], ldb4(R2c, w_c[j] - txb),
+                                                     ldb4(R2c, w_c[j] + txb), xl, xr, p, cf3);
+                        st4(&pih_out[g_off[j]], p);
+                        st4(&psi_out[g_off[j]], o);
+                        g_off[j] += NN;
+                    }
+                }
+                // the momentum moves one stage on
+#pragma unroll
+                for (int j = 0; j < K::MAXT; ++j) {
+                    p2_t[j] = q2_t[j];
+                    p1_t[j] = q1_t[j];
+                }
+#pragma unroll
+                for (int j = 0; j < K::MAXE; ++j) p1_e[j] = q1_e[j];
+                // plane m of ring 1 and plane m-1 of ring 2 are complete before
+                // anyone reads them; the planes the next iteration overwrites are
+                // no longer read
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(midbar));
+                w = warp_wait(smem_u32(midbar), (uint32_t)(g & 1), abort_flag);
+                ++g;
+                gm = gm == 2 ? 0 : gm + 1;
+                if (w) {
+                    if (w == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
+                    ok = false;
+                    break;
+                }
+                sc = sn;
+                if (++sn == S) { sn = 0; phn ^= 1u; }
+            }
+            if (!ok) break;
+            q0 += T_steps + 6;
+        }
+    }
+    __syncwarp();      // reconverge every warp (the producer's lane 0 ran alone) before the barrier
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&counters[1], 1) == (int)gridDim.x - 1) {
+            counters[0] = 0;
+            counters[1] = 0;
+            __threadfence();
+        }
+    }
+}
+
+// Two CTAs of NCW + 1 warps per SM (registers per thread as LeanRegs counts
+// them: each SM sub-partition holds 16K registers for a quarter of the warps).
+template <int TY, int TXMAX, int S, int NCW>
+__global__ void __maxnreg__((LeanRegs<NCW, 2>::VALUE))
+    k_zmarch_3step(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity, int *derr) {
+    zmarch_3step_body<TY, TXMAX, S, NCW>(lats, nlat, total_items, counters, parity, derr);
+}
+
 // ============================================================== host side
 
 int current_device() {
@@ -1302,7 +1819,9 @@ static int grid_for(int64_t len, int threads = 256) {
 // gen 1: k_zmarch (CTA barriers); gen 2: k_zmarch2 (producer warp); gen 3:
 // k_zmarch_2step (two steps per pass, complex float), whose odd last step of an
 // interval runs on the gen-2 `partner` with the same tile and launch table.
-// gen 4: k_zmarch2r (stencil radius r = 2..4, axs_step_r.cu).
+// gen 4: k_zmarch2r (stencil radius r = 2..4, axs_step_r.cu). gen 5:
+// k_zmarch_3step (three steps per pass), whose last one or two steps of an
+// interval run on its gen-3 `partner` (same tile, same launch table).
 struct ZVariant {
     int gen, ty, txmax, slots, ncw, partner, r, lean;
 };
@@ -1336,10 +1855,18 @@ static const ZVariant kZVariants[] = {
     // holds the R + 1 planes still to be centres, so S = R + 2 keeps one plane
     // load in flight per CTA; these keep three (radius 2: two), at two CTAs per SM
     {4, 4, 128, 7, 8, -1, 3},  {4, 8, 64, 7, 8, -1, 3},  {4, 8, 64, 8, 8, -1, 4},  {4, 4, 128, 5, 8, -1, 2},
+    // 46-47: three steps per pass (halo depth 3) on 8 x 64 and 16 x 32 tiles, two
+    // CTAs of eight consumer warps per SM; an interval's last one or two steps
+    // run on the two-step partner (variant 30 or 39) and its one-step partner
+    {5, 8, 64, 4, 8, 30, 0, 1},  {5, 16, 32, 4, 8, 39, 0, 1},
 };
 static const int kNumZVariants = sizeof(kZVariants) / sizeof(kZVariants[0]);
 
 static bool two_step(int variant) { return variant >= 0 && variant < kNumZVariants && kZVariants[variant].gen == 3; }
+static bool three_step(int variant) { return variant >= 0 && variant < kNumZVariants && kZVariants[variant].gen == 5; }
+// the momentum is written out of place (pih and scratch exchange after every launch)
+static bool out_of_place(int variant) { return two_step(variant) || three_step(variant); }
+static int steps_per_pass(int variant) { return three_step(variant) ? 3 : (two_step(variant) ? 2 : 1); }
 static int radius(const ZVariant &v) { return v.r > 0 ? v.r : 1; }
 
 std::string StepConfig::describe() const {
@@ -1348,6 +1875,9 @@ std::string StepConfig::describe() const {
     else if (two_step(variant))
         snprintf(b, sizeof b, "TMA z-march variant %d (two steps per pass, halo depth 2%s; odd step on variant %d), tx=%d, zchunk=%d",
                  variant, kZVariants[variant].lean ? ", lean" : "", kZVariants[variant].partner, tx, zchunk);
+    else if (three_step(variant))
+        snprintf(b, sizeof b, "TMA z-march variant %d (three steps per pass, halo depth 3; last steps on variant %d), tx=%d, zchunk=%d",
+                 variant, kZVariants[variant].partner, tx, zchunk);
     else if (variant >= 0 && variant < kNumZVariants && kZVariants[variant].gen == 4)
         snprintf(b, sizeof b, "TMA z-march variant %d (stencil radius %d), tx=%d, zchunk=%d", variant,
                  kZVariants[variant].r, tx, zchunk);
@@ -1441,6 +1971,40 @@ static void launch_zmarch3_t(const ZLat *d, int nlat, int64_t items, int *counte
     count_launches(1);
 }
 
+template <int TY, int TXMAX, int S, int NCW>
+static int prepare_zmarch5_t() {
+    typedef Z5Cfg<TY, TXMAX, S, NCW> K;
+    static PerDevice occ;   // the attribute and occupancy belong to the device
+    return occ.get([] {
+        const auto kern = k_zmarch_3step<TY, TXMAX, S, NCW>;
+        AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
+        int o = 0;
+        AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, K::NT, K::SMEM));
+        if (o < 1) {
+            cudaFuncAttributes fa;
+            AXS_CUDA(cudaFuncGetAttributes(&fa, kern));
+            fail(AXS_ERR_CUDA,
+                 "three-step z-march kernel <%d,%d,%d,%d> does not fit on an SM (%d threads x %d registers, "
+                 "%d B dynamic shared memory of %d allowed, %d B static, max %d threads per block)",
+                 TY, TXMAX, S, NCW, K::NT, fa.numRegs, K::SMEM, fa.maxDynamicSharedSizeBytes, (int)fa.sharedSizeBytes,
+                 fa.maxThreadsPerBlock);
+        }
+        return o;
+    });
+}
+
+template <int TY, int TXMAX, int S, int NCW>
+static void launch_zmarch5_t(const ZLat *d, int nlat, int64_t items, int *counters, int parity, int *derr,
+                             cudaStream_t st, int ctas_per_sm) {
+    typedef Z5Cfg<TY, TXMAX, S, NCW> K;
+    int occ = prepare_zmarch5_t<TY, TXMAX, S, NCW>();
+    int per = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ) : occ;
+    int64_t grid = std::min<int64_t>((int64_t)per * num_sms(), items);
+    k_zmarch_3step<TY, TXMAX, S, NCW><<<(int)grid, K::NT, K::SMEM, st>>>(d, nlat, items, counters, parity, derr);
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+
 static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t items, int *counters, int parity,
                           int *derr, cudaStream_t st, int ctas_per_sm) {
     if (variant >= 0 && variant < kNumZVariants && kZVariants[variant].gen == 4) {
@@ -1503,6 +2067,14 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
     case 40:
         if (esz != 4) fail(AXS_ERR_ARG, "two-step z-march variant %d needs complex float fields", variant);
         launch_zmarch3_t<16, 32, 5, 4, 1, true>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);
+        break;
+    case 46:
+        if (esz != 4) fail(AXS_ERR_ARG, "three-step z-march variant %d needs complex float fields", variant);
+        launch_zmarch5_t<8, 64, 4, 8>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);
+        break;
+    case 47:
+        if (esz != 4) fail(AXS_ERR_ARG, "three-step z-march variant %d needs complex float fields", variant);
+        launch_zmarch5_t<16, 32, 4, 8>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);
         break;
 
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
@@ -1569,10 +2141,16 @@ static void prepare_zmarch(int esz, int variant) {
     case 40:
         if (esz == 4) prepare_zmarch3_t<16, 32, 5, 4, 1, true>();
         break;
+    case 46:
+        if (esz == 4) prepare_zmarch5_t<8, 64, 4, 8>();
+        break;
+    case 47:
+        if (esz == 4) prepare_zmarch5_t<16, 32, 4, 8>();
+        break;
 
     default: fail(AXS_ERR_ARG, "bad z-march variant %d", variant);
     }
-    if (kZVariants[variant].gen == 3) prepare_zmarch(esz, kZVariants[variant].partner);
+    if (kZVariants[variant].gen == 3 || kZVariants[variant].gen == 5) prepare_zmarch(esz, kZVariants[variant].partner);
 #undef AXS_ZP
 #undef AXS_ZP2
 #undef AXS_ZP3
@@ -1600,6 +2178,13 @@ static int variant_smem(const ZVariant &v, int esz) {
         int c = (v.ty + 2 * v.r) * v.txmax * cs, h = (v.ty * rp * cs + 127) / 128 * 128;
         return v.slots * ((c + 2 * h + v.ty * v.txmax * cs + 127) / 128 * 128) + 256;
     }
+    if (v.gen == 5) {   // mirrors Z5Cfg
+        int smid = (v.ty * 32 + 127) / 128 * 128, qmid = (v.ty * 16 + 127) / 128 * 128;
+        int slot = (v.ty + 6) * v.txmax * cs + 2 * (256 + smid) + (v.ty + 4) * v.txmax * cs + 2 * (256 + qmid);
+        int m1 = ((v.ty + 4) * v.txmax * cs + 2 * (v.ty + 2) * 16 + 127) / 128 * 128;
+        int m2 = ((v.ty + 2) * v.txmax * cs + 2 * v.ty * cs + 127) / 128 * 128;
+        return v.slots * slot + 3 * m1 + 3 * m2 + 256;
+    }
     if (v.gen == 3) {
         int st_m = (v.ty * 16 + 127) / 128 * 128;
         int slot = (v.ty + 4) * v.txmax * cs + 2 * (256 + st_m) + (v.ty + 2) * v.txmax * cs + 2 * st_m;
@@ -1623,6 +2208,15 @@ static int max_smem_optin() {
 
 // The tx a variant would use for an N (largest admissible divisor), or 0.
 static int variant_tx(const ZVariant &v, int N, int esz) {
+    if (v.gen == 5) {
+        // complex float, x-tiled (the kernel takes its x halo from strips), and
+        // the two-step partner tiles N the same way
+        if (esz != 4 || variant_smem(v, esz) > max_smem_optin() || v.ty < 3) return 0;
+        const ZVariant &pv = kZVariants[v.partner];
+        int tx = variant_tx(pv, N, esz);
+        if (!tx || pv.ty != v.ty || tx > v.txmax || tx >= N || tx < 4) return 0;
+        return tx;
+    }
     if (v.gen == 3) {
         // complex float only; the partner must tile N the same way
         if (esz != 4 || variant_smem(v, esz) > max_smem_optin()) return 0;
@@ -1700,8 +2294,8 @@ static int64_t fill_zlat(ZLat &z, Lattice *L, int variant, int zchunk, int64_t i
     int tx = variant_tx(v, N, L->esz);
     if (!tx) fail(AXS_ERR_ARG, "z-march variant %d cannot tile N=%d", variant, N);
     prepare_zmarch(L->esz, variant);
-    const bool oop = v.gen == 3;
-    if (oop && (!L->scratch || L->scratch == L->pih)) fail(AXS_ERR_STATE, "two-step variant without a second momentum buffer");
+    const bool oop = v.gen == 3 || v.gen == 5;
+    if (oop && (!L->scratch || L->scratch == L->pih)) fail(AXS_ERR_STATE, "multi-step variant without a second momentum buffer");
     memset(&z, 0, sizeof z);
     int vs = 16 / (2 * L->esz);
     const int R = radius(v);
@@ -1714,11 +2308,18 @@ static int64_t fill_zlat(ZLat &z, Lattice *L, int variant, int zchunk, int64_t i
         encode_map(&z.tm_main[b], L->psi[b], N, L->esz, tx, v.ty);
         encode_map(&z.tm_xh[b], L->psi[b], N, L->esz, rp, v.ty);   // x-halo strip
         encode_map(&z.tm_pih[b], pb[b], N, L->esz, tx, v.ty);
-        if (oop) {
+        if (oop) {   // the two-step kernel's maps (a three-step variant's partner)
             encode_map(&z.t2_row2[b], L->psi[b], N, L->esz, tx, 2);
             encode_map(&z.t2_str2[b], L->psi[b], N, L->esz, vs, 2);
             encode_map(&z.t2_prow[b], pb[b], N, L->esz, tx, 1);
             encode_map(&z.t2_pstr[b], pb[b], N, L->esz, vs, v.ty);
+        }
+        if (v.gen == 5) {
+            encode_map(&z.t3_row3[b], L->psi[b], N, L->esz, tx, 3);
+            encode_map(&z.t3_strm[b], L->psi[b], N, L->esz, 2 * vs, v.ty);
+            encode_map(&z.t3_str2[b], L->psi[b], N, L->esz, 2 * vs, 2);
+            encode_map(&z.t3_prow2[b], pb[b], N, L->esz, tx, 2);
+            encode_map(&z.t3_pst1[b], pb[b], N, L->esz, vs, 1);
         }
         z.psi[b] = L->psi[b];
         z.pih[b] = pb[b];
@@ -1765,7 +2366,7 @@ static void ensure_single_table(Lattice *L) {
 static bool single_table_valid(const Lattice *L) {
     if (!L->dzlat || L->zlat_variant != L->cfg.variant || L->zlat_zchunk != L->cfg.zchunk) return false;
     if (L->zlat_pih[L->cur] != L->pih) return false;
-    return two_step(L->cfg.variant) ? L->zlat_pih[L->cur ^ 1] == L->scratch : L->zlat_pih[L->cur ^ 1] == L->pih;
+    return out_of_place(L->cfg.variant) ? L->zlat_pih[L->cur ^ 1] == L->scratch : L->zlat_pih[L->cur ^ 1] == L->pih;
 }
 
 void step_setup(Lattice *L) {
@@ -1925,6 +2526,11 @@ int lattice_advance(Lattice *L, int max_steps) {
     } else if (L->cfg.kind == 1) {
         if (!single_table_valid(L)) ensure_single_table(L);
         int kv = L->cfg.variant;
+        if (three_step(kv)) {   // an interval's last one or two steps run on the partners
+            swap = true;
+            if (max_steps >= 3) k = 3;
+            else kv = kZVariants[kv].partner;
+        }
         if (two_step(kv)) {
             swap = true;
             if (max_steps >= 2) k = 2;
@@ -2157,7 +2763,7 @@ void lattice_autotune(Lattice *L) {
     }
     const int zchunks[] = {32, 64, 128, 256};
     auto trial = [&](int v, int zc, int nrep, int nwarm) {
-        const bool two = two_step(v);
+        const bool two = out_of_place(v);
         StepConfig c;
         c.kind = 1;
         c.variant = v;
@@ -2169,7 +2775,7 @@ void lattice_autotune(Lattice *L) {
             L->cur ^= 1;
             if (two) std::swap(L->pih, L->scratch);
         }, nwarm);
-        if (two) ms *= 0.5;   // per step
+        ms /= steps_per_pass(v);   // per step
         c.tx = L->cfg.tx;
         log.push_back({c, ms});
         return std::make_pair(c, ms);
@@ -2215,6 +2821,7 @@ void lattice_autotune(Lattice *L) {
 
 // ---------------------------------------------------------------- ensemble
 static bool ensemble_variant_ok(Ensemble *E, int v) {
+    if (three_step(v)) return false;   // single lattices only
     for (Lattice *m : E->members)
         if (m->p.NDIMS != 3 || m->p.laplacian != 0 || !variant_fits(kZVariants[v], m->p, m->esz)) return false;
     return true;

@@ -386,14 +386,22 @@ def gpu_arm(args, dist):
     sites_all = dist.sum(main["sites"])
     value = sites_all * args.steps / (main["ms"] * 1e-3)
     launches = max(1, main["launches"])
-    steps_per_launch = args.steps / launches              # 2 for the two-step kernel, else 1
+    # steps per launch: 3 or 2 for the multi-step kernels (an interval's last
+    # one or two steps run on their partners, each pass moving the same bytes)
+    steps_per_launch = args.steps / launches
     per_launch_ms = main["ms"] / launches
     achieved = BYTES_PER_SITE[args.precision] * main["sites"] / (per_launch_ms * 1e-3) / 1e9
     two_step = "two steps per pass" in main["desc"]
+    three_step = "three steps per pass" in main["desc"]
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "k_zmarch_traffic.txt")
-    tkey = ("zmarch_2step_lean_fp32_1024_per_launch_bytes:" if "lean" in main["desc"] else
-            "zmarch_2step_fp32_1024_per_launch_bytes:") if two_step else "zmarch_fp32_1024_per_launch_bytes:"
+    if three_step:
+        tkey = "zmarch_3step_fp32_1024_per_launch_bytes:"
+    elif two_step:
+        tkey = ("zmarch_2step_lean_fp32_1024_per_launch_bytes:" if "lean" in main["desc"] else
+                "zmarch_2step_fp32_1024_per_launch_bytes:")
+    else:
+        tkey = "zmarch_fp32_1024_per_launch_bytes:"
     if args.precision == 32 and args.n == N_MAIN and args.stencil == 0 and os.path.exists(tfile):
         for line in open(tfile):
             if line.startswith(tkey):

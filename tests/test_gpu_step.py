@@ -108,13 +108,43 @@ def test_two_step_variants_bit_identical(axs, N):
             assert np.array_equal(g[q], g0[q]), (d0, d, q)
 
 
+THREE_STEP = ["1,46,64", "1,46,32", "1,47,64", "1,47,128"]
+
+
+@pytest.mark.parametrize("N", [160, 192])
+def test_three_step_variants_bit_identical(axs, N):
+    """Three steps per pass (halo depth 3) give the bits of one-step passes:
+    intervals of every length mod 3 (the last one or two steps run on the
+    two-step and one-step partners), eager launches and graph replays."""
+    p = params(axs, 3, N, 32)
+    outs = []
+    for force in ["0,0,64"] + THREE_STEP:
+        os.environ["AXS_FORCE_CONFIG"] = force
+        try:
+            with axs.Lattice(p) as L:
+                L.init_thermal(23)
+                for n in (1, 3, 1, 6, 2, 5, 4, 3):
+                    L.evolve(n)
+                d = L.describe()
+                outs.append((force, d, L.download(dtype=np.float32), L.time))
+        finally:
+            del os.environ["AXS_FORCE_CONFIG"]
+    f0, d0, g0, t0 = outs[0]
+    assert "generic" in d0
+    for force, d, g, t in outs[1:]:
+        assert "three steps per pass" in d, d
+        assert t == t0, (d, t, t0)
+        for q in range(4):
+            assert np.array_equal(g[q], g0[q]), (d0, d, q)
+
+
 def test_two_step_after_analysis_and_checkpoint(axs):
     """The momentum moves between two buffers in two-step mode; analysis
     (which uses the spare buffer), checkpoints and uploads in between keep
     the run identical to the one-step run."""
     p = params(axs, 3, 160, 32)
     res = []
-    for force in ["1,6,64", "1,10,64", "1,30,64"]:
+    for force in ["1,6,64", "1,10,64", "1,30,64", "1,46,64", "1,47,32"]:
         os.environ["AXS_FORCE_CONFIG"] = force
         try:
             with axs.Lattice(p) as L:
