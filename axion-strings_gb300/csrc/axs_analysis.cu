@@ -1806,11 +1806,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_background(cons
     Acc<T> a[6];
     const int64_t npair = len >> 1;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-#pragma unroll 2
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npair; i += stride) {
-        C f[2], p[2];
-        load_pair(psi, i, f);
-        load_pair(pih, i, p);
+    auto trip = [&](C (&f)[2], C (&p)[2]) {
         T t[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) t[k] = 0;
@@ -1826,6 +1822,24 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_background(cons
         }
 #pragma unroll
         for (int k = 0; k < 6; ++k) a[k].add(t[k]);
+    };
+    // the loads of two trips are in flight before either is summed (the same
+    // trips in the same order as one at a time: the same sums)
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + stride < npair; i += 2 * stride) {
+        C f0[2], p0[2], f1[2], p1[2];
+        load_pair(psi, i, f0);
+        load_pair(pih, i, p0);
+        load_pair(psi, i + stride, f1);
+        load_pair(pih, i + stride, p1);
+        trip(f0, p0);
+        trip(f1, p1);
+    }
+    if (i < npair) {
+        C f[2], p[2];
+        load_pair(psi, i, f);
+        load_pair(pih, i, p);
+        trip(f, p);
     }
     double v[6];
     for (int k = 0; k < 6; ++k) v[k] = a[k].value();
