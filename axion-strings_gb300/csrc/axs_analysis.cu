@@ -1360,6 +1360,174 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_axion_zcol(cons
     }
 }
 
+// ---- z-column kernels for the radius-R stencils (R = 2..4)
+//
+// A block marches 32 x 8 columns through z. Each thread keeps its column's
+// psi in a register ring for the z-neighbours, as the radius-1 kernels do,
+// while the in-plane neighbours at distances 1..R come from a shared-memory
+// copy of the block's plane tile with an R-wide periodic halo. The tiles are
+// staged by cp.async (8 or 16 B per element, no registers held) ZT_AHEAD
+// planes ahead in a ring of ZT_AHEAD + 1 slots, with one block barrier per
+// site. Reading 4R neighbours per site straight from global memory left the
+// warps waiting on L1/L2 latency (about a third of the DRAM rate at R = 4).
+constexpr int ZT_AHEAD = 2;
+
+__device__ __forceinline__ void cp_async_ca(uint32_t dst, const void *src, int bytes) {
+    if (bytes == 16) asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int P>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(P) : "memory"); }
+
+// One block's plane tile: (8 + 2R) rows of (32 + 2R) elements, the block's
+// columns with their periodic halo. Thread t copies elements t, t + 256, ...
+template <typename T, int R>
+struct ZTile {
+    typedef typename Cplx<T>::type C;
+    static constexpr int TW = 32 + 2 * R, TH = 8 + 2 * R, E = TW * TH, PER = (E + 255) / 256;
+    int goff[PER];   // the elements' offsets within a plane, -1 past the tile
+    __device__ __forceinline__ ZTile(int bx0, int by0, int N) {
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int e = (int)threadIdx.x + 256 * k;
+            goff[k] = -1;
+            if (e < E) {
+                int gx = (bx0 - R + e % TW) % N, gy = (by0 - R + e / TW) % N;
+                if (gx < 0) gx += N;
+                if (gy < 0) gy += N;
+                goff[k] = gy * N + gx;
+            }
+        }
+    }
+    // copy plane `plane` (a pointer to its first element) into `slot`
+    __device__ __forceinline__ void issue(const C *plane, C *slot) const {
+#pragma unroll
+        for (int k = 0; k < PER; ++k)
+            if (goff[k] >= 0) cp_async_ca(smem_u32(slot + threadIdx.x + 256 * k), plane + goff[k], (int)sizeof(C));
+    }
+};
+
+// The radius-R stencil sums of a column's site in plane z, in stencil_at's
+// order (coefficient 0 times the centre; per distance l the x pair plus the y
+// pair, plus the z pair, added with one fma), so pi_n keeps k_sync_pi's bits.
+// t points at the site in its plane tile (row length TW); the column's plane
+// z - R + j is zr[(h + j) % W].
+template <typename T, int R, int W, int TW>
+__device__ __forceinline__ void tile_stencil(const typename Cplx<T>::type *t, const typename Cplx<T>::type (&zr)[W],
+                                             int h, T &L1, T &L2) {
+    const auto &ctr = zr[(h + R) % W];
+    T a1 = (T)stencil_coef(R - 1, 3, 0) * ctr.x, a2 = (T)stencil_coef(R - 1, 3, 0) * ctr.y;
+#pragma unroll
+    for (int l = 1; l <= R; ++l) {
+        const auto xm = t[-l], xp = t[l], ym = t[-l * TW], yp = t[l * TW];
+        const auto &zm = zr[(h + R - l) % W], &zp = zr[(h + R + l) % W];
+        T s1 = (xm.x + xp.x) + (ym.x + yp.x), s2 = (xm.y + xp.y) + (ym.y + yp.y);
+        s1 = s1 + (zm.x + zp.x);
+        s2 = s2 + (zm.y + zp.y);
+        const T cl = (T)stencil_coef(R - 1, 3, l);
+        a1 = fma(cl, s1, a1);
+        a2 = fma(cl, s2, a2);
+    }
+    L1 = a1;
+    L2 = a2;
+}
+
+// k_axion_zcol for the radius-R stencils. The column's register ring holds
+// W = 2R + 2 psi planes: at site z, planes z-R .. z+R+1; once plane z-R has
+// served the stencil, plane z+R+2 is loaded into its slot, so each column
+// value is in flight for over a site. The march runs W sites per trip (the
+// ring's period) so the ring never moves between registers (a move would
+// wait for the load just issued); N and W are even, so pih's two-slot ring
+// also returns to its start. 20 B per site from DRAM as for radius 1, against
+// 44 B and per-site 64-bit index arithmetic through k_sync_pi and scratch.
+// Threads past the lattice's edge take part in the staging and barriers
+// only. N > 2R, so z + R + 2 < 2N.
+template <typename T, int R>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_axion_zcol_r(const typename Cplx<T>::type *__restrict__ psi,
+                                                         const typename Cplx<T>::type *__restrict__ pih,
+                                                         T *__restrict__ dst, const double *clock, int N, double dt,
+                                                         double inv_dx2, double lambda, double T0sq3, int prs,
+                                                         int fresh, double tau) {
+    typedef typename Cplx<T>::type C;
+    typedef ZTile<T, R> Tile;
+    constexpr int W = 2 * R + 2, A = ZT_AHEAD;
+    __shared__ __align__(16) C tiles[A + 1][Tile::E];
+    const int nbx = (N + 31) / 32, bx0 = (int)(blockIdx.x % nbx) * 32, by0 = (int)(blockIdx.x / nbx) * 8;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, x = bx0 + tx, y = by0 + ty;
+    const bool active = x < N && y < N;
+    const Tile tile(bx0, by0, N);
+    const int64_t NN = (int64_t)N * N, len = NN * N;
+#pragma unroll
+    for (int a = 0; a < A; ++a) {
+        tile.issue(psi + a * NN, tiles[a]);
+        cp_async_commit();
+    }
+    const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs, 0);
+    const T itau = (T)(1.0 / tau);
+    const int col = active ? y * N + x : 0;
+    const int cidx = (ty + R) * Tile::TW + tx + R;
+    C zr[W];   // at a trip's start z0: zr[j] = plane z0 - R + j
+#pragma unroll
+    for (int j = 0; j < W; ++j) zr[j] = psi[(int64_t)(j < R ? j - R + N : j - R) * NN + col];
+    C pr[2] = {pih[col], pih[NN + col]};   // planes z0, z0 + 1
+    const C *sn = psi + (int64_t)(R + 2) * NN + col, *p2 = pih + 2 * NN + col, *pa = psi + A * NN;
+    T *out = dst + col;
+    int slot = 0;
+    for (int z0 = 0; z0 < N; z0 += W) {
+#pragma unroll
+        for (int h = 0; h < W; ++h) {
+            const int z = z0 + h;
+            if (z < N) {   // uniform over the block
+                cp_async_wait<A - 1>();   // this thread's copies of plane z are in
+                __syncthreads();          // everyone's are; slot (z - 1) is no longer read
+                tile.issue(z + A < N ? pa : pa - len, tiles[slot == 0 ? A : slot - 1]);
+                cp_async_commit();
+                pa += NN;
+                if (active) {
+                    C p = pr[h & 1];
+                    const C ctr = zr[(h + R) % W];
+                    if (!fresh) {   // a fresh state holds pi_0 itself (the reference's ker is zero)
+                        T L1, L2;
+                        tile_stencil<T, R, W, Tile::TW>(&tiles[slot][cidx], zr, h, L1, L2);
+                        sync_pi_site<T>(ctr.x, ctr.y, L1, L2, p.x, p.y, c);
+                    }
+                    zr[h] = *(z + R + 2 < N ? sn : sn - len);
+                    pr[h & 1] = *(z + 2 < N ? p2 : p2 - len);
+                    *out = axion_f<T>(ctr.x, ctr.y, p.x, p.y, itau);
+                }
+                out += NN;
+                sn += NN;
+                p2 += NN;
+                slot = slot == A ? 0 : slot + 1;
+            }
+        }
+    }
+    cp_async_wait<0>();
+}
+
+// The axion field of a 3D finite-difference lattice into fft_in, by the
+// z-column kernel of its stencil radius.
+template <typename T>
+static void axion_zcol_t(Lattice *L) {
+    typedef typename Cplx<T>::type C;
+    const axs_params &p = L->p;
+    const int N = p.N;
+    const double dx = p.space_step, T0 = p.T_initial;
+    const C *f = (const C *)L->psi[L->cur], *q = (const C *)L->pih;
+    T *dst = (T *)L->fft_in;
+    const double *clk = L->dclock + L->cur;
+    const double dt = p.time_step, idx2 = 1.0 / (dx * dx), la = p.lambda, t3 = (T0 * T0) / 3.0;
+    const dim3 grid((N + 31) / 32, (N + 7) / 8), block(32, 8);
+    const int g = (int)(grid.x * grid.y);
+    switch (p.stencil_setting) {
+    case 0: k_axion_zcol<T><<<grid, block, 0, L->stream>>>(f, q, dst, clk, N, dt, idx2, la, t3, p.prs, L->fresh, L->tau); break;
+    case 1: k_axion_zcol_r<T, 2><<<g, 256, 0, L->stream>>>(f, q, dst, clk, N, dt, idx2, la, t3, p.prs, L->fresh, L->tau); break;
+    case 2: k_axion_zcol_r<T, 3><<<g, 256, 0, L->stream>>>(f, q, dst, clk, N, dt, idx2, la, t3, p.prs, L->fresh, L->tau); break;
+    default: k_axion_zcol_r<T, 4><<<g, 256, 0, L->stream>>>(f, q, dst, clk, N, dt, idx2, la, t3, p.prs, L->fresh, L->tau); break;
+    }
+}
+
 static void ensure_fft(Lattice *L) {
     if (L->have_plan) return;
     int N = L->p.N;
@@ -1564,19 +1732,9 @@ static AxionPending axion_spectrum_enqueue(Lattice *L, int nbins, double *host, 
     if (nbins < 1) fail(AXS_ERR_ARG, "nbins must be >= 1");
     if (L->p.form != 0) fail(AXS_ERR_STATE, "the axion kinetic spectrum is defined on the field-rescaled variables (form 0)");
     ensure_fft(L);
-    if (L->p.NDIMS == 3 && L->p.stencil_setting == 0 && L->p.laplacian == 0) {
-        const axs_params &p = L->p;
-        const int N = p.N;
-        const double dx = p.space_step, T0 = p.T_initial;
-        dim3 grid((N + 31) / 32, (N + 7) / 8), block(32, 8);
-        if (L->esz == 4)
-            k_axion_zcol<float><<<grid, block, 0, L->stream>>>(
-                (const float2 *)L->psi[L->cur], (const float2 *)L->pih, (float *)L->fft_in, L->dclock + L->cur, N,
-                (double)p.time_step, 1.0 / (dx * dx), (double)p.lambda, (T0 * T0) / 3.0, p.prs, L->fresh, L->tau);
-        else
-            k_axion_zcol<double><<<grid, block, 0, L->stream>>>(
-                (const double2 *)L->psi[L->cur], (const double2 *)L->pih, (double *)L->fft_in, L->dclock + L->cur, N,
-                (double)p.time_step, 1.0 / (dx * dx), (double)p.lambda, (T0 * T0) / 3.0, p.prs, L->fresh, L->tau);
+    if (L->p.NDIMS == 3 && L->p.laplacian == 0) {
+        if (L->esz == 4) axion_zcol_t<float>(L);
+        else axion_zcol_t<double>(L);
     } else {
         launch_sync_pi(L);
         int g = grid_cap(L->length, 256, 16);
@@ -1992,6 +2150,103 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_energies_zcol(c
     block_reduce_store<K>(v, partials);
 }
 
+// k_energies_zcol for the radius-R stencils (R = 2..4), with k_axion_zcol_r's
+// march: the column's W-plane register ring, W sites per trip, the in-plane
+// neighbours from the staged plane tiles (x+1 and y+1 of the gradient are
+// the stencil's distance-1 neighbours, z+1 the next ring plane). Two sites'
+// terms go into one compensated add, as in k_energies_zcol. 16 B from DRAM
+// per site.
+template <typename T, int R>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_energies_zcol_r(const typename Cplx<T>::type *__restrict__ psi,
+                                                            const typename Cplx<T>::type *__restrict__ pih,
+                                                            double *__restrict__ partials, const double *clock, int N,
+                                                            double dt, double inv_dx2, double lambda, double T0sq3,
+                                                            int prs, int form, int fresh, double tau, double dx,
+                                                            double lam_eff) {
+    typedef typename Cplx<T>::type C;
+    typedef ZTile<T, R> Tile;
+    constexpr int K = 3, W = 2 * R + 2, A = ZT_AHEAD;
+    __shared__ __align__(16) C tiles[A + 1][Tile::E];
+    Acc<T> acc[K];
+    const int nbx = (N + 31) / 32, bx0 = (int)(blockIdx.x % nbx) * 32, by0 = (int)(blockIdx.x / nbx) * 8;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, x = bx0 + tx, y = by0 + ty;
+    const bool active = x < N && y < N;
+    const Tile tile(bx0, by0, N);
+    const int64_t NN = (int64_t)N * N, len = NN * N;
+#pragma unroll
+    for (int a = 0; a < A; ++a) {
+        tile.issue(psi + a * NN, tiles[a]);
+        cp_async_commit();
+    }
+    const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs, form);
+    const T it = (T)(1.0 / tau), it2 = (T)(1.0 / (tau * tau));
+    const int col = active ? y * N + x : 0;
+    const int cidx = (ty + R) * Tile::TW + tx + R;
+    C zr[W];   // at a trip's start z0: zr[j] = plane z0 - R + j
+#pragma unroll
+    for (int j = 0; j < W; ++j) zr[j] = psi[(int64_t)(j < R ? j - R + N : j - R) * NN + col];
+    C pr[2] = {pih[col], pih[NN + col]};   // planes z0, z0 + 1
+    const C *sn = psi + (int64_t)(R + 2) * NN + col, *p2 = pih + 2 * NN + col, *pa = psi + A * NN;
+    int slot = 0;
+    T t[K];
+    for (int z0 = 0; z0 < N; z0 += W) {
+#pragma unroll
+        for (int h = 0; h < W; ++h) {
+            const int z = z0 + h;
+            if (z < N) {   // uniform over the block
+                cp_async_wait<A - 1>();   // this thread's copies of plane z are in
+                __syncthreads();          // everyone's are; slot (z - 1) is no longer read
+                tile.issue(z + A < N ? pa : pa - len, tiles[slot == 0 ? A : slot - 1]);
+                cp_async_commit();
+                pa += NN;
+                if ((h & 1) == 0) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) t[k] = 0;
+                }
+                if (active) {
+                    const C *ts = &tiles[slot][cidx];
+                    C p = pr[h & 1];
+                    const C zc = zr[(h + R) % W], zp = zr[(h + R + 1) % W];
+                    if (!fresh) {   // a fresh state holds pi_0 itself (the reference's ker is zero)
+                        T L1, L2;
+                        tile_stencil<T, R, W, Tile::TW>(ts, zr, h, L1, L2);
+                        sync_pi_site<T>(zc.x, zc.y, L1, L2, p.x, p.y, c);
+                    }
+                    zr[h] = *(z + R + 2 < N ? sn : sn - len);
+                    pr[h & 1] = *(z + 2 < N ? p2 : p2 - len);
+                    const C b = ts[1], e = ts[Tile::TW];   // differences in the order x, y, z
+                    const T e1 = fma(-zc.x, it, p.x), e2 = fma(-zc.y, it, p.y);
+                    t[0] += fma(e1, e1, e2 * e2);
+                    T g1 = b.x - zc.x, g2 = b.y - zc.y;
+                    T g = fma(g1, g1, g2 * g2);
+                    g1 = e.x - zc.x;
+                    g2 = e.y - zc.y;
+                    g = fma(g1, g1, fma(g2, g2, g));
+                    g1 = zp.x - zc.x;
+                    g2 = zp.y - zc.y;
+                    t[1] += fma(g1, g1, fma(g2, g2, g));
+                    const T r = fma(it2, fma(zc.x, zc.x, zc.y * zc.y), (T)-1);
+                    t[2] += r * r;
+                }
+                if (h & 1) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) acc[k].add(t[k]);
+                }
+                sn += NN;
+                p2 += NN;
+                slot = slot == A ? 0 : slot + 1;
+            }
+        }
+    }
+    cp_async_wait<0>();
+    double v[K];
+    for (int k = 0; k < K; ++k) v[k] = acc[k].value();
+    v[0] *= 0.5 / (tau * tau);
+    v[1] *= 0.5 / (tau * tau * dx * dx);
+    v[2] *= 0.25 * lam_eff;
+    block_reduce_store<K>(v, partials);
+}
+
 template <typename T>
 __global__ void k_finite(const T *__restrict__ a, int64_t n, int *flag) {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -2011,10 +2266,24 @@ static double *ensure_partials(Lattice *L, int nblocks, int K) {
     return L->dpartials;
 }
 
-// The z-column energies serve 3D lattices with the radius-1 finite-difference
-// Laplacian; the others form pi_n in scratch first.
-static bool energies_zcol(const Lattice *L) {
-    return L->p.NDIMS == 3 && L->p.stencil_setting == 0 && L->p.laplacian == 0;
+// The z-column energies serve 3D lattices with a finite-difference Laplacian
+// (any radius); 2D and the spectral Laplacian form pi_n in scratch first.
+static bool energies_zcol(const Lattice *L) { return L->p.NDIMS == 3 && L->p.laplacian == 0; }
+
+template <typename T>
+static void energies_zcol_t(Lattice *L, double *part, int g, double lam) {
+    typedef typename Cplx<T>::type C;
+    const axs_params &p = L->p;
+    const double dx = p.space_step, T0 = p.T_initial;
+    const C *f = (const C *)L->psi[L->cur], *q = (const C *)L->pih;
+    const double *clk = L->dclock + L->cur;
+    const double dt = p.time_step, idx2 = 1.0 / (dx * dx), la = p.lambda, t3 = (T0 * T0) / 3.0;
+    switch (p.stencil_setting) {
+    case 0: k_energies_zcol<T><<<g, 256, 0, L->stream>>>(f, q, part, clk, p.N, dt, idx2, la, t3, p.prs, p.form, L->fresh, L->tau, dx, lam); break;
+    case 1: k_energies_zcol_r<T, 2><<<g, 256, 0, L->stream>>>(f, q, part, clk, p.N, dt, idx2, la, t3, p.prs, p.form, L->fresh, L->tau, dx, lam); break;
+    case 2: k_energies_zcol_r<T, 3><<<g, 256, 0, L->stream>>>(f, q, part, clk, p.N, dt, idx2, la, t3, p.prs, p.form, L->fresh, L->tau, dx, lam); break;
+    default: k_energies_zcol_r<T, 4><<<g, 256, 0, L->stream>>>(f, q, part, clk, p.N, dt, idx2, la, t3, p.prs, p.form, L->fresh, L->tau, dx, lam); break;
+    }
 }
 static int zcol_blocks(int N) { return ((N + 31) / 32) * ((N + 7) / 8); }
 
@@ -2055,20 +2324,10 @@ void energies(Lattice *L, double out[3]) {
     int g;
     double *part;
     if (energies_zcol(L)) {
-        const axs_params &p = L->p;
-        const double T0 = p.T_initial;
-        g = zcol_blocks(p.N);
+        g = zcol_blocks(L->p.N);
         part = ensure_partials(L, g, 3);
-        if (L->esz == 4)
-            k_energies_zcol<float><<<g, 256, 0, L->stream>>>(
-                (const float2 *)L->psi[L->cur], (const float2 *)L->pih, part, L->dclock + L->cur, p.N,
-                (double)p.time_step, 1.0 / (dx * dx), (double)p.lambda, (T0 * T0) / 3.0, p.prs, p.form, L->fresh,
-                L->tau, dx, lam);
-        else
-            k_energies_zcol<double><<<g, 256, 0, L->stream>>>(
-                (const double2 *)L->psi[L->cur], (const double2 *)L->pih, part, L->dclock + L->cur, p.N,
-                (double)p.time_step, 1.0 / (dx * dx), (double)p.lambda, (T0 * T0) / 3.0, p.prs, p.form, L->fresh,
-                L->tau, dx, lam);
+        if (L->esz == 4) energies_zcol_t<float>(L, part, g, lam);
+        else energies_zcol_t<double>(L, part, g, lam);
     } else {
         launch_sync_pi(L);
         g = reduce_grid(L->length);

@@ -13,7 +13,10 @@ pytestmark = pytest.mark.gpu
     (3, 20, 0, 15, 1, 0),    # columns past the edge of the 32 x 8 blocks
     (3, 36, 0, 9, 0, 0),
     (3, 32, 0, 0, 1, 0),     # a fresh state: pih holds pi_0
-    (3, 24, 1, 15, 1, 0),    # radius 2: the energies form pi_n in scratch first
+    (3, 24, 1, 15, 1, 0),    # radius 2..4: the z-column march of that radius
+    (3, 24, 2, 15, 1, 0),
+    (3, 20, 3, 9, 0, 0),     # radius 4, columns past the edge of the blocks
+    (3, 24, 3, 0, 1, 0),     # radius 4, fresh
     (3, 16, 0, 6, 1, 1),     # spectral Laplacian
     (2, 48, 3, 12, 1, 0),    # radius 4 in 2D
 ])

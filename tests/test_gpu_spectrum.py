@@ -42,9 +42,12 @@ def test_powerspec_fp32(axs, oracle):
     assert rel(pk[ok], pko[ok]) <= 1e-5
 
 
-@pytest.mark.parametrize("nd,N,nbins", [(3, 32, 16), (3, 48, 128), (2, 64, 32)])
-def test_axion_spectrum_matches_oracle(axs, oracle, nd, N, nbins):
-    p = params(axs, nd, N, 64, T_initial=0.0)
+@pytest.mark.parametrize("nd,N,nbins,stencil", [(3, 32, 16, 0), (3, 48, 128, 0), (2, 64, 32, 0),
+                                                (3, 40, 32, 1), (3, 24, 16, 2), (3, 36, 24, 3), (2, 48, 16, 3)])
+def test_axion_spectrum_matches_oracle(axs, oracle, nd, N, nbins, stencil):
+    """3D finite-difference stencils of every radius form pi_n in the z-column
+    march; 2D forms it in scratch first."""
+    p = params(axs, nd, N, 64, T_initial=0.0, stencil_setting=stencil)
     op = orc(p)
     f = oracle.init_flat(op, 2, 2.0)
     with axs.Lattice(p) as L:
@@ -60,10 +63,10 @@ def test_axion_spectrum_matches_oracle(axs, oracle, nd, N, nbins):
     assert rel(k[ok], ko[ok]) <= 1e-12
 
 
-@pytest.mark.parametrize("N,nbins", [(40, 24), (32, 16)])
-def test_axion_spectrum_fresh_state(axs, oracle, N, nbins):
+@pytest.mark.parametrize("N,nbins,stencil", [(40, 24, 0), (32, 16, 0), (40, 24, 3)])
+def test_axion_spectrum_fresh_state(axs, oracle, N, nbins, stencil):
     """Right after an upload the momentum is pi_0 itself (no stencil term)."""
-    p = params(axs, 3, N, 64, T_initial=0.0)
+    p = params(axs, 3, N, 64, T_initial=0.0, stencil_setting=stencil)
     op = orc(p)
     f = oracle.init_flat(op, 5, 2.0)
     with axs.Lattice(p) as L:
