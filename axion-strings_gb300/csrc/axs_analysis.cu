@@ -1362,15 +1362,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_axion_zcol(cons
 
 // ---- z-column kernels for the radius-R stencils (R = 2..4)
 //
-// A block marches 32 x 8 columns through z. Each thread keeps its column's
-// psi in a register ring for the z-neighbours, as the radius-1 kernels do,
-// while the in-plane neighbours at distances 1..R come from a shared-memory
-// copy of the block's plane tile with an R-wide periodic halo. The tiles are
-// staged by cp.async (8 or 16 B per element, no registers held) ZT_AHEAD
-// planes ahead in a ring of ZT_AHEAD + 1 slots, with one block barrier per
-// site. Reading 4R neighbours per site straight from global memory left the
-// warps waiting on L1/L2 latency (about a third of the DRAM rate at R = 4).
-constexpr int ZT_AHEAD = 2;
+// A block marches 32 x 8 columns through z with every load from DRAM staged
+// by cp.async into shared memory, so the loads in flight hold no registers:
+// per plane, the block's psi tile with an R-wide periodic halo (the in-plane
+// neighbours) and its own pih values, in rings of S = A + 1 slots issued A
+// planes ahead, with one block barrier per site. Each thread keeps its
+// column's psi in a register ring for the z-neighbours, filled from the
+// staged tiles R + 1 planes ahead. Reading the 4R in-plane neighbours from
+// global memory left the warps waiting on L1/L2 latency, and register-held
+// column loads could keep too few bytes in flight for the DRAM rate.
 
 __device__ __forceinline__ void cp_async_ca(uint32_t dst, const void *src, int bytes) {
     if (bytes == 16) asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
@@ -1380,31 +1380,53 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int P>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(P) : "memory"); }
 
-// One block's plane tile: (8 + 2R) rows of (32 + 2R) elements, the block's
-// columns with their periodic halo. Thread t copies elements t, t + 256, ...
+// Geometry of the radius-R march. A plane tile is TH = 8 + 2R rows of
+// TW = 32 + 2RX elements (the block's columns and their periodic halo);
+// float tiles are copied in 16-byte pairs, so their x halo RX is R rounded
+// up to even (N is even, so a pair never straddles the periodic edge).
 template <typename T, int R>
-struct ZTile {
+struct ZMarch {
     typedef typename Cplx<T>::type C;
-    static constexpr int TW = 32 + 2 * R, TH = 8 + 2 * R, E = TW * TH, PER = (E + 255) / 256;
-    int goff[PER];   // the elements' offsets within a plane, -1 past the tile
-    __device__ __forceinline__ ZTile(int bx0, int by0, int N) {
+    static constexpr int VEC = sizeof(T) == 4 ? 2 : 1;           // elements per copy
+    static constexpr int RX = VEC == 2 ? (R + 1) & ~1 : R;
+    static constexpr int TW = 32 + 2 * RX, TH = 8 + 2 * R, E = TW * TH, NCP = E / VEC, PER = (NCP + 255) / 256;
+    static constexpr int A = R + 2 + (sizeof(T) == 4 ? 2 : 0);   // planes staged ahead
+    static constexpr int S = A + 1;                               // ring slots
+    static constexpr int W = 2 * R + 2;                           // register ring (planes z-R-1 .. z+R)
+    static constexpr size_t SMEM = (size_t)S * (E + 256) * sizeof(C);
+    static constexpr int MINB = sizeof(T) == 8 ? 2 : (R == 4 ? 3 : 4);   // blocks per SM the smem allows
+};
+
+// The copies one thread makes of each plane: tile copies t, t + 256, ...
+// (offsets within a plane, -1 past the tile) and its own pih value.
+template <typename T, int R>
+struct ZStage {
+    typedef ZMarch<T, R> M;
+    typedef typename M::C C;
+    int goff[M::PER];
+    __device__ __forceinline__ ZStage(int bx0, int by0, int N) {
 #pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            const int e = (int)threadIdx.x + 256 * k;
+        for (int k = 0; k < M::PER; ++k) {
+            const int q = (int)threadIdx.x + 256 * k, e = q * M::VEC;
             goff[k] = -1;
-            if (e < E) {
-                int gx = (bx0 - R + e % TW) % N, gy = (by0 - R + e / TW) % N;
+            if (q < M::NCP) {
+                int gx = (bx0 - M::RX + e % M::TW) % N, gy = (by0 - R + e / M::TW) % N;
                 if (gx < 0) gx += N;
                 if (gy < 0) gy += N;
                 goff[k] = gy * N + gx;
             }
         }
     }
-    // copy plane `plane` (a pointer to its first element) into `slot`
-    __device__ __forceinline__ void issue(const C *plane, C *slot) const {
+    // stage the plane at element offset po into ring slot s
+    __device__ __forceinline__ void issue(const C *psi, const C *pih, int64_t po, int s, C *tiles, C *pown,
+                                          bool active, int col) const {
+        C *slot = tiles + s * M::E;
 #pragma unroll
-        for (int k = 0; k < PER; ++k)
-            if (goff[k] >= 0) cp_async_ca(smem_u32(slot + threadIdx.x + 256 * k), plane + goff[k], (int)sizeof(C));
+        for (int k = 0; k < M::PER; ++k)
+            if (goff[k] >= 0)
+                cp_async_ca(smem_u32(slot + ((int)threadIdx.x + 256 * k) * M::VEC), psi + po + goff[k],
+                            (int)(M::VEC * sizeof(C)));
+        if (active) cp_async_ca(smem_u32(pown + s * 256 + threadIdx.x), pih + po + col, (int)sizeof(C));
     }
 };
 
@@ -1412,16 +1434,16 @@ struct ZTile {
 // order (coefficient 0 times the centre; per distance l the x pair plus the y
 // pair, plus the z pair, added with one fma), so pi_n keeps k_sync_pi's bits.
 // t points at the site in its plane tile (row length TW); the column's plane
-// z - R + j is zr[(h + j) % W].
+// z + d is zr[(g + d) % W].
 template <typename T, int R, int W, int TW>
 __device__ __forceinline__ void tile_stencil(const typename Cplx<T>::type *t, const typename Cplx<T>::type (&zr)[W],
-                                             int h, T &L1, T &L2) {
-    const auto &ctr = zr[(h + R) % W];
+                                             int g, T &L1, T &L2) {
+    const auto &ctr = zr[g % W];
     T a1 = (T)stencil_coef(R - 1, 3, 0) * ctr.x, a2 = (T)stencil_coef(R - 1, 3, 0) * ctr.y;
 #pragma unroll
     for (int l = 1; l <= R; ++l) {
         const auto xm = t[-l], xp = t[l], ym = t[-l * TW], yp = t[l * TW];
-        const auto &zm = zr[(h + R - l) % W], &zp = zr[(h + R + l) % W];
+        const auto &zm = zr[(g + W - l) % W], &zp = zr[(g + l) % W];
         T s1 = (xm.x + xp.x) + (ym.x + yp.x), s2 = (xm.y + xp.y) + (ym.y + yp.y);
         s1 = s1 + (zm.x + zp.x);
         s2 = s2 + (zm.y + zp.y);
@@ -1433,77 +1455,91 @@ __device__ __forceinline__ void tile_stencil(const typename Cplx<T>::type *t, co
     L2 = a2;
 }
 
-// k_axion_zcol for the radius-R stencils. The column's register ring holds
-// W = 2R + 2 psi planes: at site z, planes z-R .. z+R+1; once plane z-R has
-// served the stencil, plane z+R+2 is loaded into its slot, so each column
-// value is in flight for over a site. The march runs W sites per trip (the
-// ring's period) so the ring never moves between registers (a move would
-// wait for the load just issued); N and W are even, so pih's two-slot ring
-// also returns to its start. 20 B per site from DRAM as for radius 1, against
-// 44 B and per-site 64-bit index arithmetic through k_sync_pi and scratch.
-// Threads past the lattice's edge take part in the staging and barriers
-// only. N > 2R, so z + R + 2 < 2N.
-template <typename T, int R>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_axion_zcol_r(const typename Cplx<T>::type *__restrict__ psi,
-                                                         const typename Cplx<T>::type *__restrict__ pih,
-                                                         T *__restrict__ dst, const double *clock, int N, double dt,
-                                                         double inv_dx2, double lambda, double T0sq3, int prs,
-                                                         int fresh, double tau) {
-    typedef typename Cplx<T>::type C;
-    typedef ZTile<T, R> Tile;
-    constexpr int W = 2 * R + 2, A = ZT_AHEAD;
-    __shared__ __align__(16) C tiles[A + 1][Tile::E];
+// The march itself, shared by the radius-R axion field and energies: for
+// each site of the thread's column (threads past the lattice's edge take part
+// in the staging and barriers only) it forms pi_n with k_sync_pi's
+// arithmetic and calls site(h, z, zc, zp, p, t): the site's psi, psi of plane
+// z + 1, pi_n and its place in the staged tile. The register ring holds
+// planes z-R-1 .. z+R at site z; plane z+R+1 replaces plane z-R-1 from the
+// staged tile, so the ring has period W and the march runs W sites per trip
+// (no register moves). N > 2R and A <= 2R + 2 <= N, so a plane index past
+// the end wraps with one subtraction.
+template <typename T, int R, class Site>
+__device__ __forceinline__ void zcol_march(const typename Cplx<T>::type *__restrict__ psi,
+                                           const typename Cplx<T>::type *__restrict__ pih, int N, int fresh,
+                                           const StepCoefs<T> &c, Site &&site) {
+    typedef ZMarch<T, R> M;
+    typedef typename M::C C;
+    constexpr int W = M::W, A = M::A, S = M::S;
+    extern __shared__ __align__(16) unsigned char zsm[];
+    C *tiles = reinterpret_cast<C *>(zsm), *pown = tiles + S * M::E;
     const int nbx = (N + 31) / 32, bx0 = (int)(blockIdx.x % nbx) * 32, by0 = (int)(blockIdx.x / nbx) * 8;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, x = bx0 + tx, y = by0 + ty;
     const bool active = x < N && y < N;
-    const Tile tile(bx0, by0, N);
+    const int col = active ? y * N + x : 0;
+    const ZStage<T, R> st(bx0, by0, N);
     const int64_t NN = (int64_t)N * N, len = NN * N;
 #pragma unroll
     for (int a = 0; a < A; ++a) {
-        tile.issue(psi + a * NN, tiles[a]);
+        st.issue(psi, pih, a * NN, a, tiles, pown, active, col);
         cp_async_commit();
     }
-    const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs, 0);
-    const T itau = (T)(1.0 / tau);
-    const int col = active ? y * N + x : 0;
-    const int cidx = (ty + R) * Tile::TW + tx + R;
-    C zr[W];   // at a trip's start z0: zr[j] = plane z0 - R + j
+    C zr[W];   // at a trip's start z0: zr[j] = plane z0 - R - 1 + j
 #pragma unroll
-    for (int j = 0; j < W; ++j) zr[j] = psi[(int64_t)(j < R ? j - R + N : j - R) * NN + col];
-    C pr[2] = {pih[col], pih[NN + col]};   // planes z0, z0 + 1
-    const C *sn = psi + (int64_t)(R + 2) * NN + col, *p2 = pih + 2 * NN + col, *pa = psi + A * NN;
-    T *out = dst + col;
-    int slot = 0;
+    for (int j = 1; j < W; ++j) zr[j] = psi[(int64_t)(j <= R ? j - R - 1 + N : j - R - 1) * NN + col];
+    zr[0] = zr[1];   // plane -R-1 is never read
+    const int cidx = (ty + R) * M::TW + tx + M::RX;
+    int slot = 0, rslot = R + 1;   // ring slots of planes z and z + R + 1
+    int64_t pa = A * NN;
     for (int z0 = 0; z0 < N; z0 += W) {
 #pragma unroll
         for (int h = 0; h < W; ++h) {
             const int z = z0 + h;
             if (z < N) {   // uniform over the block
-                cp_async_wait<A - 1>();   // this thread's copies of plane z are in
-                __syncthreads();          // everyone's are; slot (z - 1) is no longer read
-                tile.issue(z + A < N ? pa : pa - len, tiles[slot == 0 ? A : slot - 1]);
+                cp_async_wait<A - R - 2>();   // this thread's copies of planes <= z + R + 1 are in
+                __syncthreads();              // everyone's are; slot (z - 1) is no longer read
+                st.issue(psi, pih, z + A < N ? pa : pa - len, slot == 0 ? A : slot - 1, tiles, pown, active, col);
                 cp_async_commit();
                 pa += NN;
                 if (active) {
-                    C p = pr[h & 1];
-                    const C ctr = zr[(h + R) % W];
+                    const C *ts = tiles + slot * M::E + cidx;
+                    zr[h] = tiles[rslot * M::E + cidx];   // plane z + R + 1 over plane z - R - 1
+                    C p = pown[slot * 256 + threadIdx.x];
+                    const C zc = zr[(h + R + 1) % W], zp = zr[(h + R + 2) % W];
                     if (!fresh) {   // a fresh state holds pi_0 itself (the reference's ker is zero)
                         T L1, L2;
-                        tile_stencil<T, R, W, Tile::TW>(&tiles[slot][cidx], zr, h, L1, L2);
-                        sync_pi_site<T>(ctr.x, ctr.y, L1, L2, p.x, p.y, c);
+                        tile_stencil<T, R, W, M::TW>(ts, zr, h + R + 1, L1, L2);
+                        sync_pi_site<T>(zc.x, zc.y, L1, L2, p.x, p.y, c);
                     }
-                    zr[h] = *(z + R + 2 < N ? sn : sn - len);
-                    pr[h & 1] = *(z + 2 < N ? p2 : p2 - len);
-                    *out = axion_f<T>(ctr.x, ctr.y, p.x, p.y, itau);
+                    site(h, z, zc, zp, p, ts);
                 }
-                out += NN;
-                sn += NN;
-                p2 += NN;
                 slot = slot == A ? 0 : slot + 1;
+                rslot = rslot == A ? 0 : rslot + 1;
             }
         }
     }
     cp_async_wait<0>();
+}
+
+// k_axion_zcol for the radius-R stencils: 20 B per site from DRAM as for
+// radius 1, against 44 B and per-site 64-bit index arithmetic through
+// k_sync_pi and scratch.
+template <typename T, int R>
+__global__ void __launch_bounds__(256, (ZMarch<T, R>::MINB)) k_axion_zcol_r(const typename Cplx<T>::type *__restrict__ psi,
+                                                                 const typename Cplx<T>::type *__restrict__ pih,
+                                                                 T *__restrict__ dst, const double *clock, int N,
+                                                                 double dt, double inv_dx2, double lambda,
+                                                                 double T0sq3, int prs, int fresh, double tau) {
+    typedef typename Cplx<T>::type C;
+    const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs, 0);
+    const T itau = (T)(1.0 / tau);
+    const int nbx = (N + 31) / 32;
+    const int x = (int)(blockIdx.x % nbx) * 32 + (threadIdx.x & 31), y = (int)(blockIdx.x / nbx) * 8 + (threadIdx.x >> 5);
+    const int64_t NN = (int64_t)N * N;
+    T *out = dst + (x < N && y < N ? y * N + x : 0);
+    zcol_march<T, R>(psi, pih, N, fresh, c, [&](int, int z, const C &zc, const C &, const C &p, const C *) {
+        out[z * NN] = axion_f<T>(zc.x, zc.y, p.x, p.y, itau);
+    });
 }
 
 // The axion field of a 3D finite-difference lattice into fft_in, by the
@@ -1520,11 +1556,15 @@ static void axion_zcol_t(Lattice *L) {
     const double dt = p.time_step, idx2 = 1.0 / (dx * dx), la = p.lambda, t3 = (T0 * T0) / 3.0;
     const dim3 grid((N + 31) / 32, (N + 7) / 8), block(32, 8);
     const int g = (int)(grid.x * grid.y);
+    auto radius = [&](auto kern, size_t smem) {
+        AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<g, 256, smem, L->stream>>>(f, q, dst, clk, N, dt, idx2, la, t3, p.prs, L->fresh, L->tau);
+    };
     switch (p.stencil_setting) {
     case 0: k_axion_zcol<T><<<grid, block, 0, L->stream>>>(f, q, dst, clk, N, dt, idx2, la, t3, p.prs, L->fresh, L->tau); break;
-    case 1: k_axion_zcol_r<T, 2><<<g, 256, 0, L->stream>>>(f, q, dst, clk, N, dt, idx2, la, t3, p.prs, L->fresh, L->tau); break;
-    case 2: k_axion_zcol_r<T, 3><<<g, 256, 0, L->stream>>>(f, q, dst, clk, N, dt, idx2, la, t3, p.prs, L->fresh, L->tau); break;
-    default: k_axion_zcol_r<T, 4><<<g, 256, 0, L->stream>>>(f, q, dst, clk, N, dt, idx2, la, t3, p.prs, L->fresh, L->tau); break;
+    case 1: radius(k_axion_zcol_r<T, 2>, ZMarch<T, 2>::SMEM); break;
+    case 2: radius(k_axion_zcol_r<T, 3>, ZMarch<T, 3>::SMEM); break;
+    default: radius(k_axion_zcol_r<T, 4>, ZMarch<T, 4>::SMEM); break;
     }
 }
 
@@ -2150,95 +2190,45 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_energies_zcol(c
     block_reduce_store<K>(v, partials);
 }
 
-// k_energies_zcol for the radius-R stencils (R = 2..4), with k_axion_zcol_r's
-// march: the column's W-plane register ring, W sites per trip, the in-plane
-// neighbours from the staged plane tiles (x+1 and y+1 of the gradient are
-// the stencil's distance-1 neighbours, z+1 the next ring plane). Two sites'
-// terms go into one compensated add, as in k_energies_zcol. 16 B from DRAM
-// per site.
+// k_energies_zcol for the radius-R stencils (R = 2..4), on k_axion_zcol_r's
+// march: x+1 and y+1 of the gradient are the stencil's distance-1 neighbours
+// in the staged tile, z+1 the next ring plane. Two sites' terms go into one
+// compensated add, as in k_energies_zcol. 16 B from DRAM per site.
 template <typename T, int R>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_energies_zcol_r(const typename Cplx<T>::type *__restrict__ psi,
-                                                            const typename Cplx<T>::type *__restrict__ pih,
-                                                            double *__restrict__ partials, const double *clock, int N,
-                                                            double dt, double inv_dx2, double lambda, double T0sq3,
-                                                            int prs, int form, int fresh, double tau, double dx,
-                                                            double lam_eff) {
+__global__ void __launch_bounds__(256, (ZMarch<T, R>::MINB)) k_energies_zcol_r(const typename Cplx<T>::type *__restrict__ psi,
+                                                                    const typename Cplx<T>::type *__restrict__ pih,
+                                                                    double *__restrict__ partials, const double *clock,
+                                                                    int N, double dt, double inv_dx2, double lambda,
+                                                                    double T0sq3, int prs, int form, int fresh,
+                                                                    double tau, double dx, double lam_eff) {
     typedef typename Cplx<T>::type C;
-    typedef ZTile<T, R> Tile;
-    constexpr int K = 3, W = 2 * R + 2, A = ZT_AHEAD;
-    __shared__ __align__(16) C tiles[A + 1][Tile::E];
+    constexpr int K = 3, TW = ZMarch<T, R>::TW;
     Acc<T> acc[K];
-    const int nbx = (N + 31) / 32, bx0 = (int)(blockIdx.x % nbx) * 32, by0 = (int)(blockIdx.x / nbx) * 8;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, x = bx0 + tx, y = by0 + ty;
-    const bool active = x < N && y < N;
-    const Tile tile(bx0, by0, N);
-    const int64_t NN = (int64_t)N * N, len = NN * N;
-#pragma unroll
-    for (int a = 0; a < A; ++a) {
-        tile.issue(psi + a * NN, tiles[a]);
-        cp_async_commit();
-    }
+    T t[K] = {0, 0, 0};
     const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs, form);
     const T it = (T)(1.0 / tau), it2 = (T)(1.0 / (tau * tau));
-    const int col = active ? y * N + x : 0;
-    const int cidx = (ty + R) * Tile::TW + tx + R;
-    C zr[W];   // at a trip's start z0: zr[j] = plane z0 - R + j
+    zcol_march<T, R>(psi, pih, N, fresh, c, [&](int h, int, const C &zc, const C &zp, const C &p, const C *ts) {
+        const C b = ts[1], e = ts[TW];   // differences in the order x, y, z
+        const T e1 = fma(-zc.x, it, p.x), e2 = fma(-zc.y, it, p.y);
+        t[0] += fma(e1, e1, e2 * e2);
+        T g1 = b.x - zc.x, g2 = b.y - zc.y;
+        T g = fma(g1, g1, g2 * g2);
+        g1 = e.x - zc.x;
+        g2 = e.y - zc.y;
+        g = fma(g1, g1, fma(g2, g2, g));
+        g1 = zp.x - zc.x;
+        g2 = zp.y - zc.y;
+        t[1] += fma(g1, g1, fma(g2, g2, g));
+        const T r = fma(it2, fma(zc.x, zc.x, zc.y * zc.y), (T)-1);
+        t[2] += r * r;
+        if (h & 1) {   // W is even, so sites pair up within a trip
 #pragma unroll
-    for (int j = 0; j < W; ++j) zr[j] = psi[(int64_t)(j < R ? j - R + N : j - R) * NN + col];
-    C pr[2] = {pih[col], pih[NN + col]};   // planes z0, z0 + 1
-    const C *sn = psi + (int64_t)(R + 2) * NN + col, *p2 = pih + 2 * NN + col, *pa = psi + A * NN;
-    int slot = 0;
-    T t[K];
-    for (int z0 = 0; z0 < N; z0 += W) {
-#pragma unroll
-        for (int h = 0; h < W; ++h) {
-            const int z = z0 + h;
-            if (z < N) {   // uniform over the block
-                cp_async_wait<A - 1>();   // this thread's copies of plane z are in
-                __syncthreads();          // everyone's are; slot (z - 1) is no longer read
-                tile.issue(z + A < N ? pa : pa - len, tiles[slot == 0 ? A : slot - 1]);
-                cp_async_commit();
-                pa += NN;
-                if ((h & 1) == 0) {
-#pragma unroll
-                    for (int k = 0; k < K; ++k) t[k] = 0;
-                }
-                if (active) {
-                    const C *ts = &tiles[slot][cidx];
-                    C p = pr[h & 1];
-                    const C zc = zr[(h + R) % W], zp = zr[(h + R + 1) % W];
-                    if (!fresh) {   // a fresh state holds pi_0 itself (the reference's ker is zero)
-                        T L1, L2;
-                        tile_stencil<T, R, W, Tile::TW>(ts, zr, h, L1, L2);
-                        sync_pi_site<T>(zc.x, zc.y, L1, L2, p.x, p.y, c);
-                    }
-                    zr[h] = *(z + R + 2 < N ? sn : sn - len);
-                    pr[h & 1] = *(z + 2 < N ? p2 : p2 - len);
-                    const C b = ts[1], e = ts[Tile::TW];   // differences in the order x, y, z
-                    const T e1 = fma(-zc.x, it, p.x), e2 = fma(-zc.y, it, p.y);
-                    t[0] += fma(e1, e1, e2 * e2);
-                    T g1 = b.x - zc.x, g2 = b.y - zc.y;
-                    T g = fma(g1, g1, g2 * g2);
-                    g1 = e.x - zc.x;
-                    g2 = e.y - zc.y;
-                    g = fma(g1, g1, fma(g2, g2, g));
-                    g1 = zp.x - zc.x;
-                    g2 = zp.y - zc.y;
-                    t[1] += fma(g1, g1, fma(g2, g2, g));
-                    const T r = fma(it2, fma(zc.x, zc.x, zc.y * zc.y), (T)-1);
-                    t[2] += r * r;
-                }
-                if (h & 1) {
-#pragma unroll
-                    for (int k = 0; k < K; ++k) acc[k].add(t[k]);
-                }
-                sn += NN;
-                p2 += NN;
-                slot = slot == A ? 0 : slot + 1;
+            for (int k = 0; k < K; ++k) {
+                acc[k].add(t[k]);
+                t[k] = 0;
             }
         }
-    }
-    cp_async_wait<0>();
+    });
     double v[K];
     for (int k = 0; k < K; ++k) v[k] = acc[k].value();
     v[0] *= 0.5 / (tau * tau);
@@ -2278,11 +2268,15 @@ static void energies_zcol_t(Lattice *L, double *part, int g, double lam) {
     const C *f = (const C *)L->psi[L->cur], *q = (const C *)L->pih;
     const double *clk = L->dclock + L->cur;
     const double dt = p.time_step, idx2 = 1.0 / (dx * dx), la = p.lambda, t3 = (T0 * T0) / 3.0;
+    auto radius = [&](auto kern, size_t smem) {
+        AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<g, 256, smem, L->stream>>>(f, q, part, clk, p.N, dt, idx2, la, t3, p.prs, p.form, L->fresh, L->tau, dx, lam);
+    };
     switch (p.stencil_setting) {
     case 0: k_energies_zcol<T><<<g, 256, 0, L->stream>>>(f, q, part, clk, p.N, dt, idx2, la, t3, p.prs, p.form, L->fresh, L->tau, dx, lam); break;
-    case 1: k_energies_zcol_r<T, 2><<<g, 256, 0, L->stream>>>(f, q, part, clk, p.N, dt, idx2, la, t3, p.prs, p.form, L->fresh, L->tau, dx, lam); break;
-    case 2: k_energies_zcol_r<T, 3><<<g, 256, 0, L->stream>>>(f, q, part, clk, p.N, dt, idx2, la, t3, p.prs, p.form, L->fresh, L->tau, dx, lam); break;
-    default: k_energies_zcol_r<T, 4><<<g, 256, 0, L->stream>>>(f, q, part, clk, p.N, dt, idx2, la, t3, p.prs, p.form, L->fresh, L->tau, dx, lam); break;
+    case 1: radius(k_energies_zcol_r<T, 2>, ZMarch<T, 2>::SMEM); break;
+    case 2: radius(k_energies_zcol_r<T, 3>, ZMarch<T, 3>::SMEM); break;
+    default: radius(k_energies_zcol_r<T, 4>, ZMarch<T, 4>::SMEM); break;
     }
 }
 static int zcol_blocks(int N) { return ((N + 31) / 32) * ((N + 7) / 8); }
