@@ -198,13 +198,53 @@ __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int
                     }
                 }
             }
+            // One vector per thread (MAXV == 1): its row, the byte offsets of its
+            // x window's vectors from the centre slot (band, strip or periodic
+            // band) and its output offset at plane za are fixed for the item,
+            // so the plane loop does no division and no branching for them.
+            constexpr int NW = (2 * K::RP + K::VS) / K::VS;   // x window [xx-RP, xx+VS+RP) in 16-byte vectors
+            // (radius 4's register ring leaves no room for these: they are
+            // formed per plane there)
+            constexpr bool HW = K::MAXV == 1 && !(K::ZREG && R >= 4);
+            int wo[HW ? NW : 1];
+            int yy1 = 0, xx1 = 0;
+            int64_t off1 = 0;
+            const bool act1 = cid < nvec;
+            const int64_t NNl = (int64_t)N * N;
+            if constexpr (HW) {
+                yy1 = act1 ? cid / nvx : 0;
+                xx1 = act1 ? (cid % nvx) * K::VS : 0;
+                const int rrow = (R + yy1) * tx;
+#pragma unroll
+                for (int kw = 0; kw < NW; ++kw) {
+                    const int pos = xx1 - K::RP + kw * K::VS;
+                    int e;   // element offset from the slot's start
+                    if (pos >= 0 && pos < tx) e = rrow + pos;
+                    else if (xhalo) e = pos < 0 ? K::C_BYTES / K::CS + yy1 * K::RP + pos + K::RP
+                                                : (K::C_BYTES + K::H_PAD) / K::CS + yy1 * K::RP + pos - tx;
+                    else e = rrow + (pos < 0 ? pos + tx : pos - tx);
+                    wo[kw] = e * K::CS;
+                }
+                off1 = ((int64_t)za * N + (y0 + yy1)) * N + (x0 + xx1);
+            }
+            // ring position of load q0 + t (plane z - R) modulo 2S, advanced per
+            // plane: the slot of load q0 + t + d is its sum with d modulo S and
+            // the load's phase whether that sum modulo 2S reaches S (no 64-bit
+            // division per plane). Slot sums stay below 3S (S >= R + 2).
+            constexpr bool POW2 = (S & (S - 1)) == 0;
+            auto wrap = [](int v) { return POW2 ? v & (S - 1) : (v >= 2 * S ? v - 2 * S : (v >= S ? v - S : v)); };
+            int rpos = (int)(q0 % (2 * S));
             for (int t = 0; t < T_steps && ok; ++t) {
-                const int64_t qn = q0 + t + 2 * R;
+                const int s_lo = wrap(rpos);
+                int hpos = rpos + 2 * R;   // load q0 + t + 2R
+                hpos = POW2 ? hpos & (2 * S - 1) : (hpos >= 2 * S ? hpos - 2 * S : hpos);
+                const int s_hi = wrap(hpos);
+                const uint32_t ph_hi = hpos >= S ? 1u : 0u;
                 int w = 0;
                 if (t == 0 && !K::ZREG)
                     for (int d = 0; d < 2 * R && !w; ++d)
                         w = warp_wait(smem_u32(&full[(q0 + d) % S]), (uint32_t)(((q0 + d) / S) & 1), abort_flag);
-                if (!w) w = warp_wait(smem_u32(&full[qn % S]), (uint32_t)((qn / S) & 1), abort_flag);
+                if (!w) w = warp_wait(smem_u32(&full[s_hi]), ph_hi, abort_flag);
                 if (w) {
                     if (w == 1 && lane == 0) { atomicOr(derr, DEVERR_TIMEOUT); *abort_flag = 1; }
                     ok = false;
@@ -213,7 +253,7 @@ __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int
                 const int z = za + t;
                 const C *Zp[2 * R + 1];   // planes z-R .. z+R (ZREG: only z and z+R are in the ring)
 #pragma unroll
-                for (int d = 0; d <= 2 * R; ++d) Zp[d] = reinterpret_cast<const C *>(smem + ((q0 + t + d) % S) * K::SLOT);
+                for (int d = 0; d <= 2 * R; ++d) Zp[d] = reinterpret_cast<const C *>(smem + wrap(s_lo + d) * K::SLOT);
                 const C *Cz = Zp[R];
                 if constexpr (K::ZREG) zr[2 * R] = *reinterpret_cast<const V *>(Zp[2 * R] + toff);
                 const C *Lh = reinterpret_cast<const C *>(reinterpret_cast<const unsigned char *>(Cz) + K::C_BYTES);
@@ -222,21 +262,32 @@ __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int
 #pragma unroll
                 for (int jv = 0; jv < K::MAXV; ++jv) {
                     const int v = cid + jv * K::NC;
-                    if (v >= nvec) continue;
-                    const int yy = v / nvx, xx = (v % nvx) * K::VS;
+                    int yy, xx;
+                    if constexpr (HW) {
+                        if (!act1) continue;
+                        yy = yy1;
+                        xx = xx1;
+                    } else {
+                        if (v >= nvec) continue;
+                        yy = v / nvx;
+                        xx = (v % nvx) * K::VS;
+                    }
                     const int rrow = (R + yy) * tx;   // the site's row in the band
                     // The x window [xx-RP, xx+VS+RP) of the site's row as 16-byte
                     // vectors: RP is a multiple of VS, so each vector comes whole
                     // from the band, a strip, or (one x tile) the periodic band.
-                    constexpr int NW = (2 * K::RP + K::VS) / K::VS;
                     C win[NW * K::VS];
 #pragma unroll
                     for (int kw = 0; kw < NW; ++kw) {
-                        const int pos = xx - K::RP + kw * K::VS;
                         const C *src;
-                        if (pos >= 0 && pos < tx) src = &Cz[rrow + pos];
-                        else if (xhalo) src = pos < 0 ? &Lh[yy * K::RP + pos + K::RP] : &Rh[yy * K::RP + pos - tx];
-                        else src = &Cz[rrow + (pos < 0 ? pos + tx : pos - tx)];
+                        if constexpr (HW) {
+                            src = reinterpret_cast<const C *>(reinterpret_cast<const unsigned char *>(Cz) + wo[kw]);
+                        } else {
+                            const int pos = xx - K::RP + kw * K::VS;
+                            if (pos >= 0 && pos < tx) src = &Cz[rrow + pos];
+                            else if (xhalo) src = pos < 0 ? &Lh[yy * K::RP + pos + K::RP] : &Rh[yy * K::RP + pos - tx];
+                            else src = &Cz[rrow + (pos < 0 ? pos + tx : pos - tx)];
+                        }
                         *reinterpret_cast<V *>(&win[kw * K::VS]) = *reinterpret_cast<const V *>(src);
                     }
                     C ctr[K::VS];
@@ -277,7 +328,7 @@ __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int
 #pragma unroll
                     for (int j = 0; j < K::VS; ++j)
                         site_update<T>(ctr[j].x, ctr[j].y, a1[j], a2[j], pv[2 * j], pv[2 * j + 1], outv[j].x, outv[j].y, cf);
-                    const int64_t off = ((int64_t)z * N + (y0 + yy)) * N + (x0 + xx);
+                    const int64_t off = HW ? off1 + (int64_t)t * NNl : ((int64_t)z * N + (y0 + yy)) * N + (x0 + xx);
                     *reinterpret_cast<V *>(&pih[off]) = *reinterpret_cast<V *>(pv);
                     *reinterpret_cast<V *>(&psi_out[off]) = *reinterpret_cast<V *>(outv);
                 }
@@ -285,19 +336,21 @@ __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int
                 // centre z, load q0+t+R); at the last plane also with the
                 // item's remaining loads
                 __syncwarp();
+                const int s_c = wrap(s_lo + R);   // load q0 + t + R (the centre)
                 if constexpr (K::ZREG) {
                     if (lane == 0) {
-                        mbar_arrive(smem_u32(&empty[(q0 + t + R) % S]));
+                        mbar_arrive(smem_u32(&empty[s_c]));
                         if (t == T_steps - 1)
-                            for (int d = 1; d <= R; ++d) mbar_arrive(smem_u32(&empty[(q0 + t + R + d) % S]));
+                            for (int d = 1; d <= R; ++d) mbar_arrive(smem_u32(&empty[wrap(s_c + d)]));
                     }
 #pragma unroll
                     for (int d = 0; d < 2 * R; ++d) zr[d] = zr[d + 1];
                 } else if (lane == 0) {
-                    mbar_arrive(smem_u32(&empty[(q0 + t) % S]));
+                    mbar_arrive(smem_u32(&empty[s_lo]));
                     if (t == T_steps - 1)
-                        for (int d = 1; d <= 2 * R; ++d) mbar_arrive(smem_u32(&empty[(q0 + t + d) % S]));
+                        for (int d = 1; d <= 2 * R; ++d) mbar_arrive(smem_u32(&empty[wrap(s_lo + d)]));
                 }
+                rpos = rpos + 1 == 2 * S ? 0 : rpos + 1;
             }
             if (!ok) break;
             q0 += T_steps + 2 * R;

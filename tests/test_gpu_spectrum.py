@@ -80,9 +80,10 @@ def test_axion_spectrum_fresh_state(axs, oracle, N, nbins, stencil):
     assert rel(k[ok], ko[ok]) <= 1e-12
 
 
-def test_axion_spectrum_fp32(axs, oracle):
+@pytest.mark.parametrize("stencil", [0, 2])
+def test_axion_spectrum_fp32(axs, oracle, stencil):
     """FP32 fields: the spectrum of the downloaded (FP32) state within 1e-4."""
-    p = params(axs, 3, 48, 32, T_initial=0.0)
+    p = params(axs, 3, 48, 32, T_initial=0.0, stencil_setting=stencil)
     op = orc(p)
     f = oracle.init_flat(op, 6, 2.0)
     with axs.Lattice(p) as L:
