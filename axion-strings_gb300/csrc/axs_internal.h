@@ -218,10 +218,11 @@ void lattice_autotune(Lattice *L);
 void ensemble_setup(Ensemble *E);
 void ensemble_evolve(Ensemble *E, int nsteps);
 void ensemble_autotune(Ensemble *E);
-// radius-R z-march kernels (axs_step_r.cu), by tile shape
-void launch_zmarch_r(int esz, int ty, int txmax, int slots, int r, const ZLat *d, int nlat, int64_t items,
+// radius-R z-march kernels (axs_step_r.cu), by tile shape; zr = 1 keeps the
+// z-neighbours in registers with a ring of 2R + 2 or more slots
+void launch_zmarch_r(int esz, int ty, int txmax, int slots, int r, int zr, const ZLat *d, int nlat, int64_t items,
                      int *counters, int parity, int *derr, cudaStream_t st, int ctas_per_sm);
-void prepare_zmarch_r(int esz, int ty, int txmax, int slots, int r);
+void prepare_zmarch_r(int esz, int ty, int txmax, int slots, int r, int zr);
 std::string ensemble_describe(const Ensemble *E);
 // ---- batched analysis over the members (axs_analysis.cu)
 void ensemble_find_strings(Ensemble *E, int64_t *nplaq, int64_t *ncores);

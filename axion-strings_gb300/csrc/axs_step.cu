@@ -1822,7 +1822,9 @@ static int grid_for(int64_t len, int threads = 256) {
 // interval runs on the gen-2 `partner` with the same tile and launch table.
 // gen 4: k_zmarch2r (stencil radius r = 2..4, axs_step_r.cu). gen 5:
 // k_zmarch_3step (three steps per pass), whose last one or two steps of an
-// interval run on its gen-3 `partner` (same tile, same launch table).
+// interval run on its gen-3 `partner` (same tile, same launch table). `lean`:
+// gen 3, the lean two-step form; gen 4, the register z-ring with a ring of
+// 2R + 2 or more slots (fewer slots always use it).
 struct ZVariant {
     int gen, ty, txmax, slots, ncw, partner, r, lean;
 };
@@ -1860,6 +1862,18 @@ static const ZVariant kZVariants[] = {
     // CTAs of eight consumer warps per SM; an interval's last one or two steps
     // run on the two-step partner (variant 30 or 39) and its one-step partner
     {5, 8, 64, 4, 8, 30, 0, 1},  {5, 16, 32, 4, 8, 39, 0, 1},
+    // 48-49: radius 2 with the z-neighbours in registers and rings of 6 and 7
+    // slots (three and four plane loads in flight per CTA; the last field,
+    // set, keeps the register ring although S >= 2R + 2)
+    {4, 4, 128, 6, 8, -1, 2, 1},  {4, 4, 128, 7, 8, -1, 2, 1},
+    // 50-55: the same deeper register rings where the slots fit two CTAs per
+    // SM: radius 2 on 4 x 128 (8 slots), radius 3 on 8 x 64 (8, 9) and 16 x 32
+    // (10), radius 4 on 16 x 32 (9, 10)
+    {4, 4, 128, 8, 8, -1, 2, 1},  {4, 8, 64, 8, 8, -1, 3, 1},  {4, 8, 64, 9, 8, -1, 3, 1},
+    {4, 16, 32, 10, 8, -1, 3, 1}, {4, 16, 32, 9, 8, -1, 4, 0}, {4, 16, 32, 10, 8, -1, 4, 1},
+    // 56-57: radius 4 on 8 x 64 with 9 slots, radius 2 on 4 x 128 with 9 (at
+    // the shared-memory limit of two CTAs per SM)
+    {4, 8, 64, 9, 8, -1, 4, 0},   {4, 4, 128, 9, 8, -1, 2, 1},
 };
 static const int kNumZVariants = sizeof(kZVariants) / sizeof(kZVariants[0]);
 
@@ -2010,7 +2024,7 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
                           int *derr, cudaStream_t st, int ctas_per_sm) {
     if (variant >= 0 && variant < kNumZVariants && kZVariants[variant].gen == 4) {
         const ZVariant &v = kZVariants[variant];
-        launch_zmarch_r(esz, v.ty, v.txmax, v.slots, v.r, d, nlat, items, counters, parity, derr, st, ctas_per_sm);
+        launch_zmarch_r(esz, v.ty, v.txmax, v.slots, v.r, v.lean, d, nlat, items, counters, parity, derr, st, ctas_per_sm);
         return;
     }
 #define AXS_ZV(I, TY, TX, S)                                                                                    \
@@ -2088,7 +2102,7 @@ static void launch_zmarch(int esz, int variant, const ZLat *d, int nlat, int64_t
 static void prepare_zmarch(int esz, int variant) {
     if (variant >= 0 && variant < kNumZVariants && kZVariants[variant].gen == 4) {
         const ZVariant &v = kZVariants[variant];
-        prepare_zmarch_r(esz, v.ty, v.txmax, v.slots, v.r);
+        prepare_zmarch_r(esz, v.ty, v.txmax, v.slots, v.r, v.lean);
         return;
     }
 #define AXS_ZP(I, TY, TX, S)                                      \
@@ -2232,7 +2246,7 @@ static int variant_tx(const ZVariant &v, int N, int esz) {
     if (esz == 8) txmax = std::min(txmax, 128);   // box inner dim: 2*tx doubles <= 256
     if (variant_smem(v, esz) > max_smem_optin()) return 0;
     if (N % v.ty != 0 || N < 4 || v.ty < radius(v)) return 0;
-    if (v.gen == 4 && v.slots < 2 * v.r + 2 && esz != 4) return 0;   // register z-ring: float fields only
+    if (v.gen == 4 && (v.lean || v.slots < 2 * v.r + 2) && esz != 4) return 0;   // register z-ring: float fields only
     for (int tx = std::min(txmax, N); tx >= vs; --tx) {
         if (N % tx) continue;
         if (tx % vs) continue;

@@ -25,7 +25,7 @@
 
 namespace axs {
 
-template <typename T, int TY, int TXMAX, int S, int R>
+template <typename T, int TY, int TXMAX, int S, int R, int ZR = 0>
 struct ZRCfg {
     static constexpr int CS = 2 * (int)sizeof(T);
     static constexpr int VS = 16 / CS;                         // sites per 16-byte vector
@@ -41,16 +41,16 @@ struct ZRCfg {
     static constexpr int SLOT = (P_OFF + TY * TXMAX * CS + 127) / 128 * 128;
     static constexpr int BAR_OFF = S * SLOT;
     static constexpr int SMEM = BAR_OFF + 256;
-    static constexpr bool ZREG = S < 2 * R + 2;                // z-neighbours in registers
+    static constexpr bool ZREG = ZR || S < 2 * R + 2;          // z-neighbours in registers (ZR: also with a deeper ring)
     static_assert(S >= (ZREG ? R + 2 : 2 * R + 2), "the ring holds the planes in use and one in flight");
     static_assert(!ZREG || (sizeof(T) == 4 && MAXV == 1), "register z-ring: float fields, one vector per thread");
     static_assert(TY >= R, "halo bands must not wrap inside a box");
 };
 
-template <typename T, int TY, int TXMAX, int S, int R>
+template <typename T, int TY, int TXMAX, int S, int R, int ZR>
 __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int nlat, int64_t total_items,
                                               int *counters, int parity, int *derr) {
-    typedef ZRCfg<T, TY, TXMAX, S, R> K;
+    typedef ZRCfg<T, TY, TXMAX, S, R, ZR> K;
     typedef typename Cplx<T>::type C;
     typedef typename Vec16<T>::type V;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -368,33 +368,33 @@ __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int
     }
 }
 
-template <typename T, int TY, int TXMAX, int S, int R>
-__global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R>::NT)
+template <typename T, int TY, int TXMAX, int S, int R, int ZR>
+__global__ void __launch_bounds__(ZRCfg<T, TY, TXMAX, S, R, ZR>::NT)
     k_zmarch2r(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity, int *derr) {
-    zmarch2r_body<T, TY, TXMAX, S, R>(lats, nlat, total_items, counters, parity, derr);
+    zmarch2r_body<T, TY, TXMAX, S, R, ZR>(lats, nlat, total_items, counters, parity, derr);
 }
 // Register z-ring: 96 registers, so that two CTAs of nine warps fit the 16K
 // registers of each SM sub-partition (at most five warps each).
-template <typename T, int TY, int TXMAX, int S, int R>
+template <typename T, int TY, int TXMAX, int S, int R, int ZR>
 __global__ void __maxnreg__(96)
     k_zmarch2r_zreg(const ZLat *__restrict__ lats, int nlat, int64_t total_items, int *counters, int parity,
                     int *derr) {
-    zmarch2r_body<T, TY, TXMAX, S, R>(lats, nlat, total_items, counters, parity, derr);
+    zmarch2r_body<T, TY, TXMAX, S, R, ZR>(lats, nlat, total_items, counters, parity, derr);
 }
-template <typename T, int TY, int TXMAX, int S, int R>
+template <typename T, int TY, int TXMAX, int S, int R, int ZR>
 static void (*zr_kernel())(const ZLat *, int, int64_t, int *, int, int *) {
-    if constexpr (ZRCfg<T, TY, TXMAX, S, R>::ZREG) return k_zmarch2r_zreg<T, TY, TXMAX, S, R>;
-    else return k_zmarch2r<T, TY, TXMAX, S, R>;
+    if constexpr (ZRCfg<T, TY, TXMAX, S, R, ZR>::ZREG) return k_zmarch2r_zreg<T, TY, TXMAX, S, R, ZR>;
+    else return k_zmarch2r<T, TY, TXMAX, S, R, ZR>;
 }
 
 // ---------------------------------------------------------------- host side
 
-template <typename T, int TY, int TXMAX, int S, int R>
+template <typename T, int TY, int TXMAX, int S, int R, int ZR>
 static int prepare_r_t() {
-    typedef ZRCfg<T, TY, TXMAX, S, R> K;
+    typedef ZRCfg<T, TY, TXMAX, S, R, ZR> K;
     static PerDevice occ;   // the attribute and occupancy belong to the device
     return occ.get([] {
-        const auto kern = zr_kernel<T, TY, TXMAX, S, R>();
+        const auto kern = zr_kernel<T, TY, TXMAX, S, R, ZR>();
         AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM));
         int o = 0;
         AXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, K::NT, K::SMEM));
@@ -403,14 +403,14 @@ static int prepare_r_t() {
     });
 }
 
-template <typename T, int TY, int TXMAX, int S, int R>
+template <typename T, int TY, int TXMAX, int S, int R, int ZR>
 static void launch_r_t(const ZLat *d, int nlat, int64_t items, int *counters, int parity, int *derr, cudaStream_t st,
                        int ctas_per_sm) {
-    typedef ZRCfg<T, TY, TXMAX, S, R> K;
-    const int occ = prepare_r_t<T, TY, TXMAX, S, R>();
+    typedef ZRCfg<T, TY, TXMAX, S, R, ZR> K;
+    const int occ = prepare_r_t<T, TY, TXMAX, S, R, ZR>();
     const int per = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ) : occ;
     const int64_t grid = std::min<int64_t>((int64_t)per * num_sms(), items);
-    zr_kernel<T, TY, TXMAX, S, R>()<<<(int)grid, K::NT, K::SMEM, st>>>(d, nlat, items, counters, parity, derr);
+    zr_kernel<T, TY, TXMAX, S, R, ZR>()<<<(int)grid, K::NT, K::SMEM, st>>>(d, nlat, items, counters, parity, derr);
     AXS_CUDA(cudaGetLastError());
     count_launches(1);
 }
@@ -426,53 +426,64 @@ static void launch_r_t(const ZLat *d, int nlat, int64_t items, int *counters, in
     X(4, 128, 10, 4)     \
     X(8, 64, 10, 4)      \
     X(4, 64, 10, 4)
-// register z-ring shapes (S < 2R + 2): float fields only
+// register z-ring shapes (S < 2R + 2, or zr = 1 for a deeper ring): float
+// fields only; (ty, txmax, slots, radius, zr)
 #define AXS_ZR_SHAPES_F(X) \
-    X(4, 128, 4, 2)        \
-    X(8, 64, 4, 2)         \
-    X(4, 128, 5, 3)        \
-    X(8, 64, 5, 3)         \
-    X(4, 128, 6, 4)        \
-    X(8, 64, 6, 4)         \
-    X(4, 128, 7, 3)        \
-    X(8, 64, 7, 3)         \
-    X(8, 64, 8, 4)         \
-    X(4, 128, 5, 2)
+    X(4, 128, 4, 2, 0)     \
+    X(8, 64, 4, 2, 0)      \
+    X(4, 128, 5, 3, 0)     \
+    X(8, 64, 5, 3, 0)      \
+    X(4, 128, 6, 4, 0)     \
+    X(8, 64, 6, 4, 0)      \
+    X(4, 128, 7, 3, 0)     \
+    X(8, 64, 7, 3, 0)      \
+    X(8, 64, 8, 4, 0)      \
+    X(4, 128, 5, 2, 0)     \
+    X(4, 128, 6, 2, 1)     \
+    X(4, 128, 7, 2, 1)     \
+    X(4, 128, 8, 2, 1)     \
+    X(8, 64, 8, 3, 1)      \
+    X(8, 64, 9, 3, 1)      \
+    X(16, 32, 10, 3, 1)    \
+    X(16, 32, 9, 4, 0)     \
+    X(16, 32, 10, 4, 1)    \
+    X(8, 64, 9, 4, 0)      \
+    X(4, 128, 9, 2, 1)
 
-void launch_zmarch_r(int esz, int ty, int txmax, int slots, int r, const ZLat *d, int nlat, int64_t items,
+void launch_zmarch_r(int esz, int ty, int txmax, int slots, int r, int zr, const ZLat *d, int nlat, int64_t items,
                      int *counters, int parity, int *derr, cudaStream_t st, int ctas_per_sm) {
-#define AXS_ZR_LAUNCH(TY, TX, S, R)                                                                         \
-    if (ty == TY && txmax == TX && slots == S && r == R) {                                                  \
-        if (esz == 4) launch_r_t<float, TY, TX, S, R>(d, nlat, items, counters, parity, derr, st, ctas_per_sm); \
-        else launch_r_t<double, TY, TX, S, R>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);         \
-        return;                                                                                             \
+#define AXS_ZR_LAUNCH(TY, TX, S, R)                                                                                 \
+    if (ty == TY && txmax == TX && slots == S && r == R && !zr) {                                                   \
+        if (esz == 4) launch_r_t<float, TY, TX, S, R, 0>(d, nlat, items, counters, parity, derr, st, ctas_per_sm); \
+        else launch_r_t<double, TY, TX, S, R, 0>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);         \
+        return;                                                                                                     \
     }
     AXS_ZR_SHAPES(AXS_ZR_LAUNCH)
 #undef AXS_ZR_LAUNCH
-#define AXS_ZR_LAUNCH_F(TY, TX, S, R)                                                                     \
-    if (ty == TY && txmax == TX && slots == S && r == R) {                                                \
-        if (esz != 4) fail(AXS_ERR_ARG, "the register z-ring radius-%d kernel needs float fields", r);      \
-        launch_r_t<float, TY, TX, S, R>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);         \
-        return;                                                                                           \
+#define AXS_ZR_LAUNCH_F(TY, TX, S, R, ZR)                                                                  \
+    if (ty == TY && txmax == TX && slots == S && r == R && zr == ZR) {                                     \
+        if (esz != 4) fail(AXS_ERR_ARG, "the register z-ring radius-%d kernel needs float fields", r);       \
+        launch_r_t<float, TY, TX, S, R, ZR>(d, nlat, items, counters, parity, derr, st, ctas_per_sm);      \
+        return;                                                                                            \
     }
     AXS_ZR_SHAPES_F(AXS_ZR_LAUNCH_F)
 #undef AXS_ZR_LAUNCH_F
     fail(AXS_ERR_ARG, "no radius-%d z-march kernel for tile %dx%d, %d slots", r, txmax, ty, slots);
 }
 
-void prepare_zmarch_r(int esz, int ty, int txmax, int slots, int r) {
-#define AXS_ZR_PREP(TY, TX, S, R)                                \
-    if (ty == TY && txmax == TX && slots == S && r == R) {       \
-        if (esz == 4) prepare_r_t<float, TY, TX, S, R>();        \
-        else prepare_r_t<double, TY, TX, S, R>();                \
-        return;                                                  \
+void prepare_zmarch_r(int esz, int ty, int txmax, int slots, int r, int zr) {
+#define AXS_ZR_PREP(TY, TX, S, R)                                       \
+    if (ty == TY && txmax == TX && slots == S && r == R && !zr) {       \
+        if (esz == 4) prepare_r_t<float, TY, TX, S, R, 0>();            \
+        else prepare_r_t<double, TY, TX, S, R, 0>();                    \
+        return;                                                         \
     }
     AXS_ZR_SHAPES(AXS_ZR_PREP)
 #undef AXS_ZR_PREP
-#define AXS_ZR_PREP_F(TY, TX, S, R)                              \
-    if (ty == TY && txmax == TX && slots == S && r == R) {       \
-        if (esz == 4) prepare_r_t<float, TY, TX, S, R>();        \
-        return;                                                  \
+#define AXS_ZR_PREP_F(TY, TX, S, R, ZR)                                 \
+    if (ty == TY && txmax == TX && slots == S && r == R && zr == ZR) {  \
+        if (esz == 4) prepare_r_t<float, TY, TX, S, R, ZR>();           \
+        return;                                                         \
     }
     AXS_ZR_SHAPES_F(AXS_ZR_PREP_F)
 #undef AXS_ZR_PREP_F

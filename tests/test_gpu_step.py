@@ -324,9 +324,12 @@ def test_spectral_after_finite_difference_lattice_of_same_shape(axs, oracle):
         assert rel(gb[q], ga[q]) <= 1e-5, (q, rel(gb[q], ga[q]))
 
 
-RADIUS_VARIANTS = {1: ["1,20,32", "1,21,64", "1,32,64", "1,33,16", "1,41,64", "1,41,32", "1,45,64"],
-                   2: ["1,22,64", "1,23,128", "1,34,32", "1,35,16", "1,42,32", "1,43,64"],
-                   3: ["1,24,32", "1,25,64", "1,26,16", "1,36,16", "1,37,64", "1,44,32"]}
+RADIUS_VARIANTS = {1: ["1,20,32", "1,21,64", "1,32,64", "1,33,16", "1,41,64", "1,41,32", "1,45,64", "1,48,64",
+                        "1,49,32", "1,50,64", "1,57,32"],
+                   2: ["1,22,64", "1,23,128", "1,34,32", "1,35,16", "1,42,32", "1,43,64", "1,51,32", "1,52,64",
+                       "1,53,16"],
+                   3: ["1,24,32", "1,25,64", "1,26,16", "1,36,16", "1,37,64", "1,44,32", "1,54,32", "1,55,16",
+                       "1,56,64"]}
 
 
 @pytest.mark.parametrize("stencil", [1, 2, 3])
