@@ -42,6 +42,9 @@ struct ZRCfg {
     static constexpr int BAR_OFF = S * SLOT;
     static constexpr int SMEM = BAR_OFF + 256;
     static constexpr bool ZREG = ZR || S < 2 * R + 2;          // z-neighbours in registers (ZR: also with a deeper ring)
+    // radius 4: only the planes below the centre in registers, those above read
+    // from the ring (where they wait to be centres): 16 registers, not 36
+    static constexpr bool ZHALF = ZREG && R >= 4;
     static_assert(S >= (ZREG ? R + 2 : 2 * R + 2), "the ring holds the planes in use and one in flight");
     static_assert(!ZREG || (sizeof(T) == 4 && MAXV == 1), "register z-ring: float fields, one vector per thread");
     static_assert(TY >= R, "halo bands must not wrap inside a box");
@@ -174,8 +177,9 @@ __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int
             const int nvx = tx / K::VS;
             const int nvec = nvx * TY;
             // ZREG: psi of this thread's vector at planes z-R .. z+R (zr[R] the
-            // centre); toff is the vector's site offset in a band
-            V zr[K::ZREG ? 2 * R + 1 : 1];
+            // centre; ZHALF: z-R .. z-1 only); toff is the vector's site offset
+            // in a band
+            V zr[K::ZREG ? (K::ZHALF ? R : 2 * R + 1) : 1];
             int toff = 0;
             if constexpr (K::ZREG) {
                 const int yy = cid < nvec ? cid / nvx : 0, xx = cid < nvec ? (cid % nvx) * K::VS : 0;
@@ -191,7 +195,8 @@ __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int
                         ok = false;
                         continue;
                     }
-                    zr[d] = *reinterpret_cast<const V *>(reinterpret_cast<const C *>(smem + ((q0 + d) % S) * K::SLOT) + toff);
+                    if (d < (K::ZHALF ? R : 2 * R))
+                        zr[d] = *reinterpret_cast<const V *>(reinterpret_cast<const C *>(smem + ((q0 + d) % S) * K::SLOT) + toff);
                     if (d < R) {
                         __syncwarp();
                         if (lane == 0) mbar_arrive(smem_u32(&empty[(q0 + d) % S]));
@@ -203,9 +208,7 @@ __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int
             // band) and its output offset at plane za are fixed for the item,
             // so the plane loop does no division and no branching for them.
             constexpr int NW = (2 * K::RP + K::VS) / K::VS;   // x window [xx-RP, xx+VS+RP) in 16-byte vectors
-            // (radius 4's register ring leaves no room for these: they are
-            // formed per plane there)
-            constexpr bool HW = K::MAXV == 1 && !(K::ZREG && R >= 4);
+            constexpr bool HW = K::MAXV == 1;
             int wo[HW ? NW : 1];
             int yy1 = 0, xx1 = 0;
             int64_t off1 = 0;
@@ -255,7 +258,7 @@ __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int
 #pragma unroll
                 for (int d = 0; d <= 2 * R; ++d) Zp[d] = reinterpret_cast<const C *>(smem + wrap(s_lo + d) * K::SLOT);
                 const C *Cz = Zp[R];
-                if constexpr (K::ZREG) zr[2 * R] = *reinterpret_cast<const V *>(Zp[2 * R] + toff);
+                if constexpr (K::ZREG && !K::ZHALF) zr[2 * R] = *reinterpret_cast<const V *>(Zp[2 * R] + toff);
                 const C *Lh = reinterpret_cast<const C *>(reinterpret_cast<const unsigned char *>(Cz) + K::C_BYTES);
                 const C *Rh = reinterpret_cast<const C *>(reinterpret_cast<const unsigned char *>(Cz) + K::C_BYTES + K::H_PAD);
                 const C *Ph = reinterpret_cast<const C *>(reinterpret_cast<const unsigned char *>(Cz) + K::P_OFF);
@@ -306,7 +309,8 @@ __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int
                         *reinterpret_cast<V *>(yp) = *reinterpret_cast<const V *>(&Cz[rrow + l * tx + xx]);
                         if constexpr (K::ZREG) {
                             *reinterpret_cast<V *>(zm) = zr[R - l];
-                            *reinterpret_cast<V *>(zp) = zr[R + l];
+                            if constexpr (K::ZHALF) *reinterpret_cast<V *>(zp) = *reinterpret_cast<const V *>(&Zp[R + l][rrow + xx]);
+                            else *reinterpret_cast<V *>(zp) = zr[R + l];
                         } else {
                             *reinterpret_cast<V *>(zm) = *reinterpret_cast<const V *>(&Zp[R - l][rrow + xx]);
                             *reinterpret_cast<V *>(zp) = *reinterpret_cast<const V *>(&Zp[R + l][rrow + xx]);
@@ -335,6 +339,8 @@ __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int
                 // this warp is done with plane z-R (load q0+t; ZREG: with the
                 // centre z, load q0+t+R); at the last plane also with the
                 // item's remaining loads
+                V cnew{};   // ZHALF: the centre, next plane's z-1
+                if constexpr (K::ZHALF) cnew = *reinterpret_cast<const V *>(Cz + toff);
                 __syncwarp();
                 const int s_c = wrap(s_lo + R);   // load q0 + t + R (the centre)
                 if constexpr (K::ZREG) {
@@ -343,8 +349,14 @@ __device__ __forceinline__ void zmarch2r_body(const ZLat *__restrict__ lats, int
                         if (t == T_steps - 1)
                             for (int d = 1; d <= R; ++d) mbar_arrive(smem_u32(&empty[wrap(s_c + d)]));
                     }
+                    if constexpr (K::ZHALF) {
 #pragma unroll
-                    for (int d = 0; d < 2 * R; ++d) zr[d] = zr[d + 1];
+                        for (int d = 0; d + 1 < R; ++d) zr[d] = zr[d + 1];
+                        zr[R - 1] = cnew;
+                    } else {
+#pragma unroll
+                        for (int d = 0; d < 2 * R; ++d) zr[d] = zr[d + 1];
+                    }
                 } else if (lane == 0) {
                     mbar_arrive(smem_u32(&empty[s_lo]));
                     if (t == T_steps - 1)
