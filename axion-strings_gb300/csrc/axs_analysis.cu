@@ -1289,80 +1289,12 @@ __global__ void k_gather_axion(const typename Cplx<T>::type *__restrict__ psi, c
     }
 }
 
-// The same f straight from psi and pih for 3D radius 1: pi_n is formed per
-// site with k_sync_pi's arithmetic and never stored. Each thread marches one
-// (x, y) column through z with psi's z-neighbours in registers, so every psi
-// plane comes from DRAM once (the x and y neighbours are the neighbouring
-// threads' loads of the same plane, from L1 or L2); 20 B per site (psi, pih
-// in, f out) instead of 48 B for the two-kernel path. Blocks are 32 x 8
-// columns. The column's psi and pih are loaded two planes ahead and the x/y
-// neighbours one plane ahead, so several planes of loads are in flight per
-// thread; offsets within a plane are 32-bit (N^2 < 2^31) to keep the float
-// thread within 64 registers (4 blocks per SM). N >= 4, so z + 3 < 2N.
-template <typename T>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_axion_zcol(const typename Cplx<T>::type *__restrict__ psi,
-                                                       const typename Cplx<T>::type *__restrict__ pih,
-                                                       T *__restrict__ dst, const double *clock, int N, double dt,
-                                                       double inv_dx2, double lambda, double T0sq3, int prs, int fresh,
-                                                       double tau) {
-    typedef typename Cplx<T>::type C;
-    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
-    if (x >= N || y >= N) return;
-    const StepCoefs<T> c = make_coefs<T>(*clock, dt, 0.5 * dt, inv_dx2, lambda, T0sq3, prs, 0);
-    const T itau = (T)(1.0 / tau);
-    const int64_t NN = (int64_t)N * N;
-    const int col = y * N + x;
-    const int xm = y * N + (x == 0 ? N - 1 : x - 1) - col, xp = y * N + (x == N - 1 ? 0 : x + 1) - col;
-    const int ym = (y == 0 ? N - 1 : y - 1) * N + x - col, yp = (y == N - 1 ? 0 : y + 1) * N + x - col;
-    // column values: psi planes z-1, z, z+1 in use, z+2 and z+3 in flight;
-    // pih plane z in use, z+1 and z+2 in flight; neighbours of plane z in use
-    // (loaded last iteration), those of z+1 in flight. Column pointers advance
-    // a plane per site and wrap once near the end; two sites per trip (N is
-    // even), so the register rotation is renaming.
-    const int64_t len = NN * N;
-    C zm = psi[(int64_t)(N - 1) * NN + col], zc = psi[col];
-    C zp = psi[NN + col], zq = psi[2 * NN + col];
-    C pc = pih[col], pq = pih[NN + col];
-    C a, b, d, e;
-    if (!fresh) { a = psi[col + xm]; b = psi[col + xp]; d = psi[col + ym]; e = psi[col + yp]; }
-    const C *s3 = psi + 3 * NN + col, *p2 = pih + 2 * NN + col, *s1 = psi + NN + col;   // planes z+3, z+2, z+1
-    T *out = dst + col;
-    for (int z = 0; z < N; z += 2) {
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int zz = z + h;
-            const C zr = *(zz + 3 < N ? s3 : s3 - len);
-            const C pr = *(zz + 2 < N ? p2 : p2 - len);
-            const C *q1 = zz + 1 < N ? s1 : s1 - len;
-            s3 += NN;
-            p2 += NN;
-            s1 += NN;
-            C p = pc;
-            if (!fresh) {   // a fresh state holds pi_0 itself (the reference's ker is zero)
-                const C na = q1[xm], nb = q1[xp], nd = q1[ym], ne = q1[yp];
-                const T L1 = lap7<T>(zc.x, a.x, b.x, d.x, e.x, zm.x, zp.x);
-                const T L2 = lap7<T>(zc.y, a.y, b.y, d.y, e.y, zm.y, zp.y);
-                sync_pi_site<T>(zc.x, zc.y, L1, L2, p.x, p.y, c);
-                a = na;
-                b = nb;
-                d = nd;
-                e = ne;
-            }
-            *out = axion_f<T>(zc.x, zc.y, p.x, p.y, itau);
-            out += NN;
-            zm = zc;
-            zc = zp;
-            zp = zq;
-            zq = zr;
-            pc = pq;
-            pq = pr;
-        }
-    }
-}
-
-// ---- z-column kernels for the radius-R stencils (R = 2..4)
+// ---- staged z-column kernels (the axion field for every stencil radius,
+// the energies for radius 2..4)
 //
-// A block marches 32 x 8 columns through z with every load from DRAM staged
+// f = |phi| dtheta/dtau = (psi2 pi1 - psi1 pi2) / (tau |psi|) and the energies
+// need pi_n = pih + dt/2 K(psi), formed per site with k_sync_pi's arithmetic
+// (stencil_at's order) and never stored. A block marches 32 x 8 columns through z with every load from DRAM staged
 // by cp.async into shared memory, so the loads in flight hold no registers:
 // per plane, the block's psi tile with an R-wide periodic halo (the in-plane
 // neighbours) and its own pih values, in rings of S = A + 1 slots issued A
@@ -1439,6 +1371,13 @@ template <typename T, int R, int W, int TW>
 __device__ __forceinline__ void tile_stencil(const typename Cplx<T>::type *t, const typename Cplx<T>::type (&zr)[W],
                                              int g, T &L1, T &L2) {
     const auto &ctr = zr[g % W];
+    if constexpr (R == 1) {   // lap7's order, as stencil_at forms radius 1
+        const auto xm = t[-1], xp = t[1], ym = t[-TW], yp = t[TW];
+        const auto &zm = zr[(g + W - 1) % W], &zp = zr[(g + 1) % W];
+        L1 = lap7<T>(ctr.x, xm.x, xp.x, ym.x, yp.x, zm.x, zp.x);
+        L2 = lap7<T>(ctr.y, xm.y, xp.y, ym.y, yp.y, zm.y, zp.y);
+        return;
+    }
     T a1 = (T)stencil_coef(R - 1, 3, 0) * ctr.x, a2 = (T)stencil_coef(R - 1, 3, 0) * ctr.y;
 #pragma unroll
     for (int l = 1; l <= R; ++l) {
@@ -1521,9 +1460,12 @@ __device__ __forceinline__ void zcol_march(const typename Cplx<T>::type *__restr
     cp_async_wait<0>();
 }
 
-// k_axion_zcol for the radius-R stencils: 20 B per site from DRAM as for
-// radius 1, against 44 B and per-site 64-bit index arithmetic through
-// k_sync_pi and scratch.
+// The axion field of the kinetic spectrum for a stencil of radius R = 1..4:
+// 20 B per site from DRAM (psi, pih in, f out), against 44 B and per-site
+// 64-bit index arithmetic through k_sync_pi and scratch. (At radius 1 a
+// march with the column's psi and pih loaded into registers two planes ahead
+// and the in-plane neighbours read from global memory ran 3.7 against 3.5 ms
+// at 1024^3.)
 template <typename T, int R>
 __global__ void __launch_bounds__(256, (ZMarch<T, R>::MINB)) k_axion_zcol_r(const typename Cplx<T>::type *__restrict__ psi,
                                                                  const typename Cplx<T>::type *__restrict__ pih,
@@ -1554,14 +1496,13 @@ static void axion_zcol_t(Lattice *L) {
     T *dst = (T *)L->fft_in;
     const double *clk = L->dclock + L->cur;
     const double dt = p.time_step, idx2 = 1.0 / (dx * dx), la = p.lambda, t3 = (T0 * T0) / 3.0;
-    const dim3 grid((N + 31) / 32, (N + 7) / 8), block(32, 8);
-    const int g = (int)(grid.x * grid.y);
+    const int g = ((N + 31) / 32) * ((N + 7) / 8);   // blocks of 32 x 8 columns
     auto radius = [&](auto kern, size_t smem) {
         AXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         kern<<<g, 256, smem, L->stream>>>(f, q, dst, clk, N, dt, idx2, la, t3, p.prs, L->fresh, L->tau);
     };
     switch (p.stencil_setting) {
-    case 0: k_axion_zcol<T><<<grid, block, 0, L->stream>>>(f, q, dst, clk, N, dt, idx2, la, t3, p.prs, L->fresh, L->tau); break;
+    case 0: radius(k_axion_zcol_r<T, 1>, ZMarch<T, 1>::SMEM); break;
     case 1: radius(k_axion_zcol_r<T, 2>, ZMarch<T, 2>::SMEM); break;
     case 2: radius(k_axion_zcol_r<T, 3>, ZMarch<T, 3>::SMEM); break;
     default: radius(k_axion_zcol_r<T, 4>, ZMarch<T, 4>::SMEM); break;
@@ -2091,7 +2032,7 @@ __global__ void __launch_bounds__(256) k_energies(const typename Cplx<T>::type *
 // (the kinetic term is quadratic in pi_n, so unlike the background means it
 // needs the full half kick per site). pi_n is formed per site with
 // k_sync_pi's arithmetic and never stored, and each thread marches one (x, y)
-// column through z as k_axion_zcol does: psi's z-neighbours stay in registers
+// column through z: psi's z-neighbours stay in registers
 // and the in-plane neighbours (also the x+1, y+1 forward differences of the
 // gradient energy; z+1 is the next plane in registers) come from the
 // neighbouring threads' loads of the same plane. 16 B from DRAM per site
