@@ -367,6 +367,26 @@ __device__ __forceinline__ void site_update(T a, T b, T L1, T L2, T &p1, T &p2, 
     bn = fma(c.dt, p2, b);
 }
 
+// Plain FP64 steps of radius 1 fold the stencil's centre weight w0 = -2 NDIMS
+// into the local coefficient: the kick is kdt_idx2 S + (kdt_coef r +
+// kdt_idx2 w0) psi with S the neighbour sum, two FP64 operations per site
+// fewer than forming the Laplacian first (GB300's FP64 pipe bounds the plain
+// FP64 step); kctr = kdt_idx2 w0. Float steps keep the Laplacian form.
+template <typename T>
+__device__ __forceinline__ void site_update_fold(T a, T b, T S1, T S2, T &p1, T &p2, T &an, T &bn,
+                                                 const StepCoefs<T> &c, T kctr) {
+    T r = fma(a, a, fma(b, b, c.c0));
+    T g = fma(c.kdt_coef, r, kctr);
+    p1 = fma(c.kdt_idx2, S1, fma(g, a, p1));
+    p2 = fma(c.kdt_idx2, S2, fma(g, b, p2));
+    an = fma(c.dt, p1, a);
+    bn = fma(c.dt, p2, b);
+}
+template <typename T>
+__device__ __forceinline__ T nsum7(T xm, T xp, T ym, T yp, T zm, T zp) { return ((xm + xp) + (ym + yp)) + (zm + zp); }
+template <typename T>
+__device__ __forceinline__ T nsum5(T xm, T xp, T ym, T yp) { return (xm + xp) + (ym + yp); }
+
 // Synchronised momentum of one site: pi_n = pih_{n-1} + dt/2 K(psi_n) with
 // c = make_coefs(tau_n, dt, dt/2, ...); (L1, L2) the stencil sums.
 template <typename T>

@@ -49,8 +49,9 @@ __global__ void k_drift0(const typename Cplx<T>::type *__restrict__ psi, typenam
 }
 
 // Stencil sums of both components at site m for radius R (R = 1 uses the
-// shared lap5/lap7 association order). Unscaled by 1/dx^2.
-template <typename T, int ND, int R>
+// shared lap5/lap7 association order). Unscaled by 1/dx^2. NB (R = 1): the
+// neighbour sums alone, for site_update_fold.
+template <typename T, int ND, int R, bool NB = false>
 __device__ __forceinline__ void stencil_at(const typename Cplx<T>::type *__restrict__ psi, int64_t m, int N,
                                            int setting, T &L1, T &L2, typename Cplx<T>::type &centre) {
     typedef typename Cplx<T>::type C;
@@ -66,13 +67,13 @@ __device__ __forceinline__ void stencil_at(const typename Cplx<T>::type *__restr
         C xm = psi[rowbase + wrapi(x - 1, N)], xp = psi[rowbase + wrapi(x + 1, N)];
         C ym = psi[planebase + wrapi(y - 1, N) * N + x], yp = psi[planebase + wrapi(y + 1, N) * N + x];
         if (ND == 2) {
-            L1 = lap5<T>(c.x, xm.x, xp.x, ym.x, yp.x);
-            L2 = lap5<T>(c.y, xm.y, xp.y, ym.y, yp.y);
+            L1 = NB ? nsum5<T>(xm.x, xp.x, ym.x, yp.x) : lap5<T>(c.x, xm.x, xp.x, ym.x, yp.x);
+            L2 = NB ? nsum5<T>(xm.y, xp.y, ym.y, yp.y) : lap5<T>(c.y, xm.y, xp.y, ym.y, yp.y);
         } else {
             int64_t yx = y * N + x;
             C zm = psi[wrapi(z - 1, N) * NN + yx], zp = psi[wrapi(z + 1, N) * NN + yx];
-            L1 = lap7<T>(c.x, xm.x, xp.x, ym.x, yp.x, zm.x, zp.x);
-            L2 = lap7<T>(c.y, xm.y, xp.y, ym.y, yp.y, zm.y, zp.y);
+            L1 = NB ? nsum7<T>(xm.x, xp.x, ym.x, yp.x, zm.x, zp.x) : lap7<T>(c.x, xm.x, xp.x, ym.x, yp.x, zm.x, zp.x);
+            L2 = NB ? nsum7<T>(xm.y, xp.y, ym.y, yp.y, zm.y, zp.y) : lap7<T>(c.y, xm.y, xp.y, ym.y, yp.y, zm.y, zp.y);
         }
         return;
     }
@@ -108,14 +109,17 @@ __global__ void __launch_bounds__(256) k_step_generic(const typename Cplx<T>::ty
                                                       int setting, int form) {
     double tau = *clock_in;
     StepCoefs<T> c = make_coefs<T>(tau, dt, dt, inv_dx2, lambda, T0sq3, prs, form);
+    constexpr bool FOLD = sizeof(T) == 8 && R == 1;
+    const T kctr = c.kdt_idx2 * (T)(-2 * ND);
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
         T L1, L2;
         typename Cplx<T>::type ctr;
-        stencil_at<T, ND, R>(psi, m, N, setting, L1, L2, ctr);
+        stencil_at<T, ND, R, FOLD>(psi, m, N, setting, L1, L2, ctr);
         auto p = pih[m];
         typename Cplx<T>::type o;
-        site_update<T>(ctr.x, ctr.y, L1, L2, p.x, p.y, o.x, o.y, c);
+        if constexpr (FOLD) site_update_fold<T>(ctr.x, ctr.y, L1, L2, p.x, p.y, o.x, o.y, c, kctr);
+        else site_update<T>(ctr.x, ctr.y, L1, L2, p.x, p.y, o.x, o.y, c);
         pih[m] = p;
         out[m] = o;
     }
@@ -498,9 +502,16 @@ __global__ void __launch_bounds__(256) k_zmarch(const ZLat *__restrict__ lats, i
                 for (int j = 0; j < K::VS; ++j) {
                     const C xm = (j == 0) ? left : ctr[j - 1];
                     const C xp = (j == K::VS - 1) ? right : ctr[j + 1];
-                    const T L1 = lap7<T>(ctr[j].x, xm.x, xp.x, up[j].x, dn[j].x, zm[j].x, zp[j].x);
-                    const T L2 = lap7<T>(ctr[j].y, xm.y, xp.y, up[j].y, dn[j].y, zm[j].y, zp[j].y);
-                    site_update<T>(ctr[j].x, ctr[j].y, L1, L2, pv[2 * j], pv[2 * j + 1], outv[j].x, outv[j].y, cf);
+                    if constexpr (sizeof(T) == 8) {   // FP64: the centre weight folded (site_update_fold)
+                        const T S1 = nsum7<T>(xm.x, xp.x, up[j].x, dn[j].x, zm[j].x, zp[j].x);
+                        const T S2 = nsum7<T>(xm.y, xp.y, up[j].y, dn[j].y, zm[j].y, zp[j].y);
+                        site_update_fold<T>(ctr[j].x, ctr[j].y, S1, S2, pv[2 * j], pv[2 * j + 1], outv[j].x, outv[j].y,
+                                            cf, cf.kdt_idx2 * (T)-6);
+                    } else {
+                        const T L1 = lap7<T>(ctr[j].x, xm.x, xp.x, up[j].x, dn[j].x, zm[j].x, zp[j].x);
+                        const T L2 = lap7<T>(ctr[j].y, xm.y, xp.y, up[j].y, dn[j].y, zm[j].y, zp[j].y);
+                        site_update<T>(ctr[j].x, ctr[j].y, L1, L2, pv[2 * j], pv[2 * j + 1], outv[j].x, outv[j].y, cf);
+                    }
                 }
                 const int64_t off = ((int64_t)z * N + (y0 + yy)) * N + (x0 + xx);
                 *reinterpret_cast<V *>(&pih_out[off]) = *reinterpret_cast<V *>(pv);
@@ -732,9 +743,17 @@ __global__ void __launch_bounds__(Z2Cfg<T, TY, TXMAX, S>::NT)
                     for (int jj = 0; jj < K::VS; ++jj) {
                         const C xm = (jj == 0) ? left : ctr[jj - 1];
                         const C xp = (jj == K::VS - 1) ? right : ctr[jj + 1];
-                        const T L1 = lap7<T>(ctr[jj].x, xm.x, xp.x, up[jj].x, dn[jj].x, zm[jj].x, zp[jj].x);
-                        const T L2 = lap7<T>(ctr[jj].y, xm.y, xp.y, up[jj].y, dn[jj].y, zm[jj].y, zp[jj].y);
-                        site_update<T>(ctr[jj].x, ctr[jj].y, L1, L2, pv[2 * jj], pv[2 * jj + 1], outv[jj].x, outv[jj].y, cf);
+                        if constexpr (sizeof(T) == 8) {   // FP64: the centre weight folded (site_update_fold)
+                            const T S1 = nsum7<T>(xm.x, xp.x, up[jj].x, dn[jj].x, zm[jj].x, zp[jj].x);
+                            const T S2 = nsum7<T>(xm.y, xp.y, up[jj].y, dn[jj].y, zm[jj].y, zp[jj].y);
+                            site_update_fold<T>(ctr[jj].x, ctr[jj].y, S1, S2, pv[2 * jj], pv[2 * jj + 1], outv[jj].x,
+                                                outv[jj].y, cf, cf.kdt_idx2 * (T)-6);
+                        } else {
+                            const T L1 = lap7<T>(ctr[jj].x, xm.x, xp.x, up[jj].x, dn[jj].x, zm[jj].x, zp[jj].x);
+                            const T L2 = lap7<T>(ctr[jj].y, xm.y, xp.y, up[jj].y, dn[jj].y, zm[jj].y, zp[jj].y);
+                            site_update<T>(ctr[jj].x, ctr[jj].y, L1, L2, pv[2 * jj], pv[2 * jj + 1], outv[jj].x,
+                                           outv[jj].y, cf);
+                        }
                     }
                     const int64_t off = ((int64_t)z * N + (y0 + yy)) * N + (x0 + xx);
                     *reinterpret_cast<V *>(&pih[off]) = *reinterpret_cast<V *>(pv);
