@@ -1294,8 +1294,9 @@ __global__ void k_gather_axion(const typename Cplx<T>::type *__restrict__ psi, c
 //
 // f = |phi| dtheta/dtau = (psi2 pi1 - psi1 pi2) / (tau |psi|) and the energies
 // need pi_n = pih + dt/2 K(psi), formed per site with k_sync_pi's arithmetic
-// (stencil_at's order) and never stored. A block marches 32 x 8 columns through z with every load from DRAM staged
-// by cp.async into shared memory, so the loads in flight hold no registers:
+// (stencil_at's order) and never stored. A block marches 32 x 8 columns
+// through z with every load from DRAM staged by cp.async into shared memory,
+// so the loads in flight hold no registers:
 // per plane, the block's psi tile with an R-wide periodic halo (the in-plane
 // neighbours) and its own pih values, in rings of S = A + 1 slots issued A
 // planes ahead, with one block barrier per site. Each thread keeps its
