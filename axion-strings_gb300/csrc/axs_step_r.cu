@@ -9,10 +9,12 @@
 //    aligned; only the tile rows need them: the stencil is a cross), plus the
 //    pih tile;
 //  * a ring of S >= 2R + 2 slots holding the planes z-R .. z+R and one in flight;
-//    or, with fewer slots (ZREG, float fields, one vector per thread), each
-//    thread carries psi of its vector at planes z-R .. z+R in registers and
-//    the ring holds only the planes z .. z+R still to be centres (S >= R + 2),
-//    so more CTAs share an SM;
+//    or (ZREG, float fields, one vector per thread: with fewer slots, or with
+//    any number when ZR is set) each thread carries psi of its vector at
+//    planes z-R .. z+R in registers (radius 4: z-R .. z-1, the rest read from
+//    the ring) and the ring holds only the planes z .. z+R still to be centres
+//    (S >= R + 2), so S - R - 1 plane loads are in flight per CTA and more
+//    CTAs share an SM;
 //  * the stencil sum formed exactly as stencil_at forms it for R > 1
 //    (c0 * psi, then per l: ((x- + x+) + (y- + y+)) + (z- + z+), fused into the
 //    sum with c_l), so every configuration is bit-identical to k_step_generic.
