@@ -209,12 +209,15 @@ static void xfer_release(Lattice *L) {
     g_xfer.erase(it);
 }
 
+// drift: dst is pih and psi[cur] holds the new psi; the first (pure drift)
+// step of the fresh state goes along with the packing (launch_pack2_drift)
 template <typename S>
-static void upload_pair(Lattice *L, const S *a, const S *b, void *dst) {
+static void upload_pair(Lattice *L, const S *a, const S *b, void *dst, bool drift = false) {
     const int is_d = sizeof(S) == 8;
     void *da = device_alias(a), *db = device_alias(b);
     if (da && db) {
-        launch_pack2(L, da, db, is_d, dst, L->length, L->stream);
+        if (drift) launch_pack2_drift(L, da, db, is_d, 0, L->length, L->stream);
+        else launch_pack2(L, da, db, is_d, dst, L->length, L->stream);
         return;
     }
     Xfer &x = xfer(L);
@@ -234,7 +237,8 @@ static void upload_pair(Lattice *L, const S *a, const S *b, void *dst) {
         AXS_CUDA(cudaMemcpyAsync(sb, b + off, (size_t)n * sizeof(S), cudaMemcpyHostToDevice, x.copy));
         AXS_CUDA(cudaEventRecord(x.copied[s], x.copy));
         AXS_CUDA(cudaStreamWaitEvent(L->stream, x.copied[s], 0));
-        launch_pack2(L, sa, sb, is_d, (char *)dst + (size_t)off * cs, n, L->stream);
+        if (drift) launch_pack2_drift(L, sa, sb, is_d, off, n, L->stream);
+        else launch_pack2(L, sa, sb, is_d, (char *)dst + (size_t)off * cs, n, L->stream);
         AXS_CUDA(cudaEventRecord(x.done[s], L->stream));
     }
 }
@@ -273,10 +277,14 @@ template <typename S>
 static void upload_fields(Lattice *L, const S *f0, const S *f1, const S *f2, const S *f3) {
     const S *src[4] = {f0, f1, f2, f3};
     const int is_d = sizeof(S) == 8;
+    set_device_clock(L);   // before the drift that reads it
+    // a full state (psi and pi): the first step, a pure drift, is formed while
+    // the momentum uploads (the link bounds the upload)
+    const bool drift = f0 && f1 && f2 && f3;
     for (int pr = 0; pr < 2; ++pr) {
         void *dst = pr == 0 ? L->psi[L->cur] : L->pih;
         if (src[2 * pr] && src[2 * pr + 1]) {
-            upload_pair<S>(L, src[2 * pr], src[2 * pr + 1], dst);
+            upload_pair<S>(L, src[2 * pr], src[2 * pr + 1], dst, drift && pr == 1);
             continue;
         }
         for (int f = 2 * pr; f < 2 * pr + 2; ++f) {   // one component of the pair
@@ -286,10 +294,9 @@ static void upload_fields(Lattice *L, const S *f0, const S *f1, const S *f2, con
             launch_pack(L, st, is_d, pr, f & 1);
         }
     }
-    L->fresh = 1;
+    L->fresh = drift ? 2 : 1;
     L->last_nplaq = -1;
     L->list_valid = false;
-    set_device_clock(L);
     AXS_CUDA(cudaStreamSynchronize(L->stream));
 }
 
@@ -439,6 +446,7 @@ int axs_set_time(axs_lattice *h, double tau, int64_t steps) {
     CHECK_HANDLE(h);
     h->L.tau = tau;
     h->L.steps = steps;
+    if (h->L.fresh == 2) h->L.fresh = 1;   // the drift formed at upload used the old time
     set_device_clock(&h->L);
     AXS_CUDA(cudaStreamSynchronize(h->L.stream));
     API_END
@@ -624,7 +632,7 @@ int axs_checkpoint(axs_lattice *h, void *buf, size_t bytes) {
     hd.NDIMS = L->p.NDIMS;
     hd.N = L->p.N;
     hd.esz = L->esz;
-    hd.fresh = L->fresh;
+    hd.fresh = L->fresh ? 1 : 0;   // psi[cur ^ 1] is not saved
     hd.tau = L->tau;
     hd.steps = L->steps;
     memcpy(buf, &hd, sizeof hd);

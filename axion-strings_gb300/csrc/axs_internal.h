@@ -130,7 +130,8 @@ struct Lattice {
     int *derr = nullptr;      // device error flags
     int *dcounter = nullptr;  // [2] work counters of the persistent step kernel
     int cur = 0;              // psi[cur] holds the current field; dclock[cur] its tau
-    int fresh = 1;            // next step is the pure drift of a freshly set state
+    int fresh = 1;            // next step is the pure drift of a freshly set state (2: an upload
+                              // formed it already into psi[cur ^ 1] and the next clock)
     double tau = 1.0;
     int64_t steps = 0;
     cudaStream_t stream = nullptr;
@@ -234,6 +235,10 @@ void launch_unpack(Lattice *L, const void *src, int which, int comp, void *dst_r
 void launch_pack(Lattice *L, const void *src_real, int src_is_double, int which, int comp);
 void launch_pack2(Lattice *L, const void *a, const void *b, int src_is_double, void *dst_cplx, int64_t n,
                   cudaStream_t st);
+// the momentum pair into pih[off, off + n) with the first (pure drift) step of
+// a fresh state into psi[cur ^ 1] and the next clock
+void launch_pack2_drift(Lattice *L, const void *a, const void *b, int src_is_double, int64_t off, int64_t n,
+                        cudaStream_t st);
 void launch_unpack2(Lattice *L, const void *src_cplx, void *a, void *b, int dst_is_double, int64_t n, cudaStream_t st);
 void check_device_errors(Lattice *L);
 void check_device_error_flag(int *derr, cudaStream_t s);

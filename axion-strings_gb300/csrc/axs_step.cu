@@ -324,6 +324,56 @@ __global__ void k_pack2_x4(const S *__restrict__ a, const S *__restrict__ b, T *
         Quad<T>::store(dst + 8 * q + 4, hi);
     }
 }
+// Upload of the momentum pair with the first step of a fresh state fused in:
+// pih = (a, b) as k_pack2(_x4) stores it, and psi_next = psi + d pih with
+// k_drift0's arithmetic (the reference's first step with ker_curr = 0 is a
+// pure drift). The upload is bound by the host link, so the drift's device
+// traffic costs nothing there. One thread writes the next clock.
+template <typename T, typename S>
+__global__ void k_pack2_drift(const S *__restrict__ a, const S *__restrict__ b, typename Cplx<T>::type *__restrict__ pih,
+                              const typename Cplx<T>::type *__restrict__ psi, typename Cplx<T>::type *__restrict__ psi_next,
+                              int64_t len, const double *clock_in, double *clock_out, double dt, int form) {
+    const double t1 = *clock_in + dt;
+    const T d = (T)(form == 1 ? dt / (t1 * t1) : dt);   // the drift of make_coefs
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < len; m += stride) {
+        typename Cplx<T>::type v, q = psi[m];
+        v.x = (T)a[m];
+        v.y = (T)b[m];
+        pih[m] = v;
+        q.x = fma(d, v.x, q.x);
+        q.y = fma(d, v.y, q.y);
+        psi_next[m] = q;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *clock_out = *clock_in + dt;
+}
+template <typename T, typename S>
+__global__ void k_pack2_drift_x4(const S *__restrict__ a, const S *__restrict__ b, T *__restrict__ pih,
+                                 const T *__restrict__ psi, T *__restrict__ psi_next, int64_t len4,
+                                 const double *clock_in, double *clock_out, double dt, int form) {
+    const double t1 = *clock_in + dt;
+    const T d = (T)(form == 1 ? dt / (t1 * t1) : dt);
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < len4; q += stride) {
+        S va[4], vb[4];
+        Quad<S>::load(a + 4 * q, va);
+        Quad<S>::load(b + 4 * q, vb);
+        T lo[4] = {(T)va[0], (T)vb[0], (T)va[1], (T)vb[1]}, hi[4] = {(T)va[2], (T)vb[2], (T)va[3], (T)vb[3]};
+        Quad<T>::store(pih + 8 * q, lo);
+        Quad<T>::store(pih + 8 * q + 4, hi);
+        T slo[4], shi[4];
+        Quad<T>::load(psi + 8 * q, slo);
+        Quad<T>::load(psi + 8 * q + 4, shi);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            slo[i] = fma(d, lo[i], slo[i]);
+            shi[i] = fma(d, hi[i], shi[i]);
+        }
+        Quad<T>::store(psi_next + 8 * q, slo);
+        Quad<T>::store(psi_next + 8 * q + 4, shi);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *clock_out = *clock_in + dt;
+}
 template <typename T, typename S>
 __global__ void k_unpack2_x4(const T *__restrict__ src, S *__restrict__ a, S *__restrict__ b, int64_t len4) {
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -2540,7 +2590,9 @@ int lattice_advance(Lattice *L, int max_steps) {
     double *cout = L->dclock + (L->cur ^ 1);
     int k = 1;
     bool swap = false;
-    if (L->fresh) {
+    if (L->fresh == 2) {   // the upload formed the drift already (launch_pack2_drift)
+        L->fresh = 0;
+    } else if (L->fresh) {
         if (L->esz == 4)
             k_drift0<float><<<grid_for(L->length), 256, 0, L->stream>>>((const float2 *)L->psi[L->cur],
                                                                          (float2 *)L->psi[L->cur ^ 1],
@@ -2738,6 +2790,7 @@ static double time_launches(cudaStream_t st, int reps, const std::function<void(
 // decides.
 void lattice_autotune(Lattice *L) {
     L->tuned = true;
+    if (L->fresh == 2) L->fresh = 1;   // the trials overwrite the drift formed at upload
     // AXS_FORCE_CONFIG="kind,variant,zchunk" pins a configuration (tests use it
     // to show that every configuration gives bit-identical results).
     const char *force = getenv("AXS_FORCE_CONFIG");
@@ -2948,6 +3001,8 @@ static int ensemble_advance(Ensemble *E, int max_steps) {
 
 void ensemble_autotune(Ensemble *E) {
     E->tuned = true;
+    for (Lattice *m : E->members)
+        if (m->fresh == 2) m->fresh = 1;   // the trials overwrite the drift formed at upload
     if (E->cfg.kind != 1) return;
     // AXS_FORCE_CONFIG="1,variant,zchunk" pins the ensemble's z-march
     // configuration too (when the variant tiles every member)
@@ -3028,7 +3083,7 @@ void ensemble_evolve(Ensemble *E, int nsteps) {
     }
     if (nsteps <= 0) return;
     for (Lattice *m : E->members)
-        if (m->fresh != E->members[0]->fresh || m->steps != E->members[0]->steps)
+        if ((m->fresh != 0) != (E->members[0]->fresh != 0) || m->steps != E->members[0]->steps)
             fail(AXS_ERR_STATE, "ensemble members are not at the same step");
     if (E->members[0]->fresh) {
         for (Lattice *m : E->members) lattice_advance(m, 1);   // pure drift per member
@@ -3219,6 +3274,54 @@ void launch_pack2(Lattice *L, const void *a, const void *b, int src_is_double, v
     } else {
         if (src_is_double) k_pack2<double, double><<<g, 256, 0, st>>>((const double *)a, (const double *)b, (double2 *)dst_cplx, n);
         else k_pack2<double, float><<<g, 256, 0, st>>>((const float *)a, (const float *)b, (double2 *)dst_cplx, n);
+    }
+    AXS_CUDA(cudaGetLastError());
+    count_launches(1);
+}
+void launch_pack2_drift(Lattice *L, const void *a, const void *b, int src_is_double, int64_t off, int64_t n,
+                        cudaStream_t st) {
+    const size_t cs = (size_t)2 * L->esz;
+    char *pih = (char *)L->pih + (size_t)off * cs;
+    const char *psi = (const char *)L->psi[L->cur] + (size_t)off * cs;
+    char *nxt = (char *)L->psi[L->cur ^ 1] + (size_t)off * cs;
+    const double *cin = L->dclock + L->cur;
+    double *cout = L->dclock + (L->cur ^ 1);
+    const double dt = L->p.time_step;
+    const int form = L->p.form;
+    if (quad_ok(a, b, pih, n) && quad_ok(a, b, nxt, n) && quad_ok(a, b, psi, n)) {
+        const int g = grid_for(n / 4);
+        if (L->esz == 4) {
+            if (src_is_double)
+                k_pack2_drift_x4<float, double><<<g, 256, 0, st>>>((const double *)a, (const double *)b, (float *)pih,
+                                                                  (const float *)psi, (float *)nxt, n / 4, cin, cout, dt, form);
+            else
+                k_pack2_drift_x4<float, float><<<g, 256, 0, st>>>((const float *)a, (const float *)b, (float *)pih,
+                                                                 (const float *)psi, (float *)nxt, n / 4, cin, cout, dt, form);
+        } else {
+            if (src_is_double)
+                k_pack2_drift_x4<double, double><<<g, 256, 0, st>>>((const double *)a, (const double *)b, (double *)pih,
+                                                                   (const double *)psi, (double *)nxt, n / 4, cin, cout, dt, form);
+            else
+                k_pack2_drift_x4<double, float><<<g, 256, 0, st>>>((const float *)a, (const float *)b, (double *)pih,
+                                                                  (const double *)psi, (double *)nxt, n / 4, cin, cout, dt, form);
+        }
+    } else {
+        const int g = grid_for(n);
+        if (L->esz == 4) {
+            if (src_is_double)
+                k_pack2_drift<float, double><<<g, 256, 0, st>>>((const double *)a, (const double *)b, (float2 *)pih,
+                                                               (const float2 *)psi, (float2 *)nxt, n, cin, cout, dt, form);
+            else
+                k_pack2_drift<float, float><<<g, 256, 0, st>>>((const float *)a, (const float *)b, (float2 *)pih,
+                                                              (const float2 *)psi, (float2 *)nxt, n, cin, cout, dt, form);
+        } else {
+            if (src_is_double)
+                k_pack2_drift<double, double><<<g, 256, 0, st>>>((const double *)a, (const double *)b, (double2 *)pih,
+                                                                (const double2 *)psi, (double2 *)nxt, n, cin, cout, dt, form);
+            else
+                k_pack2_drift<double, float><<<g, 256, 0, st>>>((const float *)a, (const float *)b, (double2 *)pih,
+                                                               (const double2 *)psi, (double2 *)nxt, n, cin, cout, dt, form);
+        }
     }
     AXS_CUDA(cudaGetLastError());
     count_launches(1);

@@ -82,3 +82,46 @@ def test_single_field_transfers(axs):
     assert np.array_equal(g[0], f[0])
     assert g[1] is None and g[2] is None
     assert np.array_equal(g[3], f[3])
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("host", ["pageable", "page-locked"])
+def test_upload_forms_the_first_drift(axs, precision, form, host):
+    """A full upload (psi and pi) forms the fresh state's first step, a pure
+    drift, while the momentum packs; the evolution from it equals, bit for
+    bit, the one that drifts in its first step (a state uploaded in parts),
+    and one whose time was reset after the upload."""
+    N = 48
+    p = params(axs, 3, N, precision, form=form)
+    dt = np.float32 if precision == 32 else np.float64
+    rng = np.random.default_rng(11 + form)
+    f = [rng.standard_normal((N, N, N)).astype(dt) for _ in range(4)]
+    pinned = []
+    if host == "page-locked":
+        pinned = [axs.PinnedBuffer((N, N, N), dt) for _ in range(4)]
+        for b, a in zip(pinned, f):
+            b.array[...] = a
+        f = [b.array for b in pinned]
+    outs = []
+    for mode in ("whole", "parts", "set_time"):
+        with axs.Lattice(p) as L:
+            L.init_flat(3, 1.0)
+            L.evolve(2)   # tuned before the upload, so the tuner's trials leave the drift alone
+            tau, steps = L.time
+            if mode == "parts":
+                L.upload(f[0], f[1], None, None, dtype=dt)
+                L.upload(None, None, f[2], f[3], dtype=dt)
+            else:
+                L.upload(*f, dtype=dt)
+            if mode == "set_time":
+                L.set_time(tau, steps)
+            L.evolve(5)
+            outs.append((L.time, L.download(dtype=dt)))
+    for b in pinned:
+        b.free()
+    (t0, g0) = outs[0]
+    for t, g in outs[1:]:
+        assert t == t0
+        for q in range(4):
+            assert np.array_equal(g[q], g0[q]), q
