@@ -1907,9 +1907,60 @@ template <> struct Acc<double> {
 
 // |theta| = |atan2(phi1, phi2)| for the background mean: float fields take
 // fast_atan2 (within 5e-7 rad, a tenth of the float means' 2e-6 tolerance
-// relative to a mean |theta| near pi/2), FP64 fields the library atan2.
+// relative to a mean |theta| near pi/2), FP64 fields abs_phi_theta (below).
 __device__ __forceinline__ float abs_theta(float a, float b) { return fabsf(fast_atan2(a, b)); }
-__device__ __forceinline__ double abs_theta(double a, double b) { return fabs(atan2(a, b)); }
+// FP64 fields: |atan2(a, b)| and |(a, b)| to double precision at a fraction
+// of the library's FP64 cost (GB300's FP64 pipe bounds the FP64 means). The
+// float angle picks the nearest of the angles k pi/128 (k = -128 .. 128); the
+// vector (b, a) is rotated by -k pi/128 with that angle's double cosine and
+// sine (formed on the host) to (x, y), a small angle from the x axis. With
+// u = y/x (the reciprocal from the float one by two Newton-Raphson steps,
+// within an ulp), |u| < 0.0125: the remainder angle atan(u) is the Taylor
+// series to u^7 and |(a, b)| = x sqrt(1 + u^2) the binomial series to u^6
+// (truncations below 3e-17). Vectors outside that (a zero, tiny, huge or
+// non-finite component) take the library's atan2 and square root. The angle
+// is brought back to [-pi, pi] before its magnitude.
+__device__ double2 g_theta_rot[257];   // (cos, sin) of k pi/128 at index k + 128
+__device__ __forceinline__ void abs_phi_theta(double a, double b, double &aphi, double &ath) {
+    const float t0 = fast_atan2((float)a, (float)b);
+    const int k = __float2int_rn(t0 * 40.743665431525205f);   // 128 / pi
+    const double2 cs = g_theta_rot[k + 128];
+    const double x = fma(b, cs.x, a * cs.y), y = fma(a, cs.x, -(b * cs.y));
+    if (x > 1e-30 && x < 1e30) {
+        double r = (double)__frcp_rn((float)x);
+        r = fma(r, fma(-x, r, 1.0), r);
+        r = fma(r, fma(-x, r, 1.0), r);
+        const double u = y * r;
+        if (fabs(u) < 0.0125) {
+            const double u2 = u * u;
+            double q = fma(u2, -1.0 / 7.0, 1.0 / 5.0);
+            q = fma(u2, q, -1.0 / 3.0);
+            double t = fma(u * u2, q, u) + (double)k * (3.141592653589793 / 128.0);
+            if (t > 3.141592653589793) t -= 6.283185307179586;
+            else if (t < -3.141592653589793) t += 6.283185307179586;
+            ath = fabs(t);
+            double w = fma(u2, 1.0 / 16.0, -1.0 / 8.0);
+            w = fma(u2, w, 0.5);
+            aphi = x * fma(u2, w, 1.0);
+            return;
+        }
+    }
+    ath = fabs(atan2(a, b));
+    aphi = sqrt(a * a + b * b);
+}
+// the rotation table of abs_phi_theta, once per device
+static void ensure_theta_table() {
+    static PerDevice done;
+    done.get([] {
+        double2 tab[257];
+        for (int k = -128; k <= 128; ++k) {
+            const double t = (double)k * (3.141592653589793 / 128.0);
+            tab[k + 128] = make_double2(cos(t), sin(t));
+        }
+        AXS_CUDA(cudaMemcpyToSymbol(g_theta_rot, tab, sizeof(tab)));
+        return 1;
+    });
+}
 
 // Two neighbouring sites q = 2i, 2i+1 (one 16-byte load for float fields).
 __device__ __forceinline__ void load_pair(const float2 *__restrict__ a, int64_t i, float2 (&v)[2]) {
@@ -1957,8 +2008,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_background(cons
             t[1] += f[h].y;
             t[2] += p[h].x;
             t[3] += p[h].y;
-            t[4] += abs_theta(f[h].x, f[h].y);
-            t[5] += sqrt(f[h].x * f[h].x + f[h].y * f[h].y);
+            if constexpr (sizeof(T) == 8) {
+                double ap, at;
+                abs_phi_theta(f[h].x, f[h].y, ap, at);
+                t[4] += at;
+                t[5] += ap;
+            } else {
+                t[4] += abs_theta(f[h].x, f[h].y);
+                t[5] += sqrt(f[h].x * f[h].x + f[h].y * f[h].y);
+            }
         }
 #pragma unroll
         for (int k = 0; k < 6; ++k) a[k].add(t[k]);
@@ -2225,6 +2283,7 @@ static int zcol_blocks(int N) { return ((N + 31) / 32) * ((N + 7) / 8); }
 
 void background(Lattice *L, double out[6]) {
     const axs_params &p = L->p;
+    if (L->esz == 8) ensure_theta_table();
     const double T0 = p.T_initial;
     const int resident = L->esz == 4 ? 4 : 2;   // k_background's blocks per SM
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>((L->length / 2 + 255) / 256, (int64_t)num_sms() * resident));
