@@ -53,3 +53,27 @@ def test_finite_check_flags_seeded_nan(axs):
         f[2][3, 4, 5] = np.nan
         L.upload(*f)
         assert not L.check_finite()
+
+
+def test_background_angle_and_modulus_edge_cases(axs):
+    """FP64 means of |theta| = |atan2(phi1, phi2)| and |phi| over sites that
+    the table rotation serves and sites it hands to the library (zeros, values
+    outside float range, the branch cut at theta = +-pi), against numpy, on a
+    fresh state (pi_n is the uploaded pi)."""
+    N = 4
+    p = params(axs, 3, N, 64)
+    rng = np.random.default_rng(5)
+    p1 = rng.standard_normal(N ** 3)
+    p2 = rng.standard_normal(N ** 3)
+    special = [(0.0, 0.0), (0.0, -1.0), (-0.0, -1.0), (1e-13, -1.0), (-1e-13, -1.0), (1.0, 0.0), (-1.0, 0.0),
+               (1e100, 3e100), (-2e-200, 1e-200), (3e-40, -5e-40), (1e-300, -2.0), (2.5, -1e-17)]
+    for i, (a, b) in enumerate(special):
+        p1[i], p2[i] = a, b
+    z = np.zeros(N ** 3)
+    with axs.Lattice(p) as L:
+        L.upload(p1.reshape(N, N, N), p2.reshape(N, N, N), z.reshape(N, N, N), z.reshape(N, N, N))
+        bg = L.background()
+    th = np.mean(np.abs(np.arctan2(p1, p2)))
+    ph = np.mean(np.sqrt(p1 * p1 + p2 * p2))
+    assert abs(bg[4] - th) <= 1e-15 * th, (bg[4], th)
+    assert abs(bg[5] - ph) <= 1e-15 * ph, (bg[5], ph)
