@@ -417,6 +417,23 @@ __device__ __forceinline__ float axion_f<float>(float a, float b, float p1, floa
     const float r2 = a * a + b * b;
     return r2 > 0.f ? (b * p1 - a * p2) * itau * rsqrtf(r2) : 0.f;
 }
+// FP64 fields: 1/|psi| by two Newton-Raphson steps for the reciprocal square
+// root, y <- y (3/2 - s y^2 / 2), from the float rsqrtf (within 1-2 ulp of the
+// correctly rounded square root and division, at a third of their cost on
+// GB300's FP64 pipe); |psi|^2 outside float range takes those.
+template <>
+__device__ __forceinline__ double axion_f<double>(double a, double b, double p1, double p2, double itau) {
+    const double s = a * a + b * b;
+    if (s > 1e-36 && s < 1e36) {
+        const double hs = 0.5 * s;
+        double y = (double)rsqrtf((float)s);
+        y = y * fma(-hs * y, y, 1.5);
+        y = y * fma(-hs * y, y, 1.5);
+        return (b * p1 - a * p2) * itau * y;
+    }
+    const double r = sqrt(s);
+    return r > 0.0 ? (b * p1 - a * p2) * itau / r : 0.0;
+}
 
 // Philox-4x32-10 (Salmon et al., SC'11) and Box-Muller; the deviate for
 // array a at offset m. Must agree with the oracle's definition.
