@@ -39,6 +39,35 @@ def test_members_bit_identical_to_alone(axs, precision):
             assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("precision", [32, 64])
+def test_uploaded_members_bit_identical_to_alone(axs, precision):
+    """Members given a full state by upload (whose first step, a pure drift,
+    is formed by the upload) evolve as the same states uploaded to lattices
+    run alone, before and after the ensemble has been tuned."""
+    specs = [(32, 1.0), (48, 2.0), (64, 0.7)]
+    plist = [params(axs, 3, N, precision, lambda_=lam, T_initial=0.0, prs=1) for N, lam in specs]
+    dt = np.float32 if precision == 32 else np.float64
+    rng = np.random.default_rng(21)
+    states = [[rng.standard_normal((N, N, N)).astype(dt) for _ in range(4)] for N, _ in specs]
+    with axs.Ensemble(plist) as E:
+        got = []
+        for rnd in range(2):   # the first evolve tunes the ensemble, the second finds it tuned
+            times = [m.time for m in E.members]   # an upload keeps a lattice's time
+            for m, f in zip(E.members, states):
+                m.upload(*f, dtype=dt)
+            E.evolve(9)
+            got.append([(t, m.download(dtype=dt)) for t, m in zip(times, E.members)])
+    for rnd in range(2):
+        for p, f, (t, g) in zip(plist, states, got[rnd]):
+            with axs.Lattice(p) as L:
+                L.set_time(*t)
+                L.upload(*f, dtype=dt)
+                L.evolve(9)
+                ref = L.download(dtype=dt)
+            for q in range(4):
+                assert np.array_equal(g[q], ref[q]), (rnd, q)
+
+
 @pytest.mark.parametrize("force", ["1,10,32", "1,13,64", "1,12,128", "1,28,128", "1,31,128", "1,39,64"])
 def test_two_step_members_bit_identical_to_one_step_alone(axs, force, monkeypatch):
     """An ensemble on a two-step variant (halo depth 2, momentum out of place)
