@@ -108,7 +108,9 @@ int axs_destroy(axs_lattice *h);
 /* Set the state from host arrays. Like a freshly initialised reference run,
  * the next step is a pure drift (the reference's ker_curr arrays are zero
  * after calloc: s_run.cpp:44-47, s_integrate.cpp:313-314). tau and the step
- * counter are left as they are. */
+ * counter are left as they are. When all four arrays are given, that drift is
+ * formed while the momentum is transferred (the next axs_evolve then starts
+ * from it); the results are the same bits as drifting in the first step. */
 int axs_upload(axs_lattice *h, const double *phi1, const double *phi2,
                const double *phidot1, const double *phidot2);
 int axs_upload_f32(axs_lattice *h, const float *phi1, const float *phi2,
