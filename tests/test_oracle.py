@@ -265,3 +265,35 @@ def test_atan_tables_match_their_generator():
         g = gen.astype(np.float32)
         ulp = np.spacing(np.abs(g))
         assert np.all(np.abs(c - g) <= ulp), (name, c, g)
+
+
+def test_fp64_angle_and_modulus_by_table_rotation():
+    """The FP64 background means' |atan2(a, b)| and |(a, b)| (abs_phi_theta in
+    axs_analysis.cu), restated in numpy: a float angle within 5e-7 rad picks
+    the nearest k pi/128; the vector is rotated by it with double cosine and
+    sine; the remainder angle and the modulus come from series in u = y/x,
+    which stays below 0.0125 (tan(pi/256 + 5e-7) = 0.01227). Within 4 ulp of
+    arctan2 and sqrt, the truncated series' terms below 3e-17."""
+    assert np.tan(np.pi / 256 + 5e-7) < 0.0125
+    u = 0.0125
+    assert u ** 9 / 9 < 1e-18 and 5 * (u * u) ** 4 / 128 < 3e-17
+    rng = np.random.default_rng(3)
+    n = 400000
+    a = rng.standard_normal(n) * np.exp(rng.uniform(-12, 12, n))
+    b = rng.standard_normal(n) * np.exp(rng.uniform(-12, 12, n))
+    a[:200], b[200:400], b[400:600], a[400:600] = 0.0, 0.0, -1.0, rng.standard_normal(200) * 1e-13
+    t0 = np.arctan2(a.astype(np.float32), b.astype(np.float32))
+    t0 = t0 + rng.uniform(-5e-7, 5e-7, n).astype(np.float32)   # the float angle's error
+    k = np.rint(t0 * np.float32(128 / np.pi)).astype(np.int64)
+    th = k * (np.pi / 128.0)
+    c, s = np.cos(th), np.sin(th)
+    x, y = b * c + a * s, a * c - b * s
+    uu = y / x
+    assert np.all(x > 0) and np.abs(uu).max() < 0.0125
+    u2 = uu * uu
+    t = (uu * u2) * ((u2 * (-1 / 7) + 1 / 5) * u2 - 1 / 3) + uu + th
+    t = np.where(t > np.pi, t - 2 * np.pi, np.where(t < -np.pi, t + 2 * np.pi, t))
+    mod = x * (u2 * ((u2 * (1 / 16) - 1 / 8) * u2 + 0.5) + 1.0)
+    ref_t, ref_m = np.abs(np.arctan2(a, b)), np.sqrt(a * a + b * b)
+    assert np.abs(np.abs(t) - ref_t).max() <= 4 * np.spacing(np.pi)
+    assert (np.abs(mod - ref_m) / ref_m).max() <= 4 * np.spacing(1.0)
